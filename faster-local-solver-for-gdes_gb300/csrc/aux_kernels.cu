@@ -1,0 +1,120 @@
+// aux_kernels.cu -- column initialisation, result extraction, graph edits.
+#include <cuda_runtime.h>
+
+#include "gde_common.cuh"
+#include "gde_device.cuh"
+#include "gde_engine.h"
+
+namespace gde {
+
+namespace {
+
+// One warp per column: set the seed's residual (and the Chebyshev start
+// x1 = a e_s, r1 = (1-a) A D^-1 a e_s, ppr_solver.py:587-601; katz_solver.py:
+// 345-355), push `push0` to the seed's neighbours, and append the touched
+// nodes to the tile's round-0 candidate list (deduplicated across columns).
+template <typename T>
+__global__ void init_columns_kernel(PushArgs a, const InitCol* cols, int ncols, int W) {
+    int wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    int lane = threadIdx.x & 31;
+    if (wid >= ncols) return;
+    InitCol ic = cols[wid];
+    const int64_t n = a.g.n;
+    const int64_t base = (int64_t)ic.tile * a.tile_stride;
+    T* R = reinterpret_cast<T*>(a.R) + base;
+    T* X = reinterpret_cast<T*>(a.X) + base;
+    T* DX = a.DX ? reinterpret_cast<T*>(a.DX) + base : nullptr;
+    int32_t* mark = a.mark + (int64_t)ic.tile * n;
+    int32_t* list = a.cand + ((int64_t)ic.tile * 2 + 0) * n;
+    int* cnt = &a.ts[ic.tile].cand_cnt[0];
+    const int stamp = a.ts[ic.tile].stamp;
+    const int64_t so = (int64_t)ic.seed * a.ld + ic.col;
+    if (lane == 0) {
+        R[so] = (T)ic.r0;
+        if (ic.x0 != 0.0) X[so] = (T)ic.x0;
+        if (DX && ic.dx0 != 0.0) DX[so] = (T)ic.dx0;
+    }
+    __syncwarp();
+    append_once(lane == 0, ic.seed, mark, stamp, list, cnt, 0xffffffffu);
+    if (ic.push0 != 0.0) {
+        const int64_t rp = a.g.row_ptr[ic.seed];
+        const int len = a.g.row_len[ic.seed];
+        for (int j0 = 0; j0 < len; j0 += 32) {
+            int j = j0 + lane;
+            bool ok = j < len;
+            int v = ok ? a.g.col[rp + j] : 0;
+            if (ok) atomicAdd(R + (int64_t)v * a.ld + ic.col, (T)ic.push0);
+            append_once(ok, v, mark, stamp, list, cnt, 0xffffffffu);
+        }
+    }
+}
+
+template <typename T, typename O>
+__global__ void extract_kernel(PushArgs a, const ExtractCol* cols, O* x_out, O* r_out, int64_t ld_out, int64_t n,
+                               int clear) {
+    const ExtractCol ec = cols[blockIdx.y];
+    const int64_t base = (int64_t)ec.tile * a.tile_stride + ec.col;
+    T* X = reinterpret_cast<T*>(a.X) + base;
+    T* R = reinterpret_cast<T*>(a.R) + base;
+    T* R2 = a.R2 ? reinterpret_cast<T*>(a.R2) + base : nullptr;
+    const int rl = ec.r_levels;
+    for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t o = u * a.ld;
+        if (x_out) {
+            double x = (double)X[o];
+            if (u == ec.seed) x = x + ec.seed_add;
+            if (ec.scale != 1.0) x = x / ec.scale;
+            x_out[ec.out_row * ld_out + u] = (O)x;
+        }
+        if (r_out) {
+            r_out[ec.out_row * rl * ld_out + u] = (O)R[o];
+            if (rl == 2) r_out[(ec.out_row * rl + 1) * ld_out + u] = R2 ? (O)R2[o] : (O)0;
+        }
+        if (clear) {
+            X[o] = T(0);
+            R[o] = T(0);
+            if (R2) R2[o] = T(0);
+        }
+    }
+}
+
+__global__ void apply_entries_kernel(int32_t* col, const int64_t* pos, const int32_t* val, int64_t k) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x)
+        col[pos[i]] = val[i];
+}
+
+}  // namespace
+
+cudaError_t init_columns(const PushArgs& a, int prec64, int W, const InitCol* d_cols, int ncols, cudaStream_t st) {
+    if (ncols == 0) return cudaSuccess;
+    int blocks = (ncols * 32 + 255) / 256;
+    if (prec64) init_columns_kernel<double><<<blocks, 256, 0, st>>>(a, d_cols, ncols, W);
+    else init_columns_kernel<float><<<blocks, 256, 0, st>>>(a, d_cols, ncols, W);
+    return cudaGetLastError();
+}
+
+cudaError_t extract_columns(const PushArgs& a, int prec64, int W, const ExtractCol* d_cols, int ncols, void* x_out,
+                            void* r_out, int out64, int64_t ld_out, int64_t n, int clear, cudaStream_t st) {
+    if (ncols == 0) return cudaSuccess;
+    int bx = (int)((n + 255) / 256);
+    if (bx > 1024) bx = 1024;
+    dim3 grid(bx, ncols);
+    if (prec64) {
+        if (out64) extract_kernel<double, double><<<grid, 256, 0, st>>>(a, d_cols, (double*)x_out, (double*)r_out, ld_out, n, clear);
+        else extract_kernel<double, float><<<grid, 256, 0, st>>>(a, d_cols, (float*)x_out, (float*)r_out, ld_out, n, clear);
+    } else {
+        if (out64) extract_kernel<float, double><<<grid, 256, 0, st>>>(a, d_cols, (double*)x_out, (double*)r_out, ld_out, n, clear);
+        else extract_kernel<float, float><<<grid, 256, 0, st>>>(a, d_cols, (float*)x_out, (float*)r_out, ld_out, n, clear);
+    }
+    return cudaGetLastError();
+}
+
+cudaError_t graph_apply_entries(int32_t* col, const int64_t* pos, const int32_t* val, int64_t k, cudaStream_t st) {
+    if (k == 0) return cudaSuccess;
+    int blocks = (int)((k + 255) / 256);
+    if (blocks > 4096) blocks = 4096;
+    apply_entries_kernel<<<blocks, 256, 0, st>>>(col, pos, val, k);
+    return cudaGetLastError();
+}
+
+}  // namespace gde

@@ -1,0 +1,937 @@
+// gde_capi.cu -- C ABI: contexts, resident graphs, tile workspaces, solves.
+//
+// Host orchestration of the GB300 push engine.  A solve groups its queries
+// into node x column tiles, initialises the tiles' seeds, runs every tile to
+// completion in one cooperative persistent launch, and extracts the
+// per-query solution rows.  All reference-facing semantics (thresholds,
+// operation counts, the Chebyshev and heat-kernel coefficient tables) are
+// computed here in FP64 exactly as the reference computes them.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <unordered_map>
+#include <vector>
+
+#include "gde_common.cuh"
+#include "gde_engine.h"
+
+using namespace gde;
+
+namespace {
+
+struct DevBuf {
+    void* p = nullptr;
+    size_t bytes = 0;
+};
+
+constexpr int kDefaultMaxRounds = 100000;
+
+}  // namespace
+
+struct gde_ctx {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    int sms = 0;
+    std::string err;
+    GridBarrier* bar = nullptr;
+    int* derr = nullptr;
+    LaunchStats* dstats = nullptr;
+    LaunchStats* hstats = nullptr;  // pinned
+    TileState* hts = nullptr;       // pinned scratch
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    std::map<std::string, DevBuf> ws;
+    std::vector<int> stamp;         // per-tile stamp bases (valid while "mark" is allocated)
+    PlainWork plain{};
+    int64_t plain_n = -1;
+};
+
+struct gde_graph {
+    gde_ctx* ctx = nullptr;
+    DevGraph g{};
+    int64_t* row_ptr = nullptr;
+    int32_t* col = nullptr;
+    int32_t* row_len = nullptr;
+    float* degf = nullptr;
+    double* degd = nullptr;
+    double* nfac = nullptr;
+    double* npush = nullptr;
+    double* tfac = nullptr;
+    float* tfac_f = nullptr;
+    double ign_beta = NAN;
+    std::vector<int64_t> h_indptr;
+    std::vector<int64_t> h_len;
+    std::vector<double> h_deg;
+    bool deg_is_len = true;
+};
+
+namespace {
+
+int fail(gde_ctx* c, int code, const std::string& msg) {
+    if (c) c->err = msg;
+    return code;
+}
+
+int cuda_fail(gde_ctx* c, cudaError_t e, const char* where) {
+    return fail(c, GDE_ECUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                               \
+    do {                                                       \
+        cudaError_t e__ = (call);                              \
+        if (e__ != cudaSuccess) return cuda_fail(ctx, e__, #call); \
+    } while (0)
+
+// Device workspace buffer `name` of at least `bytes` (grown on demand).
+void* wsget(gde_ctx* ctx, const std::string& name, size_t bytes, bool* fresh = nullptr) {
+    DevBuf& b = ctx->ws[name];
+    if (fresh) *fresh = false;
+    if (b.bytes >= bytes && b.p) return b.p;
+    if (b.p) cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+    size_t want = std::max<size_t>(bytes, 256);
+    if (cudaMalloc(&b.p, want) != cudaSuccess) {
+        cudaGetLastError();
+        b.p = nullptr;
+        return nullptr;
+    }
+    b.bytes = want;
+    if (fresh) *fresh = true;
+    return b.p;
+}
+
+void ws_release_all(gde_ctx* ctx) {
+    for (auto& kv : ctx->ws)
+        if (kv.second.p) cudaFree(kv.second.p);
+    ctx->ws.clear();
+}
+
+int64_t estimate_n(double t, double eps) {
+    // hk_solver.py:15-48 (estimate_coefficient / estimate_n) in the same FP64 order
+    double kf = std::ceil(t - 1);
+    int64_t k = (int64_t)kf;
+    double t0 = t;
+    if (k != 0)
+        for (int64_t i = 0; i < k; i++) t0 = t0 * (t / (double)(i + 2));
+    double cur_est = t0 * ((kf + 2.) / (kf + 2. - t));
+    if (cur_est < eps * std::exp(t)) return k;
+    int64_t est_k = k;
+    for (int64_t i = k; i < 1000 * (k + 1); i++) {
+        double tmp = ((kf + 2. - t) * t / std::pow(kf + 2., 2.)) * ((kf + 3.) / (kf + 3. - t));
+        cur_est = cur_est * tmp;
+        est_k += 1;
+        if (cur_est < eps * std::exp(t)) return est_k;
+    }
+    return est_k;
+}
+
+struct Defaults {
+    int small_max = 8, med_max = 2048, chunk = 2048, dense_div = 16;
+};
+
+void fill_tuning(const gde_params* p, PushArgs& a) {
+    Defaults d;
+    a.small_max = p->small_max > 0 ? p->small_max : d.small_max;
+    a.med_max = p->med_max > 0 ? p->med_max : d.med_max;
+    if (a.med_max < a.small_max) a.med_max = a.small_max;
+    a.chunk = p->chunk > 0 ? p->chunk : d.chunk;
+    a.dense_div = p->dense_div > 0 ? p->dense_div : d.dense_div;
+    a.max_rounds = p->max_rounds > 0 ? p->max_rounds : kDefaultMaxRounds;
+}
+
+bool valid_w(int W) { return W == 1 || W == 2 || W == 4 || W == 8 || W == 16 || W == 32; }
+
+// Workspace for `ntiles` tiles of width W over n nodes.
+struct TileWs {
+    PushArgs a{};
+    size_t elem = 0;
+};
+
+int alloc_tiles(gde_ctx* ctx, gde_graph* G, int ntiles, int W, int prec64, bool need_r2, bool need_dx,
+                bool own_slabs, bool kahan, TileWs& tw) {
+    const int64_t n = G->g.n;
+    const size_t es = prec64 ? 8 : 4;
+    const size_t slab = (size_t)ntiles * n * W * es;
+    PushArgs& a = tw.a;
+    a.g = G->g;
+    a.ntiles = ntiles;
+    if (own_slabs) {
+        a.ld = W;
+        a.tile_stride = (int64_t)n * W;
+        a.R = wsget(ctx, "R", slab);
+        a.X = wsget(ctx, "X", slab);
+        if (!a.R || !a.X) return fail(ctx, GDE_ENOMEM, "device memory exhausted (residual/solution slabs)");
+        a.R2 = need_r2 ? wsget(ctx, "R2", slab) : nullptr;
+        a.DX = need_dx ? wsget(ctx, "DX", slab) : nullptr;
+        if ((need_r2 && !a.R2) || (need_dx && !a.DX)) return fail(ctx, GDE_ENOMEM, "device memory exhausted (slabs)");
+    }
+    a.XC = nullptr;
+    a.kahan = 0;
+    if (kahan && !prec64) {
+        size_t xcb = own_slabs ? (size_t)ntiles * n * W * 4 : 0;
+        if (xcb) {
+            a.XC = (float*)wsget(ctx, "XC", xcb);
+            if (!a.XC) return fail(ctx, GDE_ENOMEM, "device memory exhausted (Kahan slab)");
+            a.kahan = 1;
+        }
+    }
+    a.P = wsget(ctx, "P", slab);
+    a.cand = (int32_t*)wsget(ctx, "cand", (size_t)ntiles * 2 * n * 4);
+    a.front = (int32_t*)wsget(ctx, "front", (size_t)ntiles * n * 4);
+    a.bsmall = (int32_t*)wsget(ctx, "bsmall", (size_t)ntiles * n * 4);
+    a.bmed = (int32_t*)wsget(ctx, "bmed", (size_t)ntiles * n * 4);
+    bool fresh = false;
+    a.mark = (int32_t*)wsget(ctx, "mark", (size_t)ntiles * n * 4, &fresh);
+    if (!a.P || !a.cand || !a.front || !a.bsmall || !a.bmed || !a.mark)
+        return fail(ctx, GDE_ENOMEM, "device memory exhausted (frontier lists)");
+    if (fresh) {
+        CK(cudaMemsetAsync(a.mark, 0xff, ctx->ws["mark"].bytes, ctx->stream));
+        ctx->stamp.assign(ctx->ws["mark"].bytes / 4 / std::max<int64_t>(n, 1) + 1, 0);
+    }
+    if ((int)ctx->stamp.size() < ntiles) ctx->stamp.resize(ntiles, 0);
+    tw.elem = es;
+    a.tp = (TileParams*)wsget(ctx, "tp", (size_t)ntiles * sizeof(TileParams));
+    a.ts = (TileState*)wsget(ctx, "ts", (size_t)ntiles * sizeof(TileState));
+    a.cs = (ColState*)wsget(ctx, "cs", (size_t)ntiles * W * sizeof(ColState));
+    if (!a.tp || !a.ts || !a.cs) return fail(ctx, GDE_ENOMEM, "device memory exhausted (tile state)");
+    a.stats = ctx->dstats;
+    a.bar = ctx->bar;
+    a.err = ctx->derr;
+    return GDE_OK;
+}
+
+int alloc_large(gde_ctx* ctx, gde_graph* G, int ntiles, TileWs& tw) {
+    PushArgs& a = tw.a;
+    int64_t cap = G->g.cap;
+    a.large_cap = cap / std::max(a.chunk, 1) + cap / std::max(a.med_max, 1) + 64;
+    a.blarge = (int2*)wsget(ctx, "blarge", (size_t)ntiles * a.large_cap * sizeof(int2));
+    if (!a.blarge) return fail(ctx, GDE_ENOMEM, "device memory exhausted (chunk list)");
+    return GDE_OK;
+}
+
+// Run the persistent engine until every tile is done (or max_rounds).
+int run_engine(gde_ctx* ctx, PushArgs& a, int prec64, int W, gde_stats* st, double* kernel_ms) {
+    int grid = engine_max_grid(prec64, W, ctx->sms);
+    if (grid <= 0) return fail(ctx, GDE_ECUDA, "push kernel does not fit on the device");
+    CK(cudaMemsetAsync(ctx->bar, 0, sizeof(GridBarrier), ctx->stream));
+    CK(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->stream));
+    CK(cudaMemsetAsync(ctx->dstats, 0, sizeof(LaunchStats), ctx->stream));
+    a.round_budget = a.max_rounds + 1;
+    CK(cudaEventRecord(ctx->ev[0], ctx->stream));
+    cudaError_t e = engine_launch(a, prec64, W, grid, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "cooperative launch of the push kernel");
+    CK(cudaEventRecord(ctx->ev[1], ctx->stream));
+    int herr = 0;
+    CK(cudaMemcpyAsync(&herr, ctx->derr, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->hstats, ctx->dstats, sizeof(LaunchStats), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
+    *kernel_ms += ms;
+    if (st) {
+        st->rounds += (int64_t)ctx->hstats->rounds;
+        st->dense_rounds += (int64_t)ctx->hstats->dense_rounds;
+        st->union_vol += ctx->hstats->union_vol;
+        st->col_vol += ctx->hstats->col_vol;
+        st->union_nodes += ctx->hstats->union_nodes;
+        st->col_nodes += ctx->hstats->col_nodes;
+    }
+    if (herr != 0) return fail(ctx, herr, "a device-side wait ran out of iterations (grid barrier)");
+    return GDE_OK;
+}
+
+// Chebyshev coefficient tables (ppr_solver.py:608-609, :636-637; katz_solver.py:366-368)
+std::vector<double> cheby_table(int kind, double alpha, double l_max, double mu_min, int rounds) {
+    std::vector<double> t;
+    if (kind == KIND_KATZ) {
+        double delta = (l_max - mu_min) / (l_max + mu_min);
+        t.resize(2 * (size_t)rounds);
+        for (int i = 0; i < rounds; i++) {
+            delta = 1. / (2. * ((l_max + mu_min) / (l_max - mu_min)) - delta);
+            t[2 * i] = 4. * delta / (l_max - mu_min);
+            t[2 * i + 1] = (1. - 2. * delta * (l_max + mu_min) / (l_max - mu_min));
+        }
+    } else {
+        double delta = (1. - alpha);
+        t.resize(rounds);
+        for (int i = 0; i < rounds; i++) {
+            delta = 1. / (2. / (1. - alpha) - delta);
+            t[i] = 2. * delta / (1. - alpha);
+        }
+    }
+    return t;
+}
+
+// psi table of hk_sor_queue (hk_solver.py:226-229)
+std::vector<double> psi_table(double tau, int64_t N) {
+    std::vector<double> psi(N + 2, 1.0);
+    psi[N] = 1.;
+    for (int64_t i = N - 1; i >= 0; i--) psi[i] = psi[i + 1] * tau / ((double)i + 1.) + 1.;
+    return psi;
+}
+
+int upload_ign_tables(gde_ctx* ctx, gde_graph* G, double beta) {
+    const int64_t n = G->g.n;
+    std::vector<double> nf(n), tf(n);
+    std::vector<float> tff(n);
+    for (int64_t u = 0; u < n; u++) {
+        double d = G->h_deg[u];
+        nf[u] = std::pow(d, 1 - beta);  // np.power(degree, 1 - beta), InstantGNN.py:57
+        tf[u] = std::pow(d, beta);      // degree[v] ** beta, InstantGNN.py:31
+        tff[u] = (float)tf[u];
+    }
+    if (!G->nfac) {
+        CK(cudaMalloc(&G->nfac, n * 8));
+        CK(cudaMalloc(&G->tfac, n * 8));
+        CK(cudaMalloc(&G->tfac_f, n * 4));
+    }
+    CK(cudaMemcpyAsync(G->nfac, nf.data(), n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(G->tfac, tf.data(), n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(G->tfac_f, tff.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    G->npush = G->nfac;
+    G->g.nfac = G->nfac;
+    G->g.npush = G->nfac;
+    G->g.tfac = G->tfac;
+    G->g.tfac_f = G->tfac_f;
+    G->ign_beta = beta;
+    return GDE_OK;
+}
+
+int upload_degrees(gde_ctx* ctx, gde_graph* G) {
+    const int64_t n = G->g.n;
+    std::vector<int32_t> len(n);
+    std::vector<float> df(n);
+    double vol = 0;
+    for (int64_t u = 0; u < n; u++) {
+        len[u] = (int32_t)G->h_len[u];
+        df[u] = (float)G->h_deg[u];
+        vol += G->h_deg[u];
+    }
+    CK(cudaMemcpyAsync(G->row_len, len.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(G->degd, G->h_deg.data(), n * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(G->degf, df.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    G->g.vol = vol;
+    return GDE_OK;
+}
+
+}  // namespace
+
+// ===========================================================================
+// C ABI
+// ===========================================================================
+extern "C" {
+
+const char* gde_status_str(int s) {
+    switch (s) {
+        case GDE_OK: return "ok";
+        case GDE_EINVAL: return "invalid argument";
+        case GDE_ENOMEM: return "out of memory";
+        case GDE_EITERCAP: return "round cap reached";
+        case GDE_ECUDA: return "CUDA error";
+        case GDE_EHANG: return "device-side wait ran out";
+        case GDE_ECAPACITY: return "padded row out of slack";
+        case GDE_ENOTFOUND: return "not found";
+    }
+    return "unknown status";
+}
+
+int gde_version(void) { return 1; }
+
+int gde_ctx_create(int device, gde_ctx** out) {
+    if (!out) return GDE_EINVAL;
+    *out = nullptr;
+    gde_ctx* ctx = new gde_ctx();
+    ctx->device = device;
+    cudaError_t e = cudaSetDevice(device);
+    if (e != cudaSuccess) { delete ctx; return GDE_ECUDA; }
+    int coop = 0;
+    cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, device);
+    cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
+    if (!coop) { delete ctx; return GDE_ECUDA; }
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
+        cudaMalloc(&ctx->bar, sizeof(GridBarrier)) != cudaSuccess ||
+        cudaMalloc(&ctx->derr, sizeof(int)) != cudaSuccess ||
+        cudaMalloc(&ctx->dstats, sizeof(LaunchStats)) != cudaSuccess ||
+        cudaMallocHost(&ctx->hstats, sizeof(LaunchStats)) != cudaSuccess ||
+        cudaMallocHost(&ctx->hts, sizeof(TileState) * 4096) != cudaSuccess) {
+        delete ctx;
+        return GDE_ECUDA;
+    }
+    for (auto& ev : ctx->ev) cudaEventCreate(&ev);
+    *out = ctx;
+    return GDE_OK;
+}
+
+int gde_ctx_destroy(gde_ctx* ctx) {
+    if (!ctx) return GDE_EINVAL;
+    cudaSetDevice(ctx->device);
+    cudaStreamSynchronize(ctx->stream);
+    ws_release_all(ctx);
+    if (ctx->plain_n >= 0) {
+        cudaFree(ctx->plain.xt); cudaFree(ctx->plain.rt); cudaFree(ctx->plain.tmp); cudaFree(ctx->plain.sp);
+        cudaFree(ctx->plain.eps_vec); cudaFree(ctx->plain.queue); cudaFree(ctx->plain.nz);
+        cudaFree(ctx->plain.d_count); cudaFree(ctx->plain.d_oper); cudaFreeHost(ctx->plain.h_count);
+    }
+    cudaFree(ctx->bar);
+    cudaFree(ctx->derr);
+    cudaFree(ctx->dstats);
+    cudaFreeHost(ctx->hstats);
+    cudaFreeHost(ctx->hts);
+    for (auto& ev : ctx->ev) cudaEventDestroy(ev);
+    cudaStreamDestroy(ctx->stream);
+    delete ctx;
+    return GDE_OK;
+}
+
+const char* gde_last_error(gde_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
+
+int gde_ctx_sync(gde_ctx* ctx) {
+    if (!ctx) return GDE_EINVAL;
+    CK(cudaStreamSynchronize(ctx->stream));
+    return GDE_OK;
+}
+
+int64_t gde_hk_estimate_n(double tau, double eps) {
+    if (!(tau >= 1.0) || !(eps > 0.0)) return -1;  // hk_solver.py:35-36
+    return estimate_n(tau, eps);
+}
+
+int gde_graph_upload(gde_ctx* ctx, int64_t n, int64_t cap, const int64_t* indptr, const int32_t* indices,
+                     const int64_t* row_len, const double* degree, gde_graph** out) {
+    if (!ctx || !out || n <= 0 || !indptr || !indices || cap < 0) return fail(ctx, GDE_EINVAL, "bad graph arguments");
+    if (n >= (int64_t)1 << 31) return fail(ctx, GDE_EINVAL, "node ids must fit in int32");
+    *out = nullptr;
+    CK(cudaSetDevice(ctx->device));
+    gde_graph* G = new gde_graph();
+    G->ctx = ctx;
+    G->h_indptr.assign(indptr, indptr + n + 1);
+    G->h_len.resize(n);
+    G->h_deg.resize(n);
+    for (int64_t u = 0; u < n; u++) {
+        int64_t len = row_len ? row_len[u] : indptr[u + 1] - indptr[u];
+        if (len < 0 || indptr[u] + len > cap || (u + 1 <= n && indptr[u] + len > indptr[u + 1])) {
+            delete G;
+            return fail(ctx, GDE_EINVAL, "row " + std::to_string(u) + " exceeds its CSR extent");
+        }
+        G->h_len[u] = len;
+        G->h_deg[u] = degree ? degree[u] : (double)len;
+        if (degree && degree[u] != (double)len) G->deg_is_len = false;
+    }
+    G->g.n = n;
+    G->g.cap = cap;
+    // row_ptr gets two spare entries so aligned 16-byte windows stay in bounds
+    cudaError_t e = cudaMalloc(&G->row_ptr, (n + 3) * sizeof(int64_t));
+    if (e == cudaSuccess) e = cudaMalloc(&G->col, std::max<int64_t>(cap, 1) * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&G->row_len, n * sizeof(int32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&G->degf, n * sizeof(float));
+    if (e == cudaSuccess) e = cudaMalloc(&G->degd, n * sizeof(double));
+    if (e != cudaSuccess) {
+        cudaFree(G->row_ptr); cudaFree(G->col); cudaFree(G->row_len); cudaFree(G->degf); cudaFree(G->degd);
+        delete G;
+        return fail(ctx, GDE_ENOMEM, "device memory exhausted (graph)");
+    }
+    CK(cudaMemsetAsync(G->row_ptr, 0, (n + 3) * sizeof(int64_t), ctx->stream));
+    CK(cudaMemcpyAsync(G->row_ptr, indptr, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
+    if (cap > 0) CK(cudaMemcpyAsync(G->col, indices, cap * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    G->g.row_ptr = G->row_ptr;
+    G->g.col = G->col;
+    G->g.row_len = G->row_len;
+    G->g.degf = G->degf;
+    G->g.degd = G->degd;
+    int rc = upload_degrees(ctx, G);
+    if (rc != GDE_OK) { gde_graph_free(G); return rc; }
+    *out = G;
+    return GDE_OK;
+}
+
+int gde_graph_free(gde_graph* G) {
+    if (!G) return GDE_EINVAL;
+    cudaSetDevice(G->ctx->device);
+    cudaStreamSynchronize(G->ctx->stream);
+    cudaFree(G->row_ptr); cudaFree(G->col); cudaFree(G->row_len); cudaFree(G->degf); cudaFree(G->degd);
+    cudaFree(G->nfac); cudaFree(G->tfac); cudaFree(G->tfac_f);
+    delete G;
+    return GDE_OK;
+}
+
+int gde_graph_info(gde_graph* G, int64_t* n, int64_t* cap, double* vol) {
+    if (!G) return GDE_EINVAL;
+    if (n) *n = G->g.n;
+    if (cap) *cap = G->g.cap;
+    if (vol) *vol = G->g.vol;
+    return GDE_OK;
+}
+
+int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const int32_t* seeds, const double* eps,
+              void* x_out, void* r_out, int out64, int out_mem, int64_t ld_out, double* oper_out, int32_t* rounds_out,
+              gde_stats* stats) {
+    if (!ctx || !G || !p || nq < 0 || (nq > 0 && (!seeds || !eps))) return fail(ctx, GDE_EINVAL, "bad solve arguments");
+    CK(cudaSetDevice(ctx->device));
+    const int64_t n = G->g.n;
+    const int kind = p->kind, method = p->method;
+    const int prec64 = (p->prec == GDE_FP64);
+    if (kind != KIND_PPR && kind != KIND_KATZ && kind != KIND_HK) return fail(ctx, GDE_EINVAL, "kind must be PPR, KATZ or HK");
+    const bool hk = method_is_hk(method);
+    if (hk != (kind == KIND_HK)) return fail(ctx, GDE_EINVAL, "heat-kernel methods go with GDE_HK only");
+    if (method < M_LOCAL_GD || method > M_HK_TAYLOR) return fail(ctx, GDE_EINVAL, "unknown method");
+    if (ld_out < n && (x_out || r_out)) return fail(ctx, GDE_EINVAL, "ld_out < n");
+    for (int64_t q = 0; q < nq; q++) {
+        if (seeds[q] < 0 || seeds[q] >= n) return fail(ctx, GDE_EINVAL, "seed out of range");
+        if (!(eps[q] > 0.0)) return fail(ctx, GDE_EINVAL, "eps must be > 0");
+        if (kind == KIND_PPR && (method == M_LOCAL_GD || method == M_GLOBAL_GD) && !(eps[q] * G->h_deg[seeds[q]] <= 1.))
+            return fail(ctx, GDE_EINVAL, "eps * degree[s_node] > 1 (ppr_solver.py:213)");
+    }
+    if (hk && !(p->tau >= 1.0)) return fail(ctx, GDE_EINVAL, "tau must be >= 1 (hk_solver.py:35)");
+    if (stats) memset(stats, 0, sizeof(*stats));
+    if (nq == 0) return GDE_OK;
+
+    int W = p->tile_w;
+    if (W <= 0) W = (nq == 1) ? 1 : (prec64 ? 4 : 8);
+    while (W > 1 && W > nq * 2) W >>= 1;
+    if (!valid_w(W)) return fail(ctx, GDE_EINVAL, "tile_w must be 1, 2, 4, 8, 16 or 32");
+
+    // Group queries into tiles.  HK tiles never mix Taylor lengths.
+    std::vector<int64_t> order(nq);
+    for (int64_t q = 0; q < nq; q++) order[q] = q;
+    std::vector<int64_t> Nq(nq, 0);
+    if (hk) {
+        for (int64_t q = 0; q < nq; q++)
+            Nq[q] = (method == M_HK_TAYLOR) ? estimate_n(p->tau, eps[q]) : estimate_n(p->tau, .5 * eps[q]);
+        std::stable_sort(order.begin(), order.end(), [&](int64_t a, int64_t b) { return Nq[a] < Nq[b]; });
+    }
+    struct TileDef { std::vector<int64_t> qs; int64_t N; };
+    std::vector<TileDef> tiles;
+    for (int64_t i = 0; i < nq;) {
+        TileDef td;
+        td.N = Nq[order[i]];
+        while (i < nq && (int)td.qs.size() < W && Nq[order[i]] == td.N) td.qs.push_back(order[i++]);
+        tiles.push_back(td);
+    }
+
+    // Memory per tile; launch groups sized to the free device memory.
+    const size_t es = prec64 ? 8 : 4;
+    size_t per_tile = (size_t)n * W * es * (3 + (hk ? 1 : 0) + (method_is_cheby(method) ? 1 : 0)) +
+                      (size_t)n * W * (prec64 ? 0 : 4) + (size_t)n * 4 * 6 + 4096;
+    size_t freeb = 0, totalb = 0;
+    cudaMemGetInfo(&freeb, &totalb);
+    size_t have = 0;
+    for (auto& kv : ctx->ws) have += kv.second.bytes;
+    size_t budget = (size_t)((double)(freeb + have) * 0.85);
+    int max_tiles = (int)std::min<size_t>(4096, std::max<size_t>(1, budget / std::max<size_t>(per_tile, 1)));
+
+    PushArgs base{};
+    fill_tuning(p, base);
+    const double m_vol = G->g.vol;
+    double kernel_ms = 0.0;
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+
+    // per-launch tables
+    std::vector<double> ctab;
+    if (method_is_cheby(method)) ctab = cheby_table(kind, p->alpha, p->l_max, p->mu_min, base.max_rounds + 2);
+    std::map<int64_t, std::vector<double>> psis;
+    if (hk)
+        for (auto& td : tiles)
+            if (!psis.count(td.N)) {
+                if (method == M_HK_TAYLOR) psis[td.N] = std::vector<double>(td.N + 2, 1.0);
+                else psis[td.N] = psi_table(p->tau, td.N);
+            }
+    double* d_ctab = nullptr;
+    if (!ctab.empty()) {
+        d_ctab = (double*)wsget(ctx, "ctab", ctab.size() * 8);
+        if (!d_ctab) return fail(ctx, GDE_ENOMEM, "coefficient table");
+        CK(cudaMemcpyAsync(d_ctab, ctab.data(), ctab.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    }
+    std::map<int64_t, double*> d_psi;
+    if (hk) {
+        size_t tot = 0;
+        for (auto& kv : psis) tot += kv.second.size();
+        double* buf = (double*)wsget(ctx, "psi", tot * 8);
+        if (!buf) return fail(ctx, GDE_ENOMEM, "psi table");
+        size_t off = 0;
+        for (auto& kv : psis) {
+            CK(cudaMemcpyAsync(buf + off, kv.second.data(), kv.second.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+            d_psi[kv.first] = buf + off;
+            off += kv.second.size();
+        }
+    }
+
+    for (size_t t0 = 0; t0 < tiles.size(); t0 += max_tiles) {
+        const int nt = (int)std::min<size_t>(max_tiles, tiles.size() - t0);
+        TileWs tw;
+        tw.a = base;
+        int rc = alloc_tiles(ctx, G, nt, W, prec64, hk, method_is_cheby(method), true, !prec64, tw);
+        if (rc != GDE_OK) return rc;
+        PushArgs& a = tw.a;
+        a.small_max = base.small_max; a.med_max = base.med_max; a.chunk = base.chunk;
+        a.dense_div = base.dense_div; a.max_rounds = base.max_rounds;
+        rc = alloc_large(ctx, G, nt, tw);
+        if (rc != GDE_OK) return rc;
+        const size_t slab = (size_t)nt * n * W * es;
+        CK(cudaMemsetAsync(a.R, 0, slab, ctx->stream));
+        CK(cudaMemsetAsync(a.X, 0, slab, ctx->stream));
+        if (a.R2) CK(cudaMemsetAsync(a.R2, 0, slab, ctx->stream));
+        if (a.DX) CK(cudaMemsetAsync(a.DX, 0, slab, ctx->stream));
+        if (a.XC) CK(cudaMemsetAsync(a.XC, 0, (size_t)nt * n * W * 4, ctx->stream));
+        std::vector<TileParams> tp(nt);
+        std::vector<TileState> ts(nt);
+        std::vector<ColState> cs((size_t)nt * W);
+        std::vector<InitCol> ic;
+        std::vector<ExtractCol> ec;
+        for (int t = 0; t < nt; t++) {
+            const TileDef& td = tiles[t0 + t];
+            TileParams& P = tp[t];
+            memset(&P, 0, sizeof(P));
+            P.kind = kind;
+            P.method = method;
+            P.ncols = (int)td.qs.size();
+            P.n_levels = (int)td.N;
+            P.alpha = p->alpha;
+            P.tau = p->tau;
+            P.l_max = p->l_max;
+            P.mu_min = p->mu_min;
+            P.x_gain = 1.0;
+            P.coef_tab = d_ctab;
+            P.psi_tab = hk ? d_psi[td.N] : nullptr;
+            TileState& S = ts[t];
+            memset(&S, 0, sizeof(S));
+            S.dense_next[0] = method_is_global(method) ? 1 : 0;
+            S.stamp = ctx->stamp[t];
+            for (int c = 0; c < W; c++) {
+                ColState& C = cs[(size_t)t * W + c];
+                memset(&C, 0, sizeof(C));
+                C.seed = -1;
+                if (c >= P.ncols) continue;
+                int64_t q = td.qs[c];
+                C.live = 1;
+                C.seed = seeds[q];
+                if (kind == KIND_PPR) C.theta = eps[q] * p->alpha;      // eps * alpha * degree
+                else if (kind == KIND_KATZ) C.theta = eps[q];            // eps * degree
+                else C.theta = std::exp(p->tau) * eps[q];                // np.exp(tau) * eps * degree / est_n
+                InitCol I{};
+                I.tile = t;
+                I.col = c;
+                I.seed = seeds[q];
+                const double ds = G->h_deg[seeds[q]];
+                if (method_is_cheby(method)) {
+                    if (kind == KIND_KATZ) {
+                        I.x0 = 2. / (p->l_max + p->mu_min);
+                        I.dx0 = I.x0;
+                        I.r0 = 1. - 2. / (p->l_max + p->mu_min);
+                        I.push0 = 2. * p->alpha / (p->l_max + p->mu_min);
+                    } else {
+                        I.x0 = p->alpha;
+                        I.dx0 = p->alpha;
+                        I.r0 = 0.0;
+                        I.push0 = (1. - p->alpha) * p->alpha / ds;
+                    }
+                } else {
+                    I.r0 = (kind == KIND_PPR) ? p->alpha : 1.0;
+                }
+                ic.push_back(I);
+                ExtractCol E{};
+                E.tile = t;
+                E.col = c;
+                E.out_row = q;
+                E.seed = (kind == KIND_KATZ && (method == M_LOCAL_GD || method == M_GLOBAL_GD)) ? seeds[q] : -1;
+                E.seed_add = -1.0;  // xt[s_node] -= 1. (katz_solver.py:243)
+                E.scale = hk ? std::exp(p->tau) : 1.0;  // xt /= np.exp(tau)
+                E.r_levels = (hk && method != M_HK_TAYLOR) ? 2 : 1;
+                ec.push_back(E);
+            }
+        }
+        CK(cudaMemcpyAsync(a.tp, tp.data(), nt * sizeof(TileParams), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(a.ts, ts.data(), nt * sizeof(TileState), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(a.cs, cs.data(), cs.size() * sizeof(ColState), cudaMemcpyHostToDevice, ctx->stream));
+        InitCol* d_ic = (InitCol*)wsget(ctx, "initcols", ic.size() * sizeof(InitCol));
+        ExtractCol* d_ec = (ExtractCol*)wsget(ctx, "extcols", ec.size() * sizeof(ExtractCol));
+        if (!d_ic || !d_ec) return fail(ctx, GDE_ENOMEM, "column tables");
+        CK(cudaMemcpyAsync(d_ic, ic.data(), ic.size() * sizeof(InitCol), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(d_ec, ec.data(), ec.size() * sizeof(ExtractCol), cudaMemcpyHostToDevice, ctx->stream));
+        CK(init_columns(a, prec64, W, d_ic, (int)ic.size(), ctx->stream));
+        rc = run_engine(ctx, a, prec64, W, stats, &kernel_ms);
+        if (rc != GDE_OK) return rc;
+        // results
+        const size_t oes = out64 ? 8 : 4;
+        const int rl = (hk && method != M_HK_TAYLOR) ? 2 : 1;
+        if (out_mem == GDE_MEM_DEVICE) {
+            CK(extract_columns(a, prec64, W, d_ec, (int)ec.size(), x_out, r_out, out64, ld_out, n, 0, ctx->stream));
+        } else if (x_out || r_out) {
+            // stage through device memory in chunks of columns
+            size_t row_b = (size_t)ld_out * oes;
+            int64_t per = std::max<int64_t>(1, (int64_t)((size_t)512 << 20) / (int64_t)(row_b * (1 + rl)));
+            for (size_t e0 = 0; e0 < ec.size(); e0 += per) {
+                size_t ne = std::min<size_t>(per, ec.size() - e0);
+                std::vector<ExtractCol> sub(ec.begin() + e0, ec.begin() + e0 + ne);
+                for (size_t i = 0; i < ne; i++) sub[i].out_row = (int64_t)i;
+                ExtractCol* d_sub = (ExtractCol*)wsget(ctx, "extsub", ne * sizeof(ExtractCol));
+                void* sx = x_out ? wsget(ctx, "stage_x", ne * row_b) : nullptr;
+                void* sr = r_out ? wsget(ctx, "stage_r", ne * row_b * rl) : nullptr;
+                if (!d_sub || (x_out && !sx) || (r_out && !sr)) return fail(ctx, GDE_ENOMEM, "staging buffers");
+                CK(cudaMemcpyAsync(d_sub, sub.data(), ne * sizeof(ExtractCol), cudaMemcpyHostToDevice, ctx->stream));
+                CK(extract_columns(a, prec64, W, d_sub, (int)ne, sx, sr, out64, ld_out, n, 0, ctx->stream));
+                for (size_t i = 0; i < ne; i++) {
+                    int64_t q = ec[e0 + i].out_row;
+                    if (x_out)
+                        CK(cudaMemcpyAsync((char*)x_out + q * row_b, (char*)sx + i * row_b, row_b,
+                                           cudaMemcpyDeviceToHost, ctx->stream));
+                    if (r_out)
+                        CK(cudaMemcpyAsync((char*)r_out + q * row_b * rl, (char*)sr + i * row_b * rl, row_b * rl,
+                                           cudaMemcpyDeviceToHost, ctx->stream));
+                }
+            }
+        }
+        // per-column counters and stamp bookkeeping
+        std::vector<ColState> hcs(cs.size());
+        CK(cudaMemcpyAsync(hcs.data(), a.cs, cs.size() * sizeof(ColState), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->hts, a.ts, nt * sizeof(TileState), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        bool capped = false;
+        for (int t = 0; t < nt; t++) {
+            const TileState& S = ctx->hts[t];
+            ctx->stamp[t] = S.stamp + S.round + base.max_rounds + 4;
+            if (!S.done) capped = true;
+            const TileDef& td = tiles[t0 + t];
+            for (int c = 0; c < (int)td.qs.size(); c++) {
+                const ColState& C = hcs[(size_t)t * W + c];
+                int64_t q = td.qs[c];
+                double oper;
+                if (method == M_GLOBAL_GD || method == M_GLOBAL_CHEBY) oper = (double)C.rounds * ((double)n + m_vol);
+                else if (method == M_HK_GLOBAL) oper = (double)C.rounds * (m_vol + (double)n);
+                else if (method == M_HK_TAYLOR) oper = 0.0;
+                else oper = C.oper;
+                if (oper_out) oper_out[q] = oper;
+                if (rounds_out) rounds_out[q] = C.rounds;
+            }
+        }
+        if (stats) { stats->tiles += nt; stats->tile_w = W; }
+        if (capped) {
+            CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+            return fail(ctx, GDE_EITERCAP, "max_rounds reached before the stopping rule held");
+        }
+    }
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+    CK(cudaEventSynchronize(ctx->ev[3]));
+    if (stats) {
+        float tot = 0.f;
+        cudaEventElapsedTime(&tot, ctx->ev[2], ctx->ev[3]);
+        stats->total_ms = tot;
+        stats->kernel_ms = kernel_ms;
+    }
+    return GDE_OK;
+}
+
+// ---------------------------------------------------------------------------
+// Feature push (InstantGNN)
+// ---------------------------------------------------------------------------
+static int feature_push_impl(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t F, void* Pm, void* Rm,
+                             int64_t ld, double eps, const int32_t* cand, int64_t ncand, bool cand_on_device,
+                             double* oper_out, gde_stats* stats) {
+    const int64_t n = G->g.n;
+    const int prec64 = (p->prec == GDE_FP64);
+    const int kind = p->kind;
+    if (kind != KIND_IGN && kind != KIND_UPPR) return fail(ctx, GDE_EINVAL, "feature push needs GDE_IGN or GDE_UPPR");
+    if (F <= 0 || ld < F || !Pm || !Rm) return fail(ctx, GDE_EINVAL, "bad feature matrix arguments");
+    if (!(eps > 0.0)) return fail(ctx, GDE_EINVAL, "eps must be > 0");
+    if (kind == KIND_IGN && (std::isnan(G->ign_beta) || G->ign_beta != p->beta)) {
+        int rc = upload_ign_tables(ctx, G, p->beta);
+        if (rc != GDE_OK) return rc;
+    }
+    int W = p->tile_w;
+    if (W <= 0) W = prec64 ? 8 : 16;
+    while (W > 1 && (F % W != 0 || ld % W != 0)) W >>= 1;
+    if (!valid_w(W)) return fail(ctx, GDE_EINVAL, "tile_w must be 1, 2, 4, 8, 16 or 32");
+    const int nt_total = (int)(F / W);
+    PushArgs base{};
+    fill_tuning(p, base);
+    double kernel_ms = 0.0;
+    if (stats) memset(stats, 0, sizeof(*stats));
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+    // Kahan compensation matrix for an FP32 solution
+    float* XCm = nullptr;
+    if (!prec64) {
+        XCm = (float*)wsget(ctx, "XCf", (size_t)n * ld * 4);
+        if (!XCm) return fail(ctx, GDE_ENOMEM, "Kahan matrix");
+        CK(cudaMemsetAsync(XCm, 0, (size_t)n * ld * 4, ctx->stream));
+    }
+    // tiles per launch bounded by workspace memory
+    size_t per_tile = (size_t)n * W * (prec64 ? 8 : 4) + (size_t)n * 4 * 6 + 4096;
+    size_t freeb = 0, totalb = 0;
+    cudaMemGetInfo(&freeb, &totalb);
+    int max_tiles = (int)std::min<size_t>(4096, std::max<size_t>(1, (size_t)(freeb * 0.8) / per_tile));
+    for (int t0 = 0; t0 < nt_total; t0 += max_tiles) {
+        const int nt = std::min(max_tiles, nt_total - t0);
+        TileWs tw;
+        tw.a = base;
+        int rc = alloc_tiles(ctx, G, nt, W, prec64, false, false, false, false, tw);
+        if (rc != GDE_OK) return rc;
+        PushArgs& a = tw.a;
+        rc = alloc_large(ctx, G, nt, tw);
+        if (rc != GDE_OK) return rc;
+        const size_t es = prec64 ? 8 : 4;
+        a.ld = (int)ld;
+        a.tile_stride = W;
+        a.R = (char*)Rm + (size_t)t0 * W * es;
+        a.X = (char*)Pm + (size_t)t0 * W * es;
+        a.R2 = nullptr;
+        a.DX = nullptr;
+        if (XCm) { a.XC = XCm + (size_t)t0 * W; a.kahan = 1; }
+        std::vector<TileParams> tp(nt);
+        std::vector<TileState> ts(nt);
+        std::vector<ColState> cs((size_t)nt * W);
+        for (int t = 0; t < nt; t++) {
+            TileParams& P = tp[t];
+            memset(&P, 0, sizeof(P));
+            P.kind = kind;
+            P.method = M_LOCAL_GD;
+            P.ncols = W;
+            P.alpha = p->alpha;
+            P.beta = p->beta;
+            P.x_gain = (kind == KIND_IGN) ? p->alpha : 1.0;
+            TileState& S = ts[t];
+            memset(&S, 0, sizeof(S));
+            S.stamp = ctx->stamp[t];
+            S.dense_next[0] = cand ? 0 : 1;
+            S.cand_cnt[0] = cand ? (int)ncand : 0;
+            for (int c = 0; c < W; c++) {
+                ColState& C = cs[(size_t)t * W + c];
+                memset(&C, 0, sizeof(C));
+                C.live = 1;
+                C.seed = -1;
+                C.theta = (kind == KIND_IGN) ? eps : p->alpha * eps;  // pow(d,1-b)*eps ; alpha*eps*degree
+            }
+        }
+        if (cand) {
+            for (int t = 0; t < nt; t++) {
+                int32_t* dst = a.cand + ((int64_t)t * 2 + 0) * n;
+                CK(cudaMemcpyAsync(dst, cand, ncand * 4, cand_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice,
+                                   ctx->stream));
+            }
+        }
+        CK(cudaMemcpyAsync(a.tp, tp.data(), nt * sizeof(TileParams), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(a.ts, ts.data(), nt * sizeof(TileState), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(a.cs, cs.data(), cs.size() * sizeof(ColState), cudaMemcpyHostToDevice, ctx->stream));
+        rc = run_engine(ctx, a, prec64, W, stats, &kernel_ms);
+        if (rc != GDE_OK) return rc;
+        std::vector<ColState> hcs(cs.size());
+        CK(cudaMemcpyAsync(hcs.data(), a.cs, cs.size() * sizeof(ColState), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaMemcpyAsync(ctx->hts, a.ts, nt * sizeof(TileState), cudaMemcpyDeviceToHost, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));
+        bool capped = false;
+        for (int t = 0; t < nt; t++) {
+            ctx->stamp[t] = ctx->hts[t].stamp + ctx->hts[t].round + base.max_rounds + 4;
+            if (!ctx->hts[t].done) capped = true;
+            for (int c = 0; c < W; c++)
+                if (oper_out) oper_out[(int64_t)(t0 + t) * W + c] = hcs[(size_t)t * W + c].oper;
+        }
+        if (stats) { stats->tiles += nt; stats->tile_w = W; }
+        if (capped) return fail(ctx, GDE_EITERCAP, "max_rounds reached before the stopping rule held");
+    }
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+    CK(cudaEventSynchronize(ctx->ev[3]));
+    if (stats) {
+        float tot = 0.f;
+        cudaEventElapsedTime(&tot, ctx->ev[2], ctx->ev[3]);
+        stats->total_ms = tot;
+        stats->kernel_ms = kernel_ms;
+    }
+    return GDE_OK;
+}
+
+int gde_feature_push(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t F, void* Pm, void* Rm, int64_t ld,
+                     double eps, const int32_t* cand, int64_t ncand, double* oper_out, gde_stats* stats) {
+    if (!ctx || !G || !p) return fail(ctx, GDE_EINVAL, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    if (cand)
+        for (int64_t i = 0; i < ncand; i++)
+            if (cand[i] < 0 || cand[i] >= G->g.n) return fail(ctx, GDE_EINVAL, "candidate out of range");
+    return feature_push_impl(ctx, G, p, F, Pm, Rm, ld, eps, cand, ncand, false, oper_out, stats);
+}
+
+int gde_plain_ppr_local(gde_ctx* ctx, gde_graph* G, int32_t seed, double alpha, double eps, float* x_out,
+                        float* r_out, double* oper_out, int32_t* rounds_out) {
+    if (!ctx || !G || seed < 0 || seed >= G->g.n || !(eps > 0)) return fail(ctx, GDE_EINVAL, "bad arguments");
+    CK(cudaSetDevice(ctx->device));
+    const int64_t n = G->g.n;
+    if (ctx->plain_n != n) {
+        if (ctx->plain_n >= 0) {
+            cudaFree(ctx->plain.xt); cudaFree(ctx->plain.rt); cudaFree(ctx->plain.tmp); cudaFree(ctx->plain.sp);
+            cudaFree(ctx->plain.eps_vec); cudaFree(ctx->plain.queue); cudaFree(ctx->plain.nz);
+            cudaFree(ctx->plain.d_count); cudaFree(ctx->plain.d_oper); cudaFreeHost(ctx->plain.h_count);
+        }
+        PlainWork& w = ctx->plain;
+        int64_t nb = (n + 255) / 256 + 1;
+        CK(cudaMalloc(&w.xt, n * 4));
+        CK(cudaMalloc(&w.rt, n * 4));
+        CK(cudaMalloc(&w.tmp, n * 4));
+        CK(cudaMalloc(&w.sp, n * 4));
+        CK(cudaMalloc(&w.eps_vec, n * 4));
+        CK(cudaMalloc(&w.queue, n * 4));
+        CK(cudaMalloc(&w.nz, nb * 4));
+        CK(cudaMalloc(&w.d_count, 4));
+        CK(cudaMalloc(&w.d_oper, 8));
+        CK(cudaMallocHost(&w.h_count, 4));
+        ctx->plain_n = n;
+    }
+    ctx->plain.degf = G->degf;
+    double oper = 0;
+    int rounds = 0;
+    int rc = plain_ppr_local(G->g, ctx->plain, seed, alpha, eps, &oper, &rounds, ctx->stream);
+    if (rc != GDE_OK) return fail(ctx, rc, "plain baseline failed");
+    if (x_out) CK(cudaMemcpyAsync(x_out, ctx->plain.xt, n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (r_out) CK(cudaMemcpyAsync(r_out, ctx->plain.rt, n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (oper_out) *oper_out = oper;
+    if (rounds_out) *rounds_out = rounds;
+    return GDE_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Internals shared with graph_edit.cu
+// ---------------------------------------------------------------------------
+int gde_internal_feature_push(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t F, void* Pm, void* Rm,
+                              int64_t ld, double eps, const int32_t* d_cand, int64_t ncand, double* oper_out,
+                              gde_stats* stats) {
+    return feature_push_impl(ctx, G, p, F, Pm, Rm, ld, eps, d_cand, ncand, true, oper_out, stats);
+}
+
+int gde_internal_graph_refresh(gde_ctx* ctx, gde_graph* G, const int64_t* h_degree, const int64_t* pos,
+                               const int32_t* val, int64_t nchg, double beta, int ign) {
+    if (nchg > 0) {
+        int64_t* d_pos = (int64_t*)wsget(ctx, "edit_pos", nchg * 8);
+        int32_t* d_val = (int32_t*)wsget(ctx, "edit_val", nchg * 4);
+        if (!d_pos || !d_val) return fail(ctx, GDE_ENOMEM, "edit buffers");
+        CK(cudaMemcpyAsync(d_pos, pos, nchg * 8, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(d_val, val, nchg * 4, cudaMemcpyHostToDevice, ctx->stream));
+        CK(graph_apply_entries(G->col, d_pos, d_val, nchg, ctx->stream));
+    }
+    for (int64_t u = 0; u < G->g.n; u++) {
+        G->h_len[u] = h_degree[u];
+        G->h_deg[u] = (double)h_degree[u];
+    }
+    int rc = upload_degrees(ctx, G);
+    if (rc != GDE_OK) return rc;
+    if (ign) return upload_ign_tables(ctx, G, beta);
+    return GDE_OK;
+}
+
+int gde_internal_graph_host(gde_graph* G, const int64_t** indptr, const int64_t** len, int64_t* n) {
+    *indptr = G->h_indptr.data();
+    *len = G->h_len.data();
+    *n = G->g.n;
+    return GDE_OK;
+}
+
+void* gde_internal_wsget(gde_ctx* ctx, const char* name, size_t bytes) { return wsget(ctx, name, bytes); }
+int gde_internal_fail(gde_ctx* ctx, int code, const char* msg) { return fail(ctx, code, msg); }
+cudaStream_t gde_internal_stream(gde_ctx* ctx) { return ctx->stream; }
+const double* gde_internal_npush(gde_graph* G) { return G->nfac; }
+const double* gde_internal_degd(gde_graph* G) { return G->degd; }

@@ -1,0 +1,162 @@
+// gde_common.cuh -- shared device/host definitions of the GB300 local push engine.
+//
+// The engine solves graph diffusion equations (PPR, Katz, heat kernel,
+// InstantGNN feature propagation) by synchronous local push over a symmetric
+// CSR graph.  Work is organised in *tiles*: a tile holds W solution columns
+// (queries or feature columns) laid out node-major (element (u,c) at
+// slab[u*ld + c]) so that one edge push moves W contiguous values with vector
+// atomics, and the graph's column indices are read once per tile.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "../../include/gde.h"
+
+namespace gde {
+
+// ---------------------------------------------------------------------------
+// Problem kinds and methods (per tile)
+// ---------------------------------------------------------------------------
+enum Kind : int {
+    KIND_PPR = 0,   // Q = I - (1-a) A D^-1, b = a e_s          (ppr_solver.py:18-23)
+    KIND_KATZ = 1,  // Q = I - a A,          b = e_s            (katz_solver.py:177-179)
+    KIND_HK = 2,    // Taylor-truncated heat kernel levels     (hk_solver.py:206-295)
+    KIND_IGN = 3,   // generalised PPR with exponent beta      (InstantGNN.py:12-43)
+    KIND_UPPR = 4,  // dynamic PPR update push, beta = 0 form  (ppr_solver.py:769-821)
+};
+
+enum Method : int {
+    M_LOCAL_GD = 0,     // synchronous local push (LocalGD)
+    M_GLOBAL_GD = 1,    // every node with r != 0 pushes each iteration
+    M_LOCAL_CHEBY = 2,  // Chebyshev three-term recurrence on active nodes
+    M_GLOBAL_CHEBY = 3,
+    M_HK_LOCAL = 4,     // level-synchronous heat-kernel push (omega = 1)
+    M_HK_GLOBAL = 5,    // every level sweeps all nodes
+    M_HK_TAYLOR = 6,    // global Taylor series (hk_taylor_approx)
+};
+
+__host__ __device__ inline bool method_is_global(int m) {
+    return m == M_GLOBAL_GD || m == M_GLOBAL_CHEBY || m == M_HK_GLOBAL || m == M_HK_TAYLOR;
+}
+__host__ __device__ inline bool method_is_cheby(int m) { return m == M_LOCAL_CHEBY || m == M_GLOBAL_CHEBY; }
+__host__ __device__ inline bool method_is_hk(int m) { return m == M_HK_LOCAL || m == M_HK_GLOBAL || m == M_HK_TAYLOR; }
+
+// ---------------------------------------------------------------------------
+// Device graph
+// ---------------------------------------------------------------------------
+struct DevGraph {
+    int64_t n;
+    int64_t cap;              // capacity of col[] (nnz, or padded capacity)
+    const int64_t* row_ptr;   // [n+2]; row u occupies col[row_ptr[u] .. row_ptr[u]+row_len[u])
+    const int32_t* col;       // [cap]
+    const int32_t* row_len;   // [n] live entries per row
+    const float* degf;        // [n] arithmetic degree (exact for integer degrees < 2^24)
+    const double* degd;       // [n] arithmetic degree in FP64
+    const double* nfac;       // [n] InstantGNN threshold factor d^(1-beta) (nullptr otherwise)
+    const double* npush;      // [n] InstantGNN push divisor d^(1-beta)
+    const double* tfac;       // [n] InstantGNN target divisor d^beta
+    const float* tfac_f;      // [n] same, FP32
+    double vol;               // sum of degrees (m)
+};
+
+// ---------------------------------------------------------------------------
+// Per-tile state
+// ---------------------------------------------------------------------------
+constexpr int kMaxW = 32;
+
+struct TileParams {           // host-written, read-only during a launch
+    int kind, method;
+    int ncols;                // live column slots (<= W)
+    int n_levels;             // HK: N (levels 0..N-1), Taylor: N (levels 0..N)
+    double alpha, tau;
+    double l_max, mu_min;     // Katz Chebyshev spectral bounds
+    double beta;              // InstantGNN exponent
+    double x_gain;            // InstantGNN: p += x_gain * r (alpha); dynamic PPR: 1
+    const double* coef_tab;   // Chebyshev: beta_t (PPR) or (beta1_t, beta2_t) pairs (Katz), per round
+    const double* psi_tab;    // HK: psi[0..N]
+    int64_t seed_base;        // unused by the kernel (bookkeeping)
+};
+
+// Counter discipline (no phase ever reads a field another block writes in
+// the same phase).  Round r of a tile has level = ts.round + it, parity
+// p = level & 1:
+//   PREP(r)    reads cand_cnt[r%3]; writes front/small/med/large/union_vol[p],
+//              round_active[p]; appends (Chebyshev) to cand_cnt[(r+1)%3];
+//              block 0 zeroes the p^1 counters and cand_cnt[(r+2)%3].
+//   SCATTER(r) reads the p counters; appends to cand_cnt[(r+1)%3]; block 0
+//              writes ts.done / dense_next[p^1] / ColState.live, which are
+//              only read at the start of the next round.
+struct TileState {            // device-updated
+    int cand_cnt[3];          // candidate list sizes (by level mod 3)
+    int front_cnt[2];         // frontier sizes (by parity)
+    int small_cnt[2], med_cnt[2], large_cnt[2];
+    int dense_next[2];        // 1: the PREP of that parity scans all nodes
+    int round;                // rounds completed before the current launch
+    int done;                 // 1 when every column finished
+    int stamp;                // touch-stamp base (marks start at -1; stamps only grow)
+    int pad;
+    double union_vol[2];      // volume of the union frontier per round parity
+};
+
+struct ColState {             // one per column slot
+    double theta;             // threshold scale (eps*alpha, eps, e^tau*eps, eps ...)
+    double oper;              // operation count (sum of degrees of pushed nodes)
+    int64_t fsum;             // sum over rounds of frontier size
+    int live;                 // 1 while the column still has active nodes
+    int rounds;               // rounds in which the column pushed
+    int round_active[2];      // active nodes this round (parity)
+    int check_cnt[2];         // global methods: nodes above threshold (parity)
+    int seed;                 // seed node (-1 for feature columns)
+    int pad;
+};
+
+struct LaunchStats {          // roofline counters summed over a launch
+    unsigned long long union_nodes;    // sum_t |U S_t| (per tile)
+    double union_vol;                  // sum_t vol(U S_t)
+    unsigned long long col_nodes;      // sum_t sum_c |S_t^c|
+    double col_vol;                    // sum_t sum_c vol(S_t^c)
+    unsigned long long dense_rounds;
+    unsigned long long rounds;
+    unsigned long long cand_nodes;     // candidates examined
+};
+
+struct GridBarrier {
+    unsigned int count;
+    unsigned int gen;
+};
+
+// Engine launch parameters (passed by value to the persistent kernel).
+struct PushArgs {
+    DevGraph g;
+    int ntiles;
+    int ld;                    // row stride of the slabs (elements)
+    int64_t tile_stride;       // element offset between consecutive tiles' slabs
+    void* R;                   // residual slab (levels 0,2,4.. for HK)
+    void* R2;                  // HK odd-level residual slab
+    void* X;                   // solution slab
+    float* XC;                 // Kahan compensation (FP32 solution), may be null
+    void* DX;                  // Chebyshev delta-x slab
+    int32_t* cand;             // [ntiles][2][n] (list storage by parity)
+    int32_t* front;            // [ntiles][n]
+    void* P;                   // [ntiles][n][W] push rows
+    int32_t* bsmall;           // [ntiles][n]
+    int32_t* bmed;             // [ntiles][n]
+    int2* blarge;              // [ntiles][large_cap]
+    int64_t large_cap;
+    int32_t* mark;             // [ntiles][n]
+    TileParams* tp;            // [ntiles]
+    TileState* ts;             // [ntiles]
+    ColState* cs;              // [ntiles][W]
+    LaunchStats* stats;
+    GridBarrier* bar;
+    int* err;
+    int small_max;             // rows with len <= small_max: lane group per row
+    int med_max;               // rows with len <= med_max: warp per row; else CTA chunks
+    int chunk;                 // edges per CTA chunk (large rows)
+    int dense_div;             // frontier volume > n/dense_div -> next round scans densely
+    int max_rounds;            // hard cap on a tile's rounds
+    int round_budget;          // rounds to advance in this launch (serving ticks)
+    int kahan;                 // compensated FP32 solution
+};
+
+}  // namespace gde

@@ -1,0 +1,49 @@
+// gde_engine.h -- internal interface between the C-ABI layer and the kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include "gde_common.cuh"
+
+namespace gde {
+
+// Persistent push engine (push_engine.cu).
+int engine_max_grid(int prec64, int W, int sms);
+cudaError_t engine_launch(const PushArgs& a, int prec64, int W, int grid, cudaStream_t st);
+
+// Column initialisation and result extraction (aux_kernels.cu).
+struct InitCol {
+    int tile, col;      // slot
+    int seed;           // seed node
+    double r0;          // residual at the seed
+    double x0;          // solution at the seed (Chebyshev)
+    double dx0;         // delta-x at the seed (Chebyshev)
+    double push0;       // value pushed to every neighbour of the seed (Chebyshev), 0 = none
+};
+cudaError_t init_columns(const PushArgs& a, int prec64, int W, const InitCol* d_cols, int ncols, cudaStream_t st);
+
+struct ExtractCol {
+    int tile, col;      // slot
+    int64_t out_row;    // row of the output matrices
+    int seed;           // node whose solution gets `seed_add` (Katz GD: -1)
+    double seed_add;
+    double scale;       // solution divided by this (HK: e^tau), 1 otherwise
+    int r_levels;       // 2: HK residual [2, n] output, 1 otherwise
+};
+cudaError_t extract_columns(const PushArgs& a, int prec64, int W, const ExtractCol* d_cols, int ncols, void* x_out,
+                            void* r_out, int out64, int64_t ld_out, int64_t n, int clear, cudaStream_t st);
+
+// Plain single-query baseline (plain.cu).
+struct PlainWork {
+    float *xt, *rt, *tmp, *sp, *eps_vec, *degf;
+    int32_t *queue, *nz;
+    int *d_count;
+    double *d_oper;
+    int *h_count;      // pinned
+};
+int plain_ppr_local(const DevGraph& g, PlainWork& w, int seed, double alpha, double eps, double* oper,
+                    int* rounds, cudaStream_t st);
+
+// Graph helpers (aux_kernels.cu).
+cudaError_t graph_apply_entries(int32_t* col, const int64_t* pos, const int32_t* val, int64_t k, cudaStream_t st);
+
+}  // namespace gde

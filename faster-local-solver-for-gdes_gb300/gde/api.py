@@ -1,0 +1,200 @@
+"""Python host API over the C ABI: contexts, resident graphs, batched solves.
+
+This is the layer the drop-in modules (``ppr_solver``, ``katz_solver``,
+``hk_solver``, ``InstantGNN``) and the benchmark call.  Device buffers are
+torch tensors (plumbing only); every solver runs in ``libgde.so``.
+"""
+from __future__ import annotations
+
+import ctypes
+import weakref
+
+import numpy as np
+
+from . import _lib as L
+
+_PREC = {"fp64": L.FP64, "fp32": L.FP32}
+
+
+def _ptr(a) -> int | None:
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()  # torch tensor
+
+
+class Context:
+    """One CUDA device + stream + workspace of the library (``gde_ctx``)."""
+
+    _by_device: dict[int, "Context"] = {}
+
+    def __init__(self, device: int = 0):
+        lib = L.load()
+        h = ctypes.c_void_p()
+        st = lib.gde_ctx_create(device, ctypes.byref(h))
+        if st != L.GDE_OK:
+            raise L.GDEError(st, f"gde_ctx_create(device={device}) failed: {lib.gde_status_str(st).decode()}")
+        self.ptr = h.value
+        self.device = device
+        self._fin = weakref.finalize(self, lib.gde_ctx_destroy, h.value)
+
+    @classmethod
+    def get(cls, device: int = 0) -> "Context":
+        c = cls._by_device.get(device)
+        if c is None:
+            c = cls._by_device[device] = Context(device)
+        return c
+
+    def close(self) -> None:
+        self._fin()
+
+
+class Graph:
+    """A CSR graph resident in device memory (``gde_graph``).
+
+    ``row_len`` = live entries per row (padded InstantGNN CSR); default is the
+    row-pointer difference.  ``degree`` = arithmetic degree used in the
+    formulas; default is the row length.
+    """
+
+    def __init__(self, indptr, indices, row_len=None, degree=None, ctx: Context | None = None):
+        self.ctx = ctx or Context.get(0)
+        lib = L.load()
+        indptr = np.ascontiguousarray(indptr, dtype=np.int64)
+        indices = np.ascontiguousarray(indices, dtype=np.int32)
+        n = indptr.shape[0] - 1
+        rl = None if row_len is None else np.ascontiguousarray(row_len, dtype=np.int64)
+        dg = None if degree is None else np.ascontiguousarray(degree, dtype=np.float64)
+        h = ctypes.c_void_p()
+        st = lib.gde_graph_upload(self.ctx.ptr, n, indices.shape[0], _ptr(indptr), _ptr(indices), _ptr(rl), _ptr(dg),
+                                  ctypes.byref(h))
+        L.check(self.ctx.ptr, st, "gde_graph_upload")
+        self.ptr = h.value
+        self.n = int(n)
+        self.cap = int(indices.shape[0])
+        vol = ctypes.c_double()
+        lib.gde_graph_info(self.ptr, None, None, ctypes.byref(vol))
+        self.vol = float(vol.value)
+        self._fin = weakref.finalize(self, lib.gde_graph_free, h.value)
+
+    def free(self) -> None:
+        self._fin()
+
+
+def make_params(kind: int, method: int, prec: str = "fp64", tile_w: int = 0, alpha: float = 0.0, tau: float = 0.0,
+                l_max: float = 0.0, mu_min: float = 0.0, beta: float = 0.0, omega: float = 1.0, max_rounds: int = 0,
+                tuning: dict | None = None) -> L.Params:
+    p = L.Params()
+    p.kind, p.method, p.prec, p.tile_w = kind, method, _PREC[prec], tile_w
+    p.alpha, p.tau, p.l_max, p.mu_min, p.beta, p.omega = alpha, tau, l_max, mu_min, beta, omega
+    p.max_rounds = max_rounds
+    t = tuning or {}
+    p.small_max = int(t.get("small_max", 0))
+    p.med_max = int(t.get("med_max", 0))
+    p.chunk = int(t.get("chunk", 0))
+    p.dense_div = int(t.get("dense_div", 0))
+    return p
+
+
+def solve(graph: Graph, kind: int, method: int, seeds, eps, *, prec: str = "fp64", out64: bool | None = None,
+          want_x: bool = True, want_r: bool = True, x_out=None, r_out=None, device_out: bool = False,
+          tile_w: int = 0, alpha: float = 0.0, tau: float = 0.0, l_max: float = 0.0, mu_min: float = 0.0,
+          max_rounds: int = 0, tuning: dict | None = None) -> dict:
+    """Solve one query per seed; returns dict(x, r, oper, rounds, stats).
+
+    ``x_out`` / ``r_out`` may be caller buffers (numpy / torch, host or
+    device per ``device_out``) of shape [nq, n] (HK residual: [nq, 2, n]).
+    """
+    lib = L.load()
+    seeds = np.ascontiguousarray(np.atleast_1d(seeds), dtype=np.int32)
+    nq = seeds.shape[0]
+    eps = np.ascontiguousarray(np.broadcast_to(np.asarray(eps, dtype=np.float64), (nq,)))
+    if out64 is None:
+        out64 = prec == "fp64"
+    n = graph.n
+    rl = 2 if (kind == L.HK and method != L.HK_TAYLOR) else 1
+    odt = np.float64 if out64 else np.float32
+    if want_x and x_out is None:
+        if device_out:
+            import torch
+            x_out = torch.empty((nq, n), dtype=torch.float64 if out64 else torch.float32,
+                                device=f"cuda:{graph.ctx.device}")
+        else:
+            x_out = np.empty((nq, n), dtype=odt)
+    if want_r and r_out is None:
+        shape = (nq, rl, n) if rl == 2 else (nq, n)
+        if device_out:
+            import torch
+            r_out = torch.empty(shape, dtype=torch.float64 if out64 else torch.float32,
+                                device=f"cuda:{graph.ctx.device}")
+        else:
+            r_out = np.empty(shape, dtype=odt)
+    oper = np.zeros(nq, dtype=np.float64)
+    rounds = np.zeros(nq, dtype=np.int32)
+    p = make_params(kind, method, prec, tile_w, alpha, tau, l_max, mu_min, max_rounds=max_rounds, tuning=tuning)
+    st = L.Stats()
+    status = lib.gde_solve(graph.ctx.ptr, graph.ptr, ctypes.byref(p), nq, _ptr(seeds), _ptr(eps),
+                           _ptr(x_out) if want_x else None, _ptr(r_out) if want_r else None, int(out64),
+                           L.MEM_DEVICE if device_out else L.MEM_HOST, n, _ptr(oper), _ptr(rounds), ctypes.byref(st))
+    L.check(graph.ctx.ptr, status, "gde_solve")
+    return {"x": x_out if want_x else None, "r": r_out if want_r else None, "oper": oper, "rounds": rounds,
+            "stats": st.as_dict()}
+
+
+def feature_push(graph: Graph, kind: int, P, R, eps: float, *, alpha: float, beta: float = 0.0, prec: str = "fp64",
+                 cand=None, tile_w: int = 0, max_rounds: int = 0, tuning: dict | None = None) -> dict:
+    """Multi-column push on device matrices P, R ([n, F] torch tensors), in place."""
+    lib = L.load()
+    F = int(P.shape[1])
+    ld = int(P.stride(0))
+    assert R.stride(0) == ld and P.is_cuda and R.is_cuda
+    p = make_params(kind, L.LOCAL_GD, prec, tile_w, alpha=alpha, beta=beta, max_rounds=max_rounds, tuning=tuning)
+    oper = np.zeros(F, dtype=np.float64)
+    st = L.Stats()
+    c = None if cand is None else np.ascontiguousarray(cand, dtype=np.int32)
+    status = lib.gde_feature_push(graph.ctx.ptr, graph.ptr, ctypes.byref(p), F, _ptr(P), _ptr(R), ld, eps, _ptr(c),
+                                  0 if c is None else c.shape[0], _ptr(oper), ctypes.byref(st))
+    L.check(graph.ctx.ptr, status, "gde_feature_push")
+    return {"oper": oper, "stats": st.as_dict()}
+
+
+def feature_update(graph: Graph, kind: int, h_indices: np.ndarray, h_degree: np.ndarray, us, vs, only_insert: bool,
+                   P, R, X, eps: float, *, alpha: float, beta: float = 0.0, prec: str = "fp64", tile_w: int = 0,
+                   max_rounds: int = 0) -> dict:
+    """Edge batch + repair + push (device P, R, X; host graph arrays mutated in place)."""
+    lib = L.load()
+    assert h_indices.dtype == np.int32 and h_degree.dtype == np.int64
+    assert h_indices.flags.c_contiguous and h_degree.flags.c_contiguous
+    us = np.ascontiguousarray(us, dtype=np.int32)
+    vs = np.ascontiguousarray(vs, dtype=np.int32)
+    F = int(P.shape[1])
+    ld = int(P.stride(0))
+    p = make_params(kind, L.LOCAL_GD, prec, tile_w, alpha=alpha, beta=beta, max_rounds=max_rounds)
+    oper = np.zeros(F, dtype=np.float64)
+    st = L.Stats()
+    status = lib.gde_feature_update(graph.ctx.ptr, graph.ptr, _ptr(h_indices), _ptr(h_degree), _ptr(us), _ptr(vs),
+                                    us.shape[0], int(only_insert), ctypes.byref(p), F, _ptr(P), _ptr(R), _ptr(X), ld,
+                                    eps, _ptr(oper), ctypes.byref(st))
+    L.check(graph.ctx.ptr, status, "gde_feature_update")
+    return {"oper": oper, "stats": st.as_dict()}
+
+
+def plain_ppr_local(graph: Graph, seed: int, alpha: float, eps: float, x_out=None, r_out=None):
+    """The plain single-query baseline (structure of ppr_gd_local_gpu)."""
+    lib = L.load()
+    oper = ctypes.c_double()
+    rounds = ctypes.c_int32()
+    status = lib.gde_plain_ppr_local(graph.ctx.ptr, graph.ptr, int(seed), alpha, eps, _ptr(x_out), _ptr(r_out),
+                                     ctypes.byref(oper), ctypes.byref(rounds))
+    L.check(graph.ctx.ptr, status, "gde_plain_ppr_local")
+    return oper.value, rounds.value
+
+
+def hk_estimate_n(tau: float, eps: float) -> int:
+    return int(L.load().gde_hk_estimate_n(tau, eps))
+
+
+def sync(ctx: Context | None = None) -> None:
+    c = ctx or Context.get(0)
+    L.check(c.ptr, L.load().gde_ctx_sync(c.ptr), "gde_ctx_sync")

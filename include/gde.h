@@ -1,0 +1,173 @@
+/*
+ * gde.h -- C ABI of the GB300 local push solvers for graph diffusion equations.
+ *
+ * Plain C types only (pointers, sizes, doubles); no CUDA or PyTorch types.
+ * Every entry point returns a gde_status (0 = GDE_OK); gde_last_error()
+ * gives the message of the last failure on a context.  Pointers marked
+ * "host" are ordinary CPU memory; pointers marked "device" are CUDA device
+ * memory on the context's device.  Calls on one context are serialised on
+ * the context's CUDA stream; distinct contexts may be used from distinct
+ * threads.
+ *
+ * The reference exposes these operations as Python functions
+ * (ppr_solver.py, katz_solver.py, hk_solver.py, InstantGNN.py); each entry
+ * point below names the functions it replaces.  The ctypes binding used by
+ * the drop-in Python modules is shown in INTEGRATION.md.
+ */
+#ifndef GDE_H_
+#define GDE_H_
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes (the reference reports failures only by `assert`) ---- */
+#define GDE_OK 0
+#define GDE_EINVAL 1     /* bad argument (e.g. eps*degree[s] > 1, ppr_solver.py:213) */
+#define GDE_ENOMEM 2     /* device memory or the admission budget is exhausted */
+#define GDE_EITERCAP 3   /* max_rounds reached before the stopping rule held */
+#define GDE_ECUDA 4      /* a CUDA call failed */
+#define GDE_EHANG 5      /* a bounded device-side wait ran out (kernel returned early) */
+#define GDE_ECAPACITY 6  /* a padded CSR row has no slack left for an insertion */
+#define GDE_ENOTFOUND 7  /* unknown query id */
+
+/* ---- problem kinds and methods ---- */
+#define GDE_PPR 0   /* (I - (1-a) A D^-1) x = a e_s   (ppr_solver.py:18-23) */
+#define GDE_KATZ 1  /* (I - a A) x = e_s              (katz_solver.py:177-179) */
+#define GDE_HK 2    /* heat kernel Taylor levels      (hk_solver.py:206-295) */
+#define GDE_IGN 3   /* InstantGNN feature push        (InstantGNN.py:12-43) */
+#define GDE_UPPR 4  /* dynamic PPR update push        (ppr_solver.py:769-821) */
+
+#define GDE_LOCAL_GD 0
+#define GDE_GLOBAL_GD 1
+#define GDE_LOCAL_CHEBY 2
+#define GDE_GLOBAL_CHEBY 3
+#define GDE_HK_LOCAL 4
+#define GDE_HK_GLOBAL 5
+#define GDE_HK_TAYLOR 6
+
+#define GDE_FP64 0
+#define GDE_FP32 1  /* FP32 residuals, Kahan-compensated FP32 solution, FP64 threshold tests */
+
+#define GDE_MEM_HOST 0
+#define GDE_MEM_DEVICE 1
+
+typedef struct gde_ctx gde_ctx;
+typedef struct gde_graph gde_graph;
+typedef struct gde_server gde_server;
+
+typedef struct {
+    int kind;          /* GDE_PPR / GDE_KATZ / GDE_HK */
+    int method;        /* GDE_LOCAL_GD ... GDE_HK_TAYLOR */
+    int prec;          /* GDE_FP64 / GDE_FP32 */
+    int tile_w;        /* columns per tile (1,2,4,8,16,32); 0 = autotuned choice */
+    double alpha;      /* PPR / Katz alpha */
+    double tau;        /* heat-kernel temperature */
+    double l_max;      /* Katz Chebyshev spectral bounds (katz_solver.py:341) */
+    double mu_min;
+    double beta;       /* InstantGNN exponent */
+    double omega;      /* accepted for SOR-style entry points; the synchronous push uses omega = 1 */
+    int max_rounds;    /* 0 = default (100000) */
+    int small_max;     /* degree buckets: <= small_max lane group per row, 0 = default */
+    int med_max;       /* <= med_max warp per row, else CTA chunks; 0 = default */
+    int chunk;         /* edges per CTA chunk; 0 = default */
+    int dense_div;     /* next round scans all nodes when vol(frontier) > n/dense_div; 0 = default */
+} gde_params;
+
+typedef struct {
+    double kernel_ms;           /* device time of the push launches */
+    double total_ms;            /* device time of the whole call */
+    int64_t rounds;             /* sum over tiles of rounds run */
+    int64_t dense_rounds;
+    double union_vol;           /* sum_t vol(union frontier)   -> col_idx bytes */
+    double col_vol;             /* sum_t sum_c vol(S_t^c)      -> residual update bytes */
+    uint64_t union_nodes;       /* sum_t |union frontier| */
+    uint64_t col_nodes;         /* sum_t sum_c |S_t^c| */
+    int tiles;
+    int tile_w;
+} gde_stats;
+
+/* ---- context / errors ---- */
+const char *gde_status_str(int status);
+int gde_version(void);
+int gde_ctx_create(int device, gde_ctx **out);
+int gde_ctx_destroy(gde_ctx *ctx);
+const char *gde_last_error(gde_ctx *ctx);
+int gde_ctx_sync(gde_ctx *ctx);
+
+/* ---- graph ----
+ * Uploads a CSR graph.  Row u's neighbours are indices[indptr[u] ..
+ * indptr[u]+row_len[u]); row_len == NULL means indptr[u+1]-indptr[u] (the
+ * static layout of ppr_solver.py / katz_solver.py / hk_solver.py); a padded
+ * InstantGNN CSR passes its degree array (data_process_GNN.py:93-119).
+ * degree == NULL uses the row length as the arithmetic degree (the
+ * reference's adj.sum(1), demo.py:44).  `cap` is the length of indices.
+ * Replaces the per-call cp.asarray upload of ppr_gd_local_gpu
+ * (ppr_solver.py:103-105) with a resident graph. */
+int gde_graph_upload(gde_ctx *ctx, int64_t n, int64_t cap, const int64_t *indptr, const int32_t *indices,
+                     const int64_t *row_len, const double *degree, gde_graph **out);
+int gde_graph_free(gde_graph *g);
+int gde_graph_info(gde_graph *g, int64_t *n, int64_t *cap, double *volume);
+
+/* ---- batched single-seed solves ----
+ * Solves nq queries (seed[q], eps[q]) of one kind/method in node x column
+ * tiles.  Replaces, per query:
+ *   ppr_gd(local=True/False)           ppr_solver.py:208-328  (GDE_PPR, LOCAL_GD/GLOBAL_GD, FP64)
+ *   ppr_gd_local_gpu / _standard_gpu   ppr_solver.py:82-146, :26-79 (FP32)
+ *   ppr_cheby(local=True/False)        ppr_solver.py:582-661  (LOCAL_CHEBY/GLOBAL_CHEBY)
+ *   katz_gd, katz_gd_*_gpu             katz_solver.py:167-248, :24-146
+ *   katz_cheby                         katz_solver.py:340-431
+ *   hk_sor_queue(omega=1)              hk_solver.py:206-295   (HK_LOCAL/HK_GLOBAL)
+ *   hk_taylor_approx                   hk_solver.py:51-80     (HK_TAYLOR)
+ * x_out / r_out (may be NULL) receive nq rows of ld_out values each (HK
+ * r_out: 2 rows per query, the two level buffers of hk_solver.py:212),
+ * FP64 when out64 else FP32, in host or device memory per out_mem.
+ * seeds / eps are host arrays.  oper_out / rounds_out (host, may be NULL)
+ * receive the reference's operation count and the rounds per query. */
+int gde_solve(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t nq, const int32_t *seeds, const double *eps,
+              void *x_out, void *r_out, int out64, int out_mem, int64_t ld_out, double *oper_out,
+              int32_t *rounds_out, gde_stats *stats);
+
+/* heat-kernel Taylor length, hk_solver.py:28-48 (estimate_n) */
+int64_t gde_hk_estimate_n(double tau, double eps);
+
+/* ---- multi-column feature push (InstantGNN) ----
+ * P, R: device n x F matrices (row stride ld, FP64 if prec == GDE_FP64 else
+ * FP32), updated in place.  Columns start with candidates = every node
+ * (instantGNNParallel's initial scan, InstantGNN.py:59-63) when cand == NULL,
+ * else the host list cand[0..ncand).  kind GDE_IGN: p += alpha r,
+ * r_v += (1-alpha) r_u / d_u^(1-beta) / d_v^beta, threshold d^(1-beta) eps;
+ * kind GDE_UPPR (beta = 0): p += r, threshold alpha eps d.
+ * Replaces instantGNNParallel / instantGNNSorParallel (InstantGNN.py:46-134);
+ * oper_out (host, may be NULL) receives per-column operation counts. */
+int gde_feature_push(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t F, void *P, void *R, int64_t ld,
+                     double eps, const int32_t *cand, int64_t ncand, double *oper_out, gde_stats *stats);
+
+/* ---- dynamic graph update + incremental feature push ----
+ * Applies the edge batch (us[i], vs[i]) to the padded CSR exactly as
+ * updetaGraph does (InstantGNN.py:137-180; insertion only when only_insert,
+ * else existing edges are deleted), mutating the caller's host arrays
+ * h_indices / h_degree in place and the device copy of the graph; repairs
+ * P, R at the touched nodes from X (InstantGNN.py:303-318, kind GDE_IGN) or
+ * with the beta = 0 rule (ppr_solver.py:776-792, kind GDE_UPPR); then
+ * pushes from the repaired nodes.  Replaces instantGNNUpdateBatchParallel
+ * (InstantGNN.py:332-359) and update_ppr_parallel (ppr_solver.py:824-849).
+ * X may be NULL for GDE_UPPR. */
+int gde_feature_update(gde_ctx *ctx, gde_graph *g, int32_t *h_indices, int64_t *h_degree, const int32_t *us,
+                       const int32_t *vs, int64_t k, int only_insert, const gde_params *p, int64_t F, void *P,
+                       void *R, const void *X, int64_t ld, double eps, double *oper_out, gde_stats *stats);
+
+/* ---- plain single-query baseline ----
+ * The structure of ppr_gd_local_gpu (ppr_solver.py:82-146) on this GPU:
+ * thread-per-row atomic kernel, O(n) passes and a host sync every round.
+ * x_out / r_out: device FP32 [n] (may be NULL).  Benchmark denominator. */
+int gde_plain_ppr_local(gde_ctx *ctx, gde_graph *g, int32_t seed, double alpha, double eps, float *x_out,
+                        float *r_out, double *oper_out, int32_t *rounds_out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* GDE_H_ */

@@ -711,13 +711,20 @@ void orc_update_graph(i64 n, const i64 *indptr, i32 *indices, i64 *degree, const
     free(ev_del);
 }
 
+i64 orc_ign_sync_column(i64 n, const i64 *indptr, const i32 *indices, const i64 *degree, double alpha,
+                        double x_gain, const double *eps_vec, double beta, double *p, double *r, i64 cs,
+                        const unsigned char *cand0, i64 max_rounds);
+
 /* instantGNNUpdateBatch for one column (InstantGNN.py:298-329).  p, r, x are
- * columns with stride cs; the maps are the outputs of orc_update_graph. */
-void orc_ign_update_column(i64 n, const i64 *indptr, const i32 *indices, const i64 *degree, const i64 *old_degree,
-                           double *p, double *r, const double *x, i64 cs, double alpha, double eps, double omega,
-                           int sor, int insert_only, double beta, const i64 *ins_keys, const i64 *ins_off,
-                           const i64 *ins_nbr, i64 n_ins, const i64 *del_keys, const i64 *del_off,
-                           const i64 *del_nbr, i64 n_del) {
+ * columns with stride cs; the maps are the outputs of orc_update_graph.
+ * sync=1 keeps the reference's repair and replaces the FIFO push with the
+ * synchronous push (candidates = the repaired nodes); returns its oper. */
+i64 orc_ign_update_column(i64 n, const i64 *indptr, const i32 *indices, const i64 *degree, const i64 *old_degree,
+                          double *p, double *r, const double *x, i64 cs, double alpha, double eps, double omega,
+                          int sor, int insert_only, double beta, const i64 *ins_keys, const i64 *ins_off,
+                          const i64 *ins_nbr, i64 n_ins, const i64 *del_keys, const i64 *del_off,
+                          const i64 *del_nbr, i64 n_del, int sync) {
+    i64 sync_oper = 0;
     double *eps_vec = (double *)malloc((size_t)n * sizeof(double));
     double *pc = (double *)malloc((size_t)n * sizeof(double));
     double *rc = (double *)malloc((size_t)n * sizeof(double));
@@ -757,9 +764,16 @@ void orc_ign_update_column(i64 n, const i64 *indptr, const i32 *indices, const i
             q_mark[u] = 1;
         }
     }
-    if (rear != front)
+    if (sync) {
+        unsigned char *cand0 = (unsigned char *)calloc((size_t)n, 1);
+        for (i64 t = 0; t < n_ins; t++) cand0[ins_keys[t]] = 1;
+        sync_oper = orc_ign_sync_column(n, indptr, indices, degree, alpha, alpha, eps_vec, beta, pc, rc, 1, cand0,
+                                        (i64)1 << 40);
+        free(cand0);
+    } else if (rear != front) {
         ign_push(n + 2, indptr, indices, degree, alpha, eps_vec, omega, sor, NULL, pc, rc, queue, front, rear,
                  q_mark, beta);
+    }
     for (i64 i = 0; i < n; i++) { p[i * cs] = pc[i]; r[i * cs] = rc[i]; }
     free(eps_vec);
     free(pc);
@@ -767,13 +781,14 @@ void orc_ign_update_column(i64 n, const i64 *indptr, const i32 *indices, const i
     free(queue);
     free(q_mark);
     free(del_slot);
+    return sync_oper;
 }
 
 /* update_ppr for one feature row (ppr_solver.py:769-821). */
 i64 orc_update_ppr_row(i64 n, const i64 *indptr, const i32 *indices, const i64 *degree, const i64 *old_degree,
                        double *p, double *r, double alpha, double eps, double omega, const i64 *ins_keys,
                        const i64 *ins_off, const i64 *ins_nbr, i64 n_ins, const i64 *del_keys, const i64 *del_off,
-                       const i64 *del_nbr, i64 n_del) {
+                       const i64 *del_nbr, i64 n_del, int sync) {
     double *eps_vec = (double *)malloc((size_t)n * sizeof(double));
     i64 *queue = (i64 *)calloc((size_t)n + 2, sizeof(i64));
     unsigned char *q_mark = (unsigned char *)calloc((size_t)n, 1);
@@ -810,6 +825,14 @@ i64 orc_update_ppr_row(i64 n, const i64 *indptr, const i32 *indices, const i64 *
             queue[rear] = u;
             q_mark[u] = 1;
         }
+    }
+    if (sync) {
+        unsigned char *cand0 = (unsigned char *)calloc((size_t)n, 1);
+        for (i64 t = 0; t < n_ins; t++) cand0[ins_keys[t]] = 1;
+        oper += orc_ign_sync_column(n, indptr, indices, degree, alpha, 1.0, eps_vec, 0.0, p, r, 1, cand0,
+                                    (i64)1 << 40);
+        free(cand0);
+        rear = front;  /* skip the FIFO push */
     }
     while (rear != front) {
         front = (front + 1) % qn;
@@ -856,8 +879,8 @@ i64 orc_update_ppr_row(i64 n, const i64 *indptr, const i32 *indices, const i64 *
 /* Returns the operation count sum over rounds of vol(F).                    */
 /* ------------------------------------------------------------------------ */
 i64 orc_ign_sync_column(i64 n, const i64 *indptr, const i32 *indices, const i64 *degree, double alpha,
-                        const double *eps_vec, double beta, double *p, double *r, i64 cs, const unsigned char *cand0,
-                        i64 max_rounds) {
+                        double x_gain, const double *eps_vec, double beta, double *p, double *r, i64 cs,
+                        const unsigned char *cand0, i64 max_rounds) {
     unsigned char *cand = (unsigned char *)malloc((size_t)n);
     unsigned char *next = (unsigned char *)calloc((size_t)n, 1);
     i64 *fr = (i64 *)malloc((size_t)n * sizeof(i64));
@@ -877,7 +900,7 @@ i64 orc_ign_sync_column(i64 n, const i64 *indptr, const i32 *indices, const i64 
                 p[u * cs] = ru;
                 val[i] = 0.0;
             } else {
-                p[u * cs] += alpha * ru;
+                p[u * cs] += x_gain * ru;
                 val[i] = (1. - alpha) * ru / pow((double)degree[u], 1 - beta);
                 oper += degree[u];
             }

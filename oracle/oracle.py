@@ -62,14 +62,14 @@ def lib():
         L.orc_ign_static_column.argtypes = [_i64, _p, _p, _p, _dbl, _dbl, _dbl, _int, _dbl, _p, _i64, _p, _i64]
         L.orc_update_graph.restype = None
         L.orc_update_graph.argtypes = [_i64, _p, _p, _p, _p, _p, _i64, _int, _p, _p, _p, _p, _p, _p, _p, _p]
-        L.orc_ign_update_column.restype = None
+        L.orc_ign_update_column.restype = _i64
         L.orc_ign_update_column.argtypes = [_i64, _p, _p, _p, _p, _p, _p, _p, _i64, _dbl, _dbl, _dbl, _int, _int,
-                                            _dbl, _p, _p, _p, _i64, _p, _p, _p, _i64]
+                                            _dbl, _p, _p, _p, _i64, _p, _p, _p, _i64, _int]
         L.orc_update_ppr_row.restype = _i64
         L.orc_update_ppr_row.argtypes = [_i64, _p, _p, _p, _p, _p, _p, _dbl, _dbl, _dbl, _p, _p, _p, _i64, _p, _p,
-                                         _p, _i64]
+                                         _p, _i64, _int]
         L.orc_ign_sync_column.restype = _i64
-        L.orc_ign_sync_column.argtypes = [_i64, _p, _p, _p, _dbl, _p, _dbl, _p, _p, _i64, _p, _i64]
+        L.orc_ign_sync_column.argtypes = [_i64, _p, _p, _p, _dbl, _dbl, _p, _dbl, _p, _p, _i64, _p, _i64]
         L.orc_threads.restype = _int
         L.orc_ppr_gd_many.restype = None
         L.orc_ppr_gd_many.argtypes = [_i64, _p, _p, _p, _p, _i64, _dbl, _p, _int, _p, _p, _int]
@@ -190,23 +190,32 @@ def update_graph(n, indptr, indices, degree, us, vs, onlyinsert):
     return ik[:a], io[:a + 1], inb[:io[a]], dk[:b], do[:b + 1], dnb[:do[b]]
 
 
-def ign_update(n, indptr, indices, degree, alpha, eps, omega, P, R, X, us, vs, beta, algo):
-    """``instantGNNUpdateBatchParallel`` (InstantGNN.py:332-359); mutates graph, P, R in place."""
+def ign_update(n, indptr, indices, degree, alpha, eps, omega, P, R, X, us, vs, beta, algo, sync=False):
+    """``instantGNNUpdateBatchParallel`` (InstantGNN.py:332-359); mutates graph, P, R in place.
+
+    sync=True keeps the reference's repair and uses the synchronous push;
+    returns (maps, per-column push opers).
+    """
     old_degree = degree.copy()
     maps = update_graph(n, indptr, indices, degree, us, vs, "insert" in algo)
     ik, io, inb, dk, do, dnb = maps
     F = R.shape[1]
     X = np.ascontiguousarray(X, dtype=np.float64)
+    opers = np.zeros(F, np.int64)
     for f in range(F):
-        lib().orc_ign_update_column(n, _ptr(indptr), _ptr(indices), _ptr(degree), _ptr(old_degree),
-                                    P.ctypes.data + 8 * f, R.ctypes.data + 8 * f, X.ctypes.data + 8 * f, F, alpha, eps,
-                                    omega, int("sor" in algo), int("insert" in algo), beta, _ptr(ik), _ptr(io),
-                                    _ptr(inb), len(ik), _ptr(dk), _ptr(do), _ptr(dnb), len(dk))
-    return maps
+        opers[f] = lib().orc_ign_update_column(n, _ptr(indptr), _ptr(indices), _ptr(degree), _ptr(old_degree),
+                                               P.ctypes.data + 8 * f, R.ctypes.data + 8 * f, X.ctypes.data + 8 * f, F,
+                                               alpha, eps, omega, int("sor" in algo), int("insert" in algo), beta,
+                                               _ptr(ik), _ptr(io), _ptr(inb), len(ik), _ptr(dk), _ptr(do), _ptr(dnb),
+                                               len(dk), int(sync))
+    return maps, opers
 
 
-def update_ppr(n, indptr, indices, degree, alpha, eps, omega, P, R, us, vs):
-    """``update_ppr_parallel`` (ppr_solver.py:824-849); P, R are F x n, updated in place -> opers."""
+def update_ppr(n, indptr, indices, degree, alpha, eps, omega, P, R, us, vs, sync=False):
+    """``update_ppr_parallel`` (ppr_solver.py:824-849); P, R are F x n, updated in place -> opers.
+
+    sync=True keeps the reference's repair and uses the synchronous push.
+    """
     old_degree = degree.copy()
     ik, io, inb, dk, do, dnb = update_graph(n, indptr, indices, degree, us, vs, False)
     opers = np.zeros(P.shape[0], np.int64)
@@ -215,13 +224,13 @@ def update_ppr(n, indptr, indices, degree, alpha, eps, omega, P, R, us, vs):
         r = np.ascontiguousarray(R[f])
         opers[f] = lib().orc_update_ppr_row(n, _ptr(indptr), _ptr(indices), _ptr(degree), _ptr(old_degree), _ptr(p),
                                             _ptr(r), alpha, eps, omega, _ptr(ik), _ptr(io), _ptr(inb), len(ik),
-                                            _ptr(dk), _ptr(do), _ptr(dnb), len(dk))
+                                            _ptr(dk), _ptr(do), _ptr(dnb), len(dk), int(sync))
         P[f] = p
         R[f] = r
     return opers
 
 
-def ign_sync(n, indptr, indices, degree, alpha, eps, beta, P, R, cand0=None, max_rounds=1 << 30):
+def ign_sync(n, indptr, indices, degree, alpha, eps, beta, P, R, cand0=None, max_rounds=1 << 30, x_gain=None):
     """Synchronous InstantGNN push (the GPU's frontier rule) on every column of P, R in place.
 
     Returns per-column operation counts.
@@ -234,7 +243,8 @@ def ign_sync(n, indptr, indices, degree, alpha, eps, beta, P, R, cand0=None, max
     cand0 = np.ascontiguousarray(cand0, dtype=np.uint8)
     opers = np.zeros(F, np.int64)
     for f in range(F):
-        opers[f] = lib().orc_ign_sync_column(n, _ptr(indptr), _ptr(indices), _ptr(degree), alpha, _ptr(eps_vec), beta,
+        opers[f] = lib().orc_ign_sync_column(n, _ptr(indptr), _ptr(indices), _ptr(degree), alpha,
+                                             alpha if x_gain is None else x_gain, _ptr(eps_vec), beta,
                                              P.ctypes.data + 8 * f, R.ctypes.data + 8 * f, F, _ptr(cand0), max_rounds)
     return opers
 
