@@ -1,0 +1,342 @@
+#!/usr/bin/env python
+"""Benchmark: PPR queries/s and p50/p99 latency at eps=1e-7, FP32 batched local push, one GB300.
+
+Workload (the configuration the headline metric is quoted on): the
+wiki-talk-shaped Chung-Lu graph (n = 2,364,073, 9,355,158 CSR entries,
+degree exponent ~2, max degree ~62k), personalized PageRank local GD with
+alpha = 0.1, eps = 1e-7, seeds drawn uniformly from nodes with degree >= 1.
+One step = one batch of --batch queries solved to the reference's stopping
+rule by the GPU engine (FP32 residuals, Kahan FP32 solution, FP64 threshold
+tests), results left in HBM.  `e2e` repeats the step through the public C
+ABI with host seeds/eps and the solution rows copied back to pinned host
+memory inside the timed region.
+
+Reported beside it: the plain single-query GPU baseline (the structure of
+the reference's ppr_gd_local_gpu on this GPU, the denominator of the
+speed-up), and the timed CPU baseline (the C port of the reference's
+ppr_gd local, FP64, all host cores, a bounded sample of queries).
+
+--impl reference times the reference's CPU implementation of the path (the
+C port in oracle/, the reference itself being numba Python that is not
+installed on the GPU machine) on the same workload and prints the same line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.join(ROOT, "faster-local-solver-for-gdes_gb300")
+for _p in (ROOT, PKG):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+METRIC = "PPR queries/s + p50/p99 ms at ε=1e-7, served FP32 vs plain local push, 1 GB300"
+ALPHA = 0.1
+EPS = 1e-7
+WORKLOAD = "ppr_local_gd_fp32_batched_chung_lu_2.36M"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--batch", type=int, default=512, help="queries per step")
+    ap.add_argument("--tile-w", type=int, default=8)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--plain-queries", type=int, default=4)
+    ap.add_argument("--cpu-queries", type=int, default=0, help="CPU-baseline sample (0 = 2 per host thread)")
+    ap.add_argument("--no-baselines", action="store_true")
+    ap.add_argument("--tuning", default="", help="k=v,... engine tuning overrides")
+    return ap.parse_args()
+
+
+def dist_env():
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+class ClockSampler:
+    """nvidia-smi clocks / throttle reasons sampled during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+
+    def __enter__(self):
+        try:
+            os.makedirs(os.path.dirname(self.path), exist_ok=True)
+            self.fh = open(self.path, "w")
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
+                                         stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.fh.close()
+
+    def summary(self) -> dict:
+        if self.proc is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        sm, smax, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax.append(float(f[2]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[5:9]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(smax), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peak():
+    path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        if d.get("hbm_gbs"):
+            return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def committed_traffic():
+    """Per-launch DRAM traffic of the push kernel from the committed ncu summary, if present."""
+    path = os.path.join(ROOT, "profiles", "push_kernel_traffic.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return d
+    return None
+
+
+def algorithmic_bytes(stats: dict) -> float:
+    """FP32: 4 B col_idx per union-frontier edge, 8 B residual RMW per (edge, column),
+    32 B per active (node, column): row_ptr pair, r read/zero, x RMW, degree, frontier index."""
+    return 4.0 * stats["union_vol"] + 8.0 * stats["col_vol"] + 32.0 * stats["col_nodes"]
+
+
+def cpu_baseline(g, n_queries: int, eps: float):
+    from oracle import oracle as O
+    threads = O.threads()
+    if n_queries <= 0:
+        n_queries = 2 * threads
+    from gde import graphs
+    seeds = graphs.uniform_seeds(g, n_queries, seed=424242)
+    deg = g.degree.astype(np.float64)
+    t0 = time.perf_counter()
+    O.ppr_gd_many(g.n, g.indptr, g.indices, deg, seeds, ALPHA, eps, local=True, nthreads=threads)
+    dt = time.perf_counter() - t0
+    return n_queries / dt, threads, n_queries, dt
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return
+    from gde import graphs
+    from oracle import oracle as O
+    O.build()
+    g = graphs.chung_lu_wikitalk_shape()
+    threads = O.threads()
+    per_step = max(args.cpu_queries, threads)
+    deg = g.degree.astype(np.float64)
+    for w in range(args.warmup):
+        O.ppr_gd_many(g.n, g.indptr, g.indices, deg, graphs.uniform_seeds(g, threads, seed=900 + w), ALPHA, EPS,
+                      nthreads=threads)
+    t_total = 0.0
+    for s in range(args.steps):
+        seeds = graphs.uniform_seeds(g, per_step, seed=1000 + s)
+        t0 = time.perf_counter()
+        O.ppr_gd_many(g.n, g.indptr, g.indices, deg, seeds, ALPHA, EPS, nthreads=threads)
+        t_total += time.perf_counter() - t0
+    qps = per_step * args.steps / t_total
+    line = {
+        "metric": METRIC, "value": qps, "unit": "queries/s", "impl": "reference", "n_gpus": 0,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "ppr_local_gd_fp64_cpu_port_chung_lu_2.36M", "queries_per_step": per_step,
+                   "alpha": ALPHA, "eps": EPS, "n": g.n, "nnz": g.nnz},
+        "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"{per_step} queries per step, one per OpenMP thread"},
+        "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    from gde import _lib as L
+    from gde import api, graphs
+
+    tuning = {}
+    for kv in filter(None, args.tuning.split(",")):
+        k, v = kv.split("=")
+        tuning[k] = int(v)
+    g = graphs.chung_lu_wikitalk_shape()
+    ctx = api.Context.get(local)
+    G = api.Graph(g.indptr, g.indices, ctx=ctx)
+    Q = args.batch
+    stream = torch.cuda.ExternalStream(api.ctx_stream(ctx), device=f"cuda:{local}")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")  # > L2 (129 MB)
+    x_dev = torch.empty((Q, g.n), dtype=torch.float32, device=f"cuda:{local}")
+
+    def step(seed_base, x_out=None, device_out=True):
+        seeds = graphs.uniform_seeds(g, Q, seed=seed_base)
+        return api.solve(G, L.PPR, L.LOCAL_GD, seeds, EPS, prec="fp32", alpha=ALPHA, tile_w=args.tile_w,
+                         want_r=False, x_out=x_out if x_out is not None else x_dev, device_out=device_out,
+                         tuning=tuning)
+
+    for w in range(args.warmup):
+        step(10_000 * rank + w)
+    torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
+
+    times = []
+    lat = []
+    kms = []
+    agg = {"union_vol": 0.0, "col_vol": 0.0, "col_nodes": 0, "union_nodes": 0, "rounds": 0}
+    opers = []
+    launches = 0
+    with ClockSampler(local) as clk:
+        for s in range(args.steps):
+            flush.zero_()  # L2 flush between timed steps
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            res = step(20_000 * rank + 100 + s)
+            e1.record(stream)
+            e1.synchronize()
+            times.append(e0.elapsed_time(e1))
+            st = res["stats"]
+            kms.append(st["kernel_ms"])
+            for k in agg:
+                agg[k] += st[k]
+            lat.extend(res["latency_ms"].tolist())
+            opers.extend(res["oper"].tolist())
+            launches += max(1, int(np.ceil(st["tiles"] / 4096)))
+    torch.cuda.synchronize()
+    total_ms = float(sum(times))
+    if world > 1:
+        t = torch.tensor([total_ms], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        total_ms = float(t.item())
+    value = Q * args.steps * world / (total_ms / 1e3)
+
+    # ---- end to end through the C ABI with host buffers ----
+    x_host = torch.empty((Q, g.n), dtype=torch.float32).pin_memory()
+    e2e_ms = []
+    for s in range(args.e2e_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        step(30_000 * rank + s, x_out=x_host, device_out=False)
+        e1.record(stream)
+        e1.synchronize()
+        e2e_ms.append(e0.elapsed_time(e1))
+    e2e_value = Q * max(1, args.e2e_steps) * world / (sum(e2e_ms) / 1e3) if e2e_ms else None
+
+    if rank != 0:
+        if world > 1:
+            torch.distributed.barrier()
+        return
+
+    peak, peak_kind = measured_peak()
+    kernel_ms_total = float(sum(kms))
+    bytes_total = algorithmic_bytes(agg)
+    achieved = bytes_total / (kernel_ms_total / 1e3) / 1e9
+    traffic = committed_traffic()
+    per_launch_bytes = bytes_total / launches
+    roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+            "peak_kind": peak_kind,
+            "traffic": (traffic["dram_bytes_per_query"] * Q if traffic else None),
+            "algorithmic_bytes_per_launch": per_launch_bytes, "kernel": "push_kernel<float,%d>" % args.tile_w,
+            "kernel_ms_per_launch": kernel_ms_total / launches}
+    lat_sorted = np.sort(np.asarray(lat))
+    out = {
+        "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": WORKLOAD, "n": g.n, "nnz": g.nnz, "queries_per_step": Q, "alpha": ALPHA, "eps": EPS,
+                   "tile_w": args.tile_w, "precision": "fp32 residual, kahan fp32 x, fp64 threshold",
+                   "l2": "512 MB buffer written between timed steps", "parallelism": f"replicas x{world}"},
+        "p50_ms": float(np.percentile(lat_sorted, 50)) if lat else None,
+        "p99_ms": float(np.percentile(lat_sorted, 99)) if lat else None,
+        "mean_oper": float(np.mean(opers)) if opers else None,
+        "rounds_total": agg["rounds"],
+        "gpu_launches": int(launches + args.steps * 2),
+        "roofline": roof,
+        "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": Q * (4 + 8),
+                "d2h_bytes_per_step": Q * g.n * 4 + Q * (8 + 4 + 4)},
+    }
+    out["clocks"] = clk.summary()
+    if not args.no_baselines:
+        # plain single-query GPU baseline (the x20 denominator)
+        xs = torch.zeros(g.n, dtype=torch.float32, device=f"cuda:{local}")
+        seeds = graphs.uniform_seeds(g, args.plain_queries + 1, seed=777)
+        api.plain_ppr_local(G, int(seeds[0]), ALPHA, EPS, x_out=xs)  # warm-up
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for s in seeds[1:]:
+            api.plain_ppr_local(G, int(s), ALPHA, EPS, x_out=xs)
+        torch.cuda.synchronize()
+        plain_qps = args.plain_queries / (time.perf_counter() - t0)
+        out["plain_gpu"] = {"value": plain_qps, "unit": "queries/s", "sample": f"{args.plain_queries} queries",
+                            "speedup": value / plain_qps}
+        qps, threads, nq, dt = cpu_baseline(g, args.cpu_queries, EPS)
+        out["cpu_baseline"] = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
+                               "sample": f"{nq} queries (ppr_gd local FP64, one per OpenMP thread), {dt:.1f} s"}
+    print(json.dumps(out), flush=True)
+    if world > 1:
+        torch.distributed.barrier()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

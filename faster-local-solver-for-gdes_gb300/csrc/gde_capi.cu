@@ -392,6 +392,8 @@ int gde_ctx_destroy(gde_ctx* ctx) {
 
 const char* gde_last_error(gde_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 
+void* gde_ctx_stream(gde_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
 int gde_ctx_sync(gde_ctx* ctx) {
     if (!ctx) return GDE_EINVAL;
     CK(cudaStreamSynchronize(ctx->stream));
@@ -471,7 +473,7 @@ int gde_graph_info(gde_graph* G, int64_t* n, int64_t* cap, double* vol) {
 
 int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const int32_t* seeds, const double* eps,
               void* x_out, void* r_out, int out64, int out_mem, int64_t ld_out, double* oper_out, int32_t* rounds_out,
-              gde_stats* stats) {
+              float* lat_ms_out, gde_stats* stats) {
     if (!ctx || !G || !p || nq < 0 || (nq > 0 && (!seeds || !eps))) return fail(ctx, GDE_EINVAL, "bad solve arguments");
     CK(cudaSetDevice(ctx->device));
     const int64_t n = G->g.n;
@@ -708,6 +710,10 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
                 else oper = C.oper;
                 if (oper_out) oper_out[q] = oper;
                 if (rounds_out) rounds_out[q] = C.rounds;
+                if (lat_ms_out)
+                    lat_ms_out[q] = C.finish_ns > ctx->hstats->start_ns
+                                        ? (float)((double)(C.finish_ns - ctx->hstats->start_ns) * 1e-6)
+                                        : 0.f;
             }
         }
         if (stats) { stats->tiles += nt; stats->tile_w = W; }

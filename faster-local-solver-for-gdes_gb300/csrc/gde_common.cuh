@@ -108,6 +108,7 @@ struct ColState {             // one per column slot
     int check_cnt[2];         // global methods: nodes above threshold (parity)
     int seed;                 // seed node (-1 for feature columns)
     int pad;
+    unsigned long long finish_ns;  // %globaltimer when the column finished (0 = not yet)
 };
 
 struct LaunchStats {          // roofline counters summed over a launch
@@ -118,6 +119,7 @@ struct LaunchStats {          // roofline counters summed over a launch
     unsigned long long dense_rounds;
     unsigned long long rounds;
     unsigned long long cand_nodes;     // candidates examined
+    unsigned long long start_ns;       // %globaltimer at kernel start (block 0)
 };
 
 struct GridBarrier {

@@ -4,6 +4,13 @@
 
 namespace gde {
 
+// Device-wide nanosecond clock (PTX %globaltimer).
+__device__ __forceinline__ unsigned long long globaltimer_ns() {
+    unsigned long long t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
 // Append v to a candidate list once per stamp (mark dedup), one atomic per
 // warp for all appending lanes.  `mask` must name every lane executing the
 // call.

@@ -378,6 +378,10 @@ __device__ void prep_phase(const PushArgs& a, int t, TileSh& sh, PrepSh& ps) {
                     }
                 } else {
                     a_k = global ? (rv != 0.0) : (fabs(rv) >= thr);
+                    // An absorbing node (threshold 0) is visited once by the
+                    // reference's initial scan and never re-enqueued; with a
+                    // zero residual it has nothing to absorb.
+                    if (absorb && rv == 0.0) a_k = false;
                     if (a_k) {
                         double pv;
                         if (kind == KIND_PPR || kind == KIND_UPPR) pv = ((1. - alpha) * rv) / du;
@@ -699,7 +703,10 @@ __device__ void finish_round(const PushArgs& a, int t, const TileSh& sh) {
             bool worked = gcheck ? (cs.check_cnt[sh.parity] > 0) : (cs.round_active[sh.parity] > 0);
             if (method_is_hk(m) && m != M_HK_LOCAL) worked = true;  // fixed sweeps per level
             if (worked) cs.rounds += 1;
-            if (!worked || hk_end) cs.live = 0;
+            if (!worked || hk_end) {
+                cs.live = 0;
+                cs.finish_ns = globaltimer_ns();
+            }
         }
     }
     if (threadIdx.x == 0) {
@@ -714,6 +721,7 @@ __global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
     __shared__ int s_cnt[kMaxW];
     __shared__ unsigned s_live[kMaxTiles / 32];
     __shared__ int s_any, s_check;
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.stats->start_ns = globaltimer_ns();
     int it = 0;
     for (; it < a.round_budget; ++it) {
         // ---- snapshot of live tiles for this round ----

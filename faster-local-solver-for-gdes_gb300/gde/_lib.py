@@ -50,8 +50,9 @@ SIGNATURES = {
     "gde_graph_upload": (_int, [_p, _i64, _i64, _p, _p, _p, _p, ctypes.POINTER(_p)]),
     "gde_graph_free": (_int, [_p]),
     "gde_graph_info": (_int, [_p, _p, _p, _p]),
-    "gde_solve": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _p, _p, _int, _int, _i64, _p, _p,
+    "gde_solve": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _p, _p, _int, _int, _i64, _p, _p, _p,
                          ctypes.POINTER(Stats)]),
+    "gde_ctx_stream": (_p, [_p]),
     "gde_hk_estimate_n": (_i64, [_dbl, _dbl]),
     "gde_feature_push": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _i64, _dbl, _p, _i64, _p,
                                 ctypes.POINTER(Stats)]),

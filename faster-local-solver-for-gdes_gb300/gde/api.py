@@ -132,14 +132,22 @@ def solve(graph: Graph, kind: int, method: int, seeds, eps, *, prec: str = "fp64
             r_out = np.empty(shape, dtype=odt)
     oper = np.zeros(nq, dtype=np.float64)
     rounds = np.zeros(nq, dtype=np.int32)
+    lat = np.zeros(nq, dtype=np.float32)
     p = make_params(kind, method, prec, tile_w, alpha, tau, l_max, mu_min, max_rounds=max_rounds, tuning=tuning)
     st = L.Stats()
     status = lib.gde_solve(graph.ctx.ptr, graph.ptr, ctypes.byref(p), nq, _ptr(seeds), _ptr(eps),
                            _ptr(x_out) if want_x else None, _ptr(r_out) if want_r else None, int(out64),
-                           L.MEM_DEVICE if device_out else L.MEM_HOST, n, _ptr(oper), _ptr(rounds), ctypes.byref(st))
+                           L.MEM_DEVICE if device_out else L.MEM_HOST, n, _ptr(oper), _ptr(rounds), _ptr(lat),
+                           ctypes.byref(st))
     L.check(graph.ctx.ptr, status, "gde_solve")
     return {"x": x_out if want_x else None, "r": r_out if want_r else None, "oper": oper, "rounds": rounds,
-            "stats": st.as_dict()}
+            "latency_ms": lat, "stats": st.as_dict()}
+
+
+def ctx_stream(ctx: Context | None = None) -> int:
+    """The library's CUDA stream handle (for torch.cuda.ExternalStream / events)."""
+    c = ctx or Context.get(0)
+    return int(L.load().gde_ctx_stream(c.ptr) or 0)
 
 
 def feature_push(graph: Graph, kind: int, P, R, eps: float, *, alpha: float, beta: float = 0.0, prec: str = "fp64",

@@ -124,11 +124,17 @@ int gde_graph_info(gde_graph *g, int64_t *n, int64_t *cap, double *volume);
  * x_out / r_out (may be NULL) receive nq rows of ld_out values each (HK
  * r_out: 2 rows per query, the two level buffers of hk_solver.py:212),
  * FP64 when out64 else FP32, in host or device memory per out_mem.
- * seeds / eps are host arrays.  oper_out / rounds_out (host, may be NULL)
- * receive the reference's operation count and the rounds per query. */
+ * seeds / eps are host arrays.  oper_out / rounds_out / lat_ms_out (host,
+ * may be NULL) receive the reference's operation count, the rounds, and the
+ * device time from the start of the push launch to the round the query
+ * finished in. */
 int gde_solve(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t nq, const int32_t *seeds, const double *eps,
               void *x_out, void *r_out, int out64, int out_mem, int64_t ld_out, double *oper_out,
-              int32_t *rounds_out, gde_stats *stats);
+              int32_t *rounds_out, float *lat_ms_out, gde_stats *stats);
+
+/* The context's CUDA stream (a cudaStream_t), for callers that order their
+ * own work or CUDA events with the library's. */
+void *gde_ctx_stream(gde_ctx *ctx);
 
 /* heat-kernel Taylor length, hk_solver.py:28-48 (estimate_n) */
 int64_t gde_hk_estimate_n(double tau, double eps);

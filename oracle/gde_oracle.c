@@ -180,6 +180,12 @@ i64 orc_cheby(i64 n, const i64 *indptr, const i32 *indices, const double *degree
             }
         }
         for (;;) {
+            if (sync && rear > 0) {
+                /* the sync rule marks without filling queue[]: rebuild it first */
+                i64 k = 0;
+                for (i64 i = 0; i < n; i++)
+                    if (q_mark[i]) queue[k++] = i;
+            }
             if (katz)
                 for (i64 i = 0; i < rear; i++) oper += (i64)degree[queue[i]];
             if (rear == 0) break;
