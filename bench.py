@@ -231,6 +231,7 @@ def run_ours(args):
     times = []
     lat = []
     kms = []
+    ph = {"check": [], "prep": [], "scatter": []}
     agg = {"union_vol": 0.0, "col_vol": 0.0, "col_nodes": 0, "union_nodes": 0, "rounds": 0}
     opers = []
     launches = 0
@@ -247,6 +248,8 @@ def run_ours(args):
             times.append(e0.elapsed_time(e1))
             st = res["stats"]
             kms.append(st["kernel_ms"])
+            for k in ph:
+                ph[k].append(st[k + "_ms"])
             for k in agg:
                 agg[k] += st[k]
             lat.extend(res["latency_ms"].tolist())
@@ -303,6 +306,7 @@ def run_ours(args):
         "p99_ms": float(np.percentile(lat_sorted, 99)) if lat else None,
         "mean_oper": float(np.mean(opers)) if opers else None,
         "rounds_total": agg["rounds"],
+        "phase_ms": {k: float(sum(ph[k])) / args.steps for k in ph},
         "gpu_launches": int(launches + args.steps * 2),
         "roofline": roof,
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": Q * (4 + 8),

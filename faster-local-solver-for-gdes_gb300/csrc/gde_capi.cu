@@ -131,7 +131,7 @@ int64_t estimate_n(double t, double eps) {
 }
 
 struct Defaults {
-    int small_max = 8, med_max = 2048, chunk = 2048, dense_div = 16;
+    int small_max = 8, med_max = 2048, chunk = 2048, dense_div = 2;
 };
 
 void fill_tuning(const gde_params* p, PushArgs& a) {
@@ -142,6 +142,7 @@ void fill_tuning(const gde_params* p, PushArgs& a) {
     a.chunk = p->chunk > 0 ? p->chunk : d.chunk;
     a.dense_div = p->dense_div > 0 ? p->dense_div : d.dense_div;
     a.max_rounds = p->max_rounds > 0 ? p->max_rounds : kDefaultMaxRounds;
+    a.allow_dense = 1;
 }
 
 bool valid_w(int W) { return W == 1 || W == 2 || W == 4 || W == 8 || W == 16 || W == 32; }
@@ -240,6 +241,9 @@ int run_engine(gde_ctx* ctx, PushArgs& a, int prec64, int W, gde_stats* st, doub
         st->col_vol += ctx->hstats->col_vol;
         st->union_nodes += ctx->hstats->union_nodes;
         st->col_nodes += ctx->hstats->col_nodes;
+        st->check_ms += (double)ctx->hstats->check_ns * 1e-6;
+        st->prep_ms += (double)ctx->hstats->prep_ns * 1e-6;
+        st->scatter_ms += (double)ctx->hstats->scatter_ns * 1e-6;
     }
     if (herr != 0) return fail(ctx, herr, "a device-side wait ran out of iterations (grid barrier)");
     return GDE_OK;
@@ -572,7 +576,7 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
         if (rc != GDE_OK) return rc;
         PushArgs& a = tw.a;
         a.small_max = base.small_max; a.med_max = base.med_max; a.chunk = base.chunk;
-        a.dense_div = base.dense_div; a.max_rounds = base.max_rounds;
+        a.dense_div = base.dense_div; a.max_rounds = base.max_rounds; a.allow_dense = base.allow_dense;
         rc = alloc_large(ctx, G, nt, tw);
         if (rc != GDE_OK) return rc;
         const size_t slab = (size_t)nt * n * W * es;
@@ -778,6 +782,10 @@ static int feature_push_impl(gde_ctx* ctx, gde_graph* G, const gde_params* p, in
         int rc = alloc_tiles(ctx, G, nt, W, prec64, false, false, false, false, tw);
         if (rc != GDE_OK) return rc;
         PushArgs& a = tw.a;
+        // an incremental update (candidates given on the device) visits only
+        // touched nodes: degree edits may have lowered untouched thresholds,
+        // and the reference never re-examines those nodes
+        a.allow_dense = cand_on_device ? 0 : 1;
         rc = alloc_large(ctx, G, nt, tw);
         if (rc != GDE_OK) return rc;
         const size_t es = prec64 ? 8 : 4;

@@ -120,6 +120,9 @@ struct LaunchStats {          // roofline counters summed over a launch
     unsigned long long rounds;
     unsigned long long cand_nodes;     // candidates examined
     unsigned long long start_ns;       // %globaltimer at kernel start (block 0)
+    unsigned long long check_ns;       // block 0's time in CHECK phases (incl. barrier wait)
+    unsigned long long prep_ns;        // ... PREP phases
+    unsigned long long scatter_ns;     // ... SCATTER phases
 };
 
 struct GridBarrier {
@@ -159,6 +162,7 @@ struct PushArgs {
     int max_rounds;            // hard cap on a tile's rounds
     int round_budget;          // rounds to advance in this launch (serving ticks)
     int kahan;                 // compensated FP32 solution
+    int allow_dense;           // 0: every round visits only touched nodes (dynamic updates)
 };
 
 }  // namespace gde

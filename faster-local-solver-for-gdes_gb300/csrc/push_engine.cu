@@ -273,7 +273,7 @@ template <typename T, int W>
 __device__ void prep_phase(const PushArgs& a, int t, TileSh& sh, PrepSh& ps) {
     constexpr int VEC = (sizeof(T) == 4) ? (W >= 4 ? 4 : W) : (W >= 2 ? 2 : 1);
     constexpr int L = W / VEC;          // lanes per node
-    constexpr int GPB = kThreads / L;   // nodes per block iteration
+    constexpr int GPW = 32 / L;         // nodes per warp iteration
     const DevGraph& g = a.g;
     const int64_t n = g.n;
     const int par = sh.parity;
@@ -326,10 +326,12 @@ __device__ void prep_phase(const PushArgs& a, int t, TileSh& sh, PrepSh& ps) {
     int my_cnt = 0;
     int* next_cnt = &ts.cand_cnt[(sh.level + 1) % 3];
 
-    // Rotate the starting block by tile so that short lists spread over SMs.
-    const int64_t bstart = (blockIdx.x + (int64_t)t * 37) % gridDim.x;
-    for (int64_t base = bstart * GPB; base < ncand; base += (int64_t)gridDim.x * GPB) {
-        int64_t i = base + threadIdx.x / L;
+    // Warps stride independently over the candidates; the starting warp is
+    // rotated by tile so that short lists spread over SMs.
+    const int64_t nwarps = (int64_t)gridDim.x * kWarps;
+    const int64_t wstart = ((int64_t)blockIdx.x * kWarps + warp + (int64_t)t * 131) % nwarps;
+    for (int64_t base = wstart * GPW; base < ncand; base += nwarps * GPW) {
+        int64_t i = base + grp_w;
         bool valid = i < ncand;
         int u = 0;
         bool act[VEC];
@@ -466,47 +468,36 @@ __device__ void prep_phase(const PushArgs& a, int t, TileSh& sh, PrepSh& ps) {
             if (lane >= o) sc += y;
         }
         int wch = __shfl_sync(kFull, sc, 31);
-        if (lane == 0) {
-            ps.warp_cnt[warp][0] = __popc(bf);
-            ps.warp_cnt[warp][1] = __popc(bs);
-            ps.warp_cnt[warp][2] = __popc(bm);
-            ps.warp_cnt[warp][3] = wch;
+        // one global atomic per non-empty list per warp
+        int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+        if (lane == 0 && bf) {
+            b0 = atomicAdd(&ts.front_cnt[par], __popc(bf));
+            if (bs) b1 = atomicAdd(&ts.small_cnt[par], __popc(bs));
+            if (bm) b2 = atomicAdd(&ts.med_cnt[par], __popc(bm));
+            if (wch) b3 = atomicAdd(&ts.large_cnt[par], wch);
         }
-        __syncthreads();
-        if (threadIdx.x < 4) {
-            int tot = 0;
-            for (int w = 0; w < kWarps; ++w) {
-                int c = ps.warp_cnt[w][threadIdx.x];
-                ps.warp_cnt[w][threadIdx.x] = tot;  // exclusive prefix over warps
-                tot += c;
-            }
-            int b = 0;
-            if (tot) {
-                if (threadIdx.x == 0) b = atomicAdd(&ts.front_cnt[par], tot);
-                else if (threadIdx.x == 1) b = atomicAdd(&ts.small_cnt[par], tot);
-                else if (threadIdx.x == 2) b = atomicAdd(&ts.med_cnt[par], tot);
-                else b = atomicAdd(&ts.large_cnt[par], tot);
-            }
-            ps.base[threadIdx.x] = b;
-        }
-        __syncthreads();
         unsigned below = (1u << lane) - 1u;
         int fidx = 0;
-        if (leader && node_in) {
-            fidx = ps.base[0] + ps.warp_cnt[warp][0] + __popc(bf & below);
-            front[fidx] = u;
-            if (bucket == 0) bsmall[ps.base[1] + ps.warp_cnt[warp][1] + __popc(bs & below)] = fidx;
-            else if (bucket == 1) bmed[ps.base[2] + ps.warp_cnt[warp][2] + __popc(bm & below)] = fidx;
-            else {
-                int lb = ps.base[3] + ps.warp_cnt[warp][3] + (sc - lch);
-                for (int ch = 0; ch < nch; ++ch) blarge[lb + ch] = make_int2(fidx, ch);
+        if (bf) {
+            b0 = __shfl_sync(kFull, b0, 0);
+            b1 = __shfl_sync(kFull, b1, 0);
+            b2 = __shfl_sync(kFull, b2, 0);
+            b3 = __shfl_sync(kFull, b3, 0);
+            if (leader && node_in) {
+                fidx = b0 + __popc(bf & below);
+                front[fidx] = u;
+                if (bucket == 0) bsmall[b1 + __popc(bs & below)] = fidx;
+                else if (bucket == 1) bmed[b2 + __popc(bm & below)] = fidx;
+                else {
+                    int lb = b3 + (sc - lch);
+                    for (int ch = 0; ch < nch; ++ch) blarge[lb + ch] = make_int2(fidx, ch);
+                }
+                my_vol += du;
+                my_cnt += 1;
             }
-            my_vol += du;
-            my_cnt += 1;
+            fidx = __shfl_sync(kFull, fidx, grp_w * L);
+            if (node_in) vstore<T, VEC>(Pw + (int64_t)fidx * W + c0, push);
         }
-        fidx = __shfl_sync(kFull, fidx, grp_w * L);
-        if (node_in) vstore<T, VEC>(Pw + (int64_t)fidx * W + c0, push);
-        __syncthreads();  // warp_cnt/base are rewritten next iteration
     }
     // ---- flush per-column counters ----
 #pragma unroll
@@ -585,7 +576,10 @@ __device__ void scatter_phase(const PushArgs& a, int t, TileSh& sh) {
         Tgt = slab_ptr<T>(a.R, a, t);
     }
     // Does the next round scan densely?  Every block decides identically.
-    const bool dense_next = global || (ts.union_vol[par] * (double)a.dense_div > (double)n);
+    // Thresholds can drop between solves (a dynamic-graph update lowers d^(1-b)),
+    // so update pushes keep the reference's touched-only rule (allow_dense = 0).
+    const bool dense_next =
+        global || (a.allow_dense && ts.union_vol[par] * (double)a.dense_div > (double)n);
     const bool track = !dense_next && !sh.final_level && !(method == M_HK_TAYLOR && hk_last_level(sh));
     const bool tgt_scale = (kind == KIND_IGN);
     const int stamp = sh.stamp;
@@ -740,6 +734,8 @@ __global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
         }
         __syncthreads();
         if (!s_any) break;
+        const bool timer = (blockIdx.x == 0 && threadIdx.x == 0);
+        unsigned long long t0 = timer ? globaltimer_ns() : 0ull;
         // ---- CHECK (global GD / Chebyshev tiles) ----
         if (s_check) {
             for (int t = 0; t < a.ntiles; ++t) {
@@ -749,6 +745,11 @@ __global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
                 check_phase<T, W>(a, t, it, s_cnt);
             }
             if (!grid_barrier(a.bar, a.err)) return;
+            if (timer) {
+                unsigned long long t1 = globaltimer_ns();
+                a.stats->check_ns += t1 - t0;
+                t0 = t1;
+            }
         }
         // ---- PREP ----
         for (int t = 0; t < a.ntiles; ++t) {
@@ -757,6 +758,11 @@ __global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
             prep_phase<T, W>(a, t, sh, ps);
         }
         if (!grid_barrier(a.bar, a.err)) return;
+        if (timer) {
+            unsigned long long t1 = globaltimer_ns();
+            a.stats->prep_ns += t1 - t0;
+            t0 = t1;
+        }
         // ---- SCATTER + bookkeeping ----
         for (int t = 0; t < a.ntiles; ++t) {
             if (!(s_live[t >> 5] & (1u << (t & 31)))) continue;
@@ -766,6 +772,7 @@ __global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
             __syncthreads();
         }
         if (!grid_barrier(a.bar, a.err)) return;
+        if (timer) a.stats->scatter_ns += globaltimer_ns() - t0;
     }
     // Record the rounds advanced by this launch (all blocks are past their
     // last read of ts.round once the final barrier completes).

@@ -87,6 +87,9 @@ typedef struct {
     uint64_t col_nodes;         /* sum_t sum_c |S_t^c| */
     int tiles;
     int tile_w;
+    double check_ms;            /* push-kernel time split by phase (global-check / prep / scatter), */
+    double prep_ms;             /* each including the wait at the phase's closing grid barrier */
+    double scatter_ms;
 } gde_stats;
 
 /* ---- context / errors ---- */
