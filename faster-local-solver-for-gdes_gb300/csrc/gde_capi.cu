@@ -322,6 +322,10 @@ int upload_degrees(gde_ctx* ctx, gde_graph* G) {
     CK(cudaMemcpyAsync(G->degf, df.data(), n * 4, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaStreamSynchronize(ctx->stream));
     G->g.vol = vol;
+    int exact = 1;
+    for (int64_t u = 0; u < n; u++)
+        if ((double)df[u] != G->h_deg[u]) { exact = 0; break; }
+    G->g.degf_exact = exact;
     return GDE_OK;
 }
 
@@ -530,7 +534,7 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
     size_t have = 0;
     for (auto& kv : ctx->ws) have += kv.second.bytes;
     size_t budget = (size_t)((double)(freeb + have) * 0.85);
-    int max_tiles = (int)std::min<size_t>(4096, std::max<size_t>(1, budget / std::max<size_t>(per_tile, 1)));
+    int max_tiles = (int)std::min<size_t>(512, std::max<size_t>(1, budget / std::max<size_t>(per_tile, 1)));
 
     PushArgs base{};
     fill_tuning(p, base);
@@ -774,7 +778,7 @@ static int feature_push_impl(gde_ctx* ctx, gde_graph* G, const gde_params* p, in
     size_t per_tile = (size_t)n * W * (prec64 ? 8 : 4) + (size_t)n * 4 * 6 + 4096;
     size_t freeb = 0, totalb = 0;
     cudaMemGetInfo(&freeb, &totalb);
-    int max_tiles = (int)std::min<size_t>(4096, std::max<size_t>(1, (size_t)(freeb * 0.8) / per_tile));
+    int max_tiles = (int)std::min<size_t>(512, std::max<size_t>(1, (size_t)(freeb * 0.8) / per_tile));
     for (int t0 = 0; t0 < nt_total; t0 += max_tiles) {
         const int nt = std::min(max_tiles, nt_total - t0);
         TileWs tw;

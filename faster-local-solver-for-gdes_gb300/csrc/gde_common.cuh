@@ -57,6 +57,7 @@ struct DevGraph {
     const double* tfac;       // [n] InstantGNN target divisor d^beta
     const float* tfac_f;      // [n] same, FP32
     double vol;               // sum of degrees (m)
+    int degf_exact;           // 1 when every degree is an integer < 2^24 (degf == degd exactly)
 };
 
 // ---------------------------------------------------------------------------

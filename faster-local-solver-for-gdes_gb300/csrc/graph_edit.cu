@@ -13,6 +13,7 @@
 #include <cuda_runtime.h>
 
 #include <cmath>
+#include <algorithm>
 #include <cstring>
 #include <string>
 #include <unordered_map>
@@ -193,6 +194,12 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
             ins.add(v, u);
         }
     }
+    // A slot can be written more than once (swap-with-last deletions); the
+    // device receives each touched slot once, with its final value.
+    std::sort(pos.begin(), pos.end());
+    pos.erase(std::unique(pos.begin(), pos.end()), pos.end());
+    val.resize(pos.size());
+    for (size_t i = 0; i < pos.size(); i++) val[i] = h_indices[pos[i]];
     int rc = gde_internal_graph_refresh(ctx, G, h_degree, pos.data(), val.data(), (int64_t)pos.size(), p->beta,
                                         kind == KIND_IGN);
     if (rc != GDE_OK) return rc;

@@ -258,11 +258,78 @@ __device__ void check_phase(const PushArgs& a, int t, int it, int* s_cnt) {
 }
 
 // ---------------------------------------------------------------------------
-// PREP phase
+// Work distribution.  Each phase flattens its work over all live tiles
+// (candidates for PREP; short rows, medium rows and long-row chunks for
+// SCATTER) and gives every block one contiguous, equal share of each
+// flattened space, so a round's work is balanced over the whole GPU no
+// matter how it is spread over tiles, and a block touches only the one or
+// two tiles its share overlaps.
+// ---------------------------------------------------------------------------
+constexpr int kMaxLaunchTiles = 512;
+
+struct RoundSh {
+    int ntl;                                    // live tiles this round
+    int any_check;                              // some live tile needs a CHECK phase
+    int tiles[kMaxLaunchTiles];                 // live tile ids (ascending)
+    long long off[3][kMaxLaunchTiles + 1];      // exclusive prefix sums of the current phase's spaces
+    int level[kMaxLaunchTiles];                 // per live tile: rounds since its start
+    unsigned char flags[kMaxLaunchTiles];       // per live tile scatter flags (SF_*)
+    long long scan_tmp[kWarps];
+};
+
+enum : unsigned char { SF_FINAL = 1, SF_TRACK = 2, SF_NOPUSH = 4, SF_TGTSCALE = 8, SF_HK = 16 };
+
+// Exclusive prefix over vals[0..m) (m <= 512) written to out[0..m]; block-wide.
+__device__ void block_exclusive_scan(const long long* vals, int m, long long* out, long long* tmp) {
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    long long v0 = (2 * tid < m) ? vals[2 * tid] : 0;
+    long long v1 = (2 * tid + 1 < m) ? vals[2 * tid + 1] : 0;
+    long long s = v0 + v1;
+    long long inc = s;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        long long y = __shfl_up_sync(kFull, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) tmp[warp] = inc;
+    __syncthreads();
+    if (tid == 0) {
+        long long acc = 0;
+        for (int w = 0; w < kWarps; ++w) {
+            long long c = tmp[w];
+            tmp[w] = acc;
+            acc += c;
+        }
+        out[m] = acc;
+    }
+    __syncthreads();
+    long long excl = tmp[warp] + inc - s;
+    if (2 * tid < m) out[2 * tid] = excl;
+    if (2 * tid + 1 < m) out[2 * tid + 1] = excl + v0;
+    __syncthreads();
+}
+
+// First live-tile index k with off[k+1] > x (off ascending, off[0] = 0).
+__device__ __forceinline__ int find_tile(const long long* off, int ntl, long long x) {
+    int lo = 0, hi = ntl - 1;
+    while (lo < hi) {
+        int mid = (lo + hi) >> 1;
+        if (off[mid + 1] > x) hi = mid;
+        else lo = mid + 1;
+    }
+    return lo;
+}
+
+// This block's share [lo, hi) of a flattened space of `total` items.
+__device__ __forceinline__ void block_share(long long total, long long& lo, long long& hi) {
+    lo = total * (long long)blockIdx.x / gridDim.x;
+    hi = total * (long long)(blockIdx.x + 1) / gridDim.x;
+}
+
+// ---------------------------------------------------------------------------
+// PREP over candidates [beg, end) of tile t.
 // ---------------------------------------------------------------------------
 struct PrepSh {
-    int warp_cnt[kWarps][4];
-    int base[4];
     double col_oper[kMaxW];
     int col_nodes[kMaxW];
     double vol;
@@ -270,7 +337,7 @@ struct PrepSh {
 };
 
 template <typename T, int W>
-__device__ void prep_phase(const PushArgs& a, int t, TileSh& sh, PrepSh& ps) {
+__device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& ps, long long beg, long long end) {
     constexpr int VEC = (sizeof(T) == 4) ? (W >= 4 ? 4 : W) : (W >= 2 ? 2 : 1);
     constexpr int L = W / VEC;          // lanes per node
     constexpr int GPW = 32 / L;         // nodes per warp iteration
@@ -283,9 +350,8 @@ __device__ void prep_phase(const PushArgs& a, int t, TileSh& sh, PrepSh& ps) {
     const bool hk = method_is_hk(method);
     const bool ign = (kind == KIND_IGN || kind == KIND_UPPR);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int lane_g = threadIdx.x % L, grp_w = lane / L;
+    const int lane_g = lane % L, grp_w = lane / L;
     const int c0 = lane_g * VEC;
-    const int64_t ncand = sh.dense ? n : sh.cand_cnt;
     const int32_t* cand = a.cand + ((int64_t)t * 2 + par) * n;
     int32_t* next = a.cand + ((int64_t)t * 2 + (par ^ 1)) * n;
     int32_t* mark = a.mark + (int64_t)t * n;
@@ -300,91 +366,101 @@ __device__ void prep_phase(const PushArgs& a, int t, TileSh& sh, PrepSh& ps) {
     float* XC = a.kahan ? slab_ptr<float>(a.XC, a, t) : nullptr;
     T* DX = cheby ? slab_ptr<T>(a.DX, a, t) : nullptr;
     const double alpha = sh.tp.alpha;
+    int* next_cnt = &ts.cand_cnt[(sh.level + 1) % 3];
 
     if (threadIdx.x < W) { ps.col_oper[threadIdx.x] = 0.0; ps.col_nodes[threadIdx.x] = 0; }
     if (threadIdx.x == 0) { ps.vol = 0.0; ps.nodes = 0; }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        int np = par ^ 1;
-        ts.cand_cnt[(sh.level + 2) % 3] = 0;
-        ts.front_cnt[np] = 0;
-        ts.small_cnt[np] = 0;
-        ts.med_cnt[np] = 0;
-        ts.large_cnt[np] = 0;
-        ts.union_vol[np] = 0.0;
-    }
-    if (blockIdx.x == 0 && threadIdx.x < W) {
-        a.cs[(int64_t)t * W + threadIdx.x].round_active[par ^ 1] = 0;
-        a.cs[(int64_t)t * W + threadIdx.x].check_cnt[par ^ 1] = 0;
-    }
     __syncthreads();
 
     double my_oper[VEC];
     int my_nodes[VEC];
+    double thr_scale[VEC];
+    bool live[VEC];
 #pragma unroll
-    for (int i = 0; i < VEC; ++i) { my_oper[i] = 0.0; my_nodes[i] = 0; }
+    for (int k = 0; k < VEC; ++k) {
+        my_oper[k] = 0.0;
+        my_nodes[k] = 0;
+        live[k] = sh.col_live[c0 + k] != 0;
+        thr_scale[k] = sh.col_theta[c0 + k];
+    }
     double my_vol = 0.0;
     int my_cnt = 0;
-    int* next_cnt = &ts.cand_cnt[(sh.level + 1) % 3];
 
-    // Warps stride independently over the candidates; the starting warp is
-    // rotated by tile so that short lists spread over SMs.
-    const int64_t nwarps = (int64_t)gridDim.x * kWarps;
-    const int64_t wstart = ((int64_t)blockIdx.x * kWarps + warp + (int64_t)t * 131) % nwarps;
-    for (int64_t base = wstart * GPW; base < ncand; base += nwarps * GPW) {
-        int64_t i = base + grp_w;
-        bool valid = i < ncand;
+    for (long long base = beg + (long long)warp * GPW; base < end; base += (long long)kWarps * GPW) {
+        const long long i = base + grp_w;
+        const bool valid = i < end;
         int u = 0;
         bool act[VEC];
         Vec<T, VEC> push;
 #pragma unroll
         for (int k = 0; k < VEC; ++k) { act[k] = false; push.v[k] = T(0); }
         double du = 1.0;
-        int len = 0;
         bool absorb = false;
+        bool any = false;
+        Vec<T, VEC> r;
         if (valid) {
             u = sh.dense ? (int)i : cand[i];
-            du = g.degd[u];
-            len = g.row_len[u];
             const int64_t off = (int64_t)u * a.ld + c0;
-            Vec<T, VEC> r;
             vload<T, VEC>(R + off, r);
+            // fast test first: most scanned nodes are below every threshold
+            du = g.degf_exact ? (double)g.degf[u] : g.degd[u];
             const double thr_base = (kind == KIND_IGN) ? g.nfac[u] : du;
-            absorb = ign && is_absorbing(g, u);
-            Vec<T, VEC> dxv;
-            if (cheby) vload<T, VEC>(DX + off, dxv);
-            bool any_write = false;
-            Vec<T, VEC> xadd;
 #pragma unroll
             for (int k = 0; k < VEC; ++k) {
-                xadd.v[k] = T(0);
-                const int c = c0 + k;
-                if (!sh.col_live[c]) continue;
+                if (!live[k]) continue;
                 const double rv = (double)r.v[k];
-                double thr;
-                if (hk) thr = ((sh.col_theta[c] * thr_base) / (double)sh.tp.n_levels) / sh.psi;
-                else thr = sh.col_theta[c] * thr_base;
                 bool a_k;
-                if (cheby) {
-                    // ppr_solver.py:642-646 / katz_solver.py:407-411
-                    double tmp;
-                    if (kind == KIND_KATZ) tmp = sh.coef1 * rv - sh.coef2 * (double)dxv.v[k];
-                    else tmp = sh.coef1 * rv + (sh.coef1 - 1.) * (double)dxv.v[k];
-                    a_k = global ? (tmp != 0.0) : (fabs(rv) >= thr);
-                    if (a_k) {
+                if (global) {
+                    a_k = (rv != 0.0);
+                } else {
+                    double thr;
+                    if (hk) thr = ((thr_scale[k] * thr_base) / (double)sh.tp.n_levels) / sh.psi;
+                    else thr = thr_scale[k] * thr_base;
+                    a_k = fabs(rv) >= thr;
+                }
+                act[k] = a_k;
+                any |= a_k;
+            }
+            if (cheby && global) {
+                // global Chebyshev updates every node whose three-term step is non-zero
+                Vec<T, VEC> dxv;
+                vload<T, VEC>(DX + off, dxv);
+#pragma unroll
+                for (int k = 0; k < VEC; ++k) {
+                    if (!live[k]) continue;
+                    act[k] = ((double)r.v[k] != 0.0) || ((double)dxv.v[k] != 0.0);
+                    any |= act[k];
+                }
+            }
+            if (any) {
+                du = g.degd[u];
+                absorb = ign && is_absorbing(g, u);
+                Vec<T, VEC> dxv;
+                if (cheby) vload<T, VEC>(DX + off, dxv);
+                Vec<T, VEC> xadd;
+                bool wrote = false;
+#pragma unroll
+                for (int k = 0; k < VEC; ++k) {
+                    xadd.v[k] = T(0);
+                    if (!act[k]) continue;
+                    const double rv = (double)r.v[k];
+                    if (cheby) {
+                        // ppr_solver.py:642-646 / katz_solver.py:407-411
+                        double tmp;
+                        if (kind == KIND_KATZ) tmp = sh.coef1 * rv - sh.coef2 * (double)dxv.v[k];
+                        else tmp = sh.coef1 * rv + (sh.coef1 - 1.) * (double)dxv.v[k];
+                        if (global && tmp == 0.0) { act[k] = false; continue; }
                         T tmpT = (T)tmp;
                         xadd.v[k] = tmpT;
                         dxv.v[k] = tmpT;
                         r.v[k] = (T)(rv - (double)tmpT);  // rt[u] += -delta_xt[u] (:657)
                         double pv = (kind == KIND_KATZ) ? alpha * (double)tmpT : ((1. - alpha) * (double)tmpT) / du;
                         push.v[k] = (T)pv;
-                    }
-                } else {
-                    a_k = global ? (rv != 0.0) : (fabs(rv) >= thr);
-                    // An absorbing node (threshold 0) is visited once by the
-                    // reference's initial scan and never re-enqueued; with a
-                    // zero residual it has nothing to absorb.
-                    if (absorb && rv == 0.0) a_k = false;
-                    if (a_k) {
+                    } else {
+                        // An absorbing node (threshold 0) is visited once by the
+                        // reference's initial scan and never re-enqueued; with a
+                        // zero residual it has nothing to absorb.
+                        if (absorb && rv == 0.0) { act[k] = false; continue; }
                         double pv;
                         if (kind == KIND_PPR || kind == KIND_UPPR) pv = ((1. - alpha) * rv) / du;
                         else if (kind == KIND_KATZ) pv = alpha * rv;
@@ -399,107 +475,105 @@ __device__ void prep_phase(const PushArgs& a, int t, TileSh& sh, PrepSh& ps) {
                         xadd.v[k] = (kind == KIND_IGN && !absorb) ? (T)(sh.tp.x_gain * rv) : r.v[k];
                         r.v[k] = T(0);
                     }
-                }
-                act[k] = a_k;
-                if (a_k) {
-                    any_write = true;
+                    wrote = true;
                     my_nodes[k] += 1;
                     if (!absorb) my_oper[k] += du;
                 }
-            }
-            if (any_write) {
-                vstore<T, VEC>(R + off, r);
-                if (cheby) vstore<T, VEC>(DX + off, dxv);
-                Vec<T, VEC> xv;
-                vload<T, VEC>(X + off, xv);
-                if (absorb) {
-                    // p[u] = r[u]; r[u] = 0 for an absorbing node (InstantGNN.py:22-25)
+                if (wrote) {
+                    vstore<T, VEC>(R + off, r);
+                    if (cheby) vstore<T, VEC>(DX + off, dxv);
+                    Vec<T, VEC> xv;
+                    vload<T, VEC>(X + off, xv);
+                    if (absorb) {
+                        // p[u] = r[u]; r[u] = 0 for an absorbing node (InstantGNN.py:22-25)
 #pragma unroll
-                    for (int k = 0; k < VEC; ++k)
-                        if (act[k]) {
-                            xv.v[k] = xadd.v[k];
-                            if (XC) XC[off + k] = 0.f;
-                        }
-                } else if (XC) {
-                    // Kahan-compensated FP32 accumulation of the solution
+                        for (int k = 0; k < VEC; ++k)
+                            if (act[k]) {
+                                xv.v[k] = xadd.v[k];
+                                if (XC) XC[off + k] = 0.f;
+                            }
+                    } else if (XC) {
+                        // Kahan-compensated FP32 accumulation of the solution
 #pragma unroll
-                    for (int k = 0; k < VEC; ++k)
-                        if (act[k]) {
-                            float cc = XC[off + k];
-                            float y = (float)xadd.v[k] - cc;
-                            float s = (float)xv.v[k] + y;
-                            XC[off + k] = (s - (float)xv.v[k]) - y;
-                            xv.v[k] = (T)s;
-                        }
-                } else {
+                        for (int k = 0; k < VEC; ++k)
+                            if (act[k]) {
+                                float cc = XC[off + k];
+                                float y = (float)xadd.v[k] - cc;
+                                float s = (float)xv.v[k] + y;
+                                XC[off + k] = (s - (float)xv.v[k]) - y;
+                                xv.v[k] = (T)s;
+                            }
+                    } else {
 #pragma unroll
-                    for (int k = 0; k < VEC; ++k)
-                        if (act[k]) xv.v[k] = xv.v[k] + xadd.v[k];
+                        for (int k = 0; k < VEC; ++k)
+                            if (act[k]) xv.v[k] = xv.v[k] + xadd.v[k];
+                    }
+                    vstore<T, VEC>(X + off, xv);
                 }
-                vstore<T, VEC>(X + off, xv);
+                any = false;
+#pragma unroll
+                for (int k = 0; k < VEC; ++k) any |= act[k];
             }
         }
         // ---- node-level frontier decision (OR over the lane group) ----
-        bool any = false;
-#pragma unroll
-        for (int k = 0; k < VEC; ++k) any |= act[k];
-        unsigned bal = __ballot_sync(kFull, any);
-        unsigned gmask = ((L == 32) ? kFull : ((1u << L) - 1u)) << (grp_w * L);
-        bool node_act = valid && (bal & gmask) != 0;
-        bool leader = (lane_g == 0);
+        const unsigned bal = __ballot_sync(kFull, any);
+        if (bal == 0) continue;  // warp-uniform: nothing active in this warp
+        const unsigned gmask = ((L == 32) ? kFull : ((1u << L) - 1u)) << (grp_w * L);
+        const bool node_act = valid && (bal & gmask) != 0;
+        const bool leader = (lane_g == 0);
         // Chebyshev moves r[u] by -dx[u]: u itself is a candidate next round
         if (cheby && !global) append_once(leader && node_act, u, mark, sh.stamp, next, next_cnt, kFull);
-        bool node_in = node_act && !absorb;  // absorbed nodes do not push
+        const bool node_in = node_act && !absorb;  // absorbed nodes do not push
+        int len = 0;
         int nch = 0;
-        int bucket = -1;  // 0 small, 1 medium, 2 large
-        if (node_in) {
+        int bucket = -1;  // 0 short, 1 medium, 2 long
+        if (node_in && leader) {
+            len = g.row_len[u];
             if (len <= a.small_max) bucket = 0;
             else if (len <= a.med_max) bucket = 1;
             else { bucket = 2; nch = (len + a.chunk - 1) / a.chunk; }
         }
-        unsigned bf = __ballot_sync(kFull, leader && node_in);
-        unsigned bs = __ballot_sync(kFull, leader && bucket == 0);
-        unsigned bm = __ballot_sync(kFull, leader && bucket == 1);
-        int lch = (leader && bucket == 2) ? nch : 0;
+        const unsigned bf = __ballot_sync(kFull, leader && node_in);
+        if (bf == 0) continue;
+        const unsigned bs = __ballot_sync(kFull, bucket == 0);
+        const unsigned bm = __ballot_sync(kFull, bucket == 1);
+        int lch = (bucket == 2) ? nch : 0;
         int sc = lch;  // inclusive warp scan of chunk counts
 #pragma unroll
         for (int o = 1; o < 32; o <<= 1) {
             int y = __shfl_up_sync(kFull, sc, o);
             if (lane >= o) sc += y;
         }
-        int wch = __shfl_sync(kFull, sc, 31);
-        // one global atomic per non-empty list per warp
+        const int wch = __shfl_sync(kFull, sc, 31);
         int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
-        if (lane == 0 && bf) {
+        if (lane == 0) {
             b0 = atomicAdd(&ts.front_cnt[par], __popc(bf));
             if (bs) b1 = atomicAdd(&ts.small_cnt[par], __popc(bs));
             if (bm) b2 = atomicAdd(&ts.med_cnt[par], __popc(bm));
             if (wch) b3 = atomicAdd(&ts.large_cnt[par], wch);
         }
-        unsigned below = (1u << lane) - 1u;
+        b0 = __shfl_sync(kFull, b0, 0);
+        b1 = __shfl_sync(kFull, b1, 0);
+        b2 = __shfl_sync(kFull, b2, 0);
+        b3 = __shfl_sync(kFull, b3, 0);
+        const unsigned below = (1u << lane) - 1u;
         int fidx = 0;
-        if (bf) {
-            b0 = __shfl_sync(kFull, b0, 0);
-            b1 = __shfl_sync(kFull, b1, 0);
-            b2 = __shfl_sync(kFull, b2, 0);
-            b3 = __shfl_sync(kFull, b3, 0);
-            if (leader && node_in) {
-                fidx = b0 + __popc(bf & below);
-                front[fidx] = u;
-                if (bucket == 0) bsmall[b1 + __popc(bs & below)] = fidx;
-                else if (bucket == 1) bmed[b2 + __popc(bm & below)] = fidx;
-                else {
-                    int lb = b3 + (sc - lch);
-                    for (int ch = 0; ch < nch; ++ch) blarge[lb + ch] = make_int2(fidx, ch);
-                }
-                my_vol += du;
-                my_cnt += 1;
+        if (leader && node_in) {
+            fidx = b0 + __popc(bf & below);
+            front[fidx] = u;
+            if (bucket == 0) bsmall[b1 + __popc(bs & below)] = fidx;
+            else if (bucket == 1) bmed[b2 + __popc(bm & below)] = fidx;
+            else {
+                int lb = b3 + (sc - lch);
+                for (int ch = 0; ch < nch; ++ch) blarge[lb + ch] = make_int2(fidx, ch);
             }
-            fidx = __shfl_sync(kFull, fidx, grp_w * L);
-            if (node_in) vstore<T, VEC>(Pw + (int64_t)fidx * W + c0, push);
+            my_vol += du;
+            my_cnt += 1;
         }
+        fidx = __shfl_sync(kFull, fidx, grp_w * L);
+        if (node_in) vstore<T, VEC>(Pw + (int64_t)fidx * W + c0, push);
     }
-    // ---- flush per-column counters ----
+    // ---- flush per-column counters (one global atomic per column per block) ----
 #pragma unroll
     for (int k = 0; k < VEC; ++k) {
         if (my_nodes[k]) {
@@ -525,13 +599,67 @@ __device__ void prep_phase(const PushArgs& a, int t, TileSh& sh, PrepSh& ps) {
         atomicAdd(&a.stats->union_nodes, (unsigned long long)ps.nodes);
         atomicAdd(&a.stats->union_vol, ps.vol);
     }
-    if (threadIdx.x == 0 && blockIdx.x == 0) atomicAdd(&a.stats->cand_nodes, (unsigned long long)ncand);
     __syncthreads();
 }
 
+// Zero the counters a tile's next round will fill (block 0, before PREP
+// work; these fields were last used a round ago, see gde_common.cuh).
+template <int W>
+__device__ void zero_next_counters(const PushArgs& a, int t, int level) {
+    TileState& ts = a.ts[t];
+    const int np = (level & 1) ^ 1;
+    if (threadIdx.x == 0) {
+        ts.cand_cnt[(level + 2) % 3] = 0;
+        ts.front_cnt[np] = 0;
+        ts.small_cnt[np] = 0;
+        ts.med_cnt[np] = 0;
+        ts.large_cnt[np] = 0;
+        ts.union_vol[np] = 0.0;
+    }
+    if (threadIdx.x < W) {
+        a.cs[(int64_t)t * W + threadIdx.x].round_active[np] = 0;
+        a.cs[(int64_t)t * W + threadIdx.x].check_cnt[np] = 0;
+    }
+}
+
 // ---------------------------------------------------------------------------
-// SCATTER phase
+// SCATTER pieces (tile t, its scatter flags and level)
 // ---------------------------------------------------------------------------
+template <typename T, int W>
+struct ScatterCtx {
+    T* tgt;
+    const T* Pw;
+    const int32_t* front;
+    int32_t* mark;
+    int32_t* next;
+    int* next_cnt;
+    int stamp;
+    bool track;
+    bool tgt_scale;
+};
+
+template <typename T, int W>
+__device__ __forceinline__ ScatterCtx<T, W> scatter_ctx(const PushArgs& a, int t, int level, unsigned char flags) {
+    ScatterCtx<T, W> c;
+    const int64_t n = a.g.n;
+    const int par = level & 1;
+    if (flags & SF_HK) {
+        if (flags & SF_FINAL) c.tgt = slab_ptr<T>(a.X, a, t);
+        else c.tgt = slab_ptr<T>((level & 1) ? a.R : a.R2, a, t);
+    } else {
+        c.tgt = slab_ptr<T>(a.R, a, t);
+    }
+    c.Pw = reinterpret_cast<const T*>(a.P) + (int64_t)t * n * W;
+    c.front = a.front + (int64_t)t * n;
+    c.mark = a.mark + (int64_t)t * n;
+    c.next = a.cand + ((int64_t)t * 2 + (par ^ 1)) * n;
+    c.next_cnt = &a.ts[t].cand_cnt[(level + 1) % 3];
+    c.stamp = a.ts[t].stamp + level + 1;
+    c.track = (flags & SF_TRACK) != 0;
+    c.tgt_scale = (flags & SF_TGTSCALE) != 0;
+    return c;
+}
+
 template <typename T, int VEC>
 __device__ __forceinline__ void push_edge(const DevGraph& g, T* tgt, int64_t ld, int c0, int v, const Vec<T, VEC>& p,
                                           bool tgt_scale) {
@@ -545,156 +673,136 @@ __device__ __forceinline__ void push_edge(const DevGraph& g, T* tgt, int64_t ld,
     vred<T, VEC>(tgt + (int64_t)v * ld + c0, q);
 }
 
+// long rows: the whole CTA pushes chunks [beg, end) of tile t
 template <typename T, int W>
-__device__ void scatter_phase(const PushArgs& a, int t, TileSh& sh) {
+__device__ void scatter_large(const PushArgs& a, int t, const ScatterCtx<T, W>& c, long long beg, long long end) {
+    constexpr int VEC = (sizeof(T) == 4) ? (W >= 4 ? 4 : W) : (W >= 2 ? 2 : 1);
+    constexpr int L = W / VEC;
+    const DevGraph& g = a.g;
+    const int lane_g = threadIdx.x % L;
+    const int c0 = lane_g * VEC;
+    const int2* blarge = a.blarge + (int64_t)t * a.large_cap;
+    for (long long k = beg; k < end; ++k) {
+        const int2 e = blarge[k];
+        const int u = c.front[e.x];
+        const int64_t rp = g.row_ptr[u];
+        const int len = g.row_len[u];
+        const int b = e.y * a.chunk;
+        const int en = min(len, b + a.chunk);
+        Vec<T, VEC> p;
+        vload<T, VEC>(c.Pw + (int64_t)e.x * W + c0, p);
+        const int gidx = threadIdx.x / L;
+        for (int j0 = b; j0 < en; j0 += kThreads / L) {
+            const int j = j0 + gidx;
+            const bool ok = j < en;
+            const int v = ok ? g.col[rp + j] : 0;
+            if (ok) push_edge<T, VEC>(g, c.tgt, a.ld, c0, v, p, c.tgt_scale);
+            if (c.track) append_once(ok && lane_g == 0, v, c.mark, c.stamp, c.next, c.next_cnt, kFull);
+        }
+    }
+}
+
+// medium rows: one warp per row, rows [beg, end) of tile t
+template <typename T, int W>
+__device__ void scatter_med(const PushArgs& a, int t, const ScatterCtx<T, W>& c, long long beg, long long end) {
     constexpr int VEC = (sizeof(T) == 4) ? (W >= 4 ? 4 : W) : (W >= 2 ? 2 : 1);
     constexpr int L = W / VEC;
     constexpr int GPW = 32 / L;
     const DevGraph& g = a.g;
-    const int64_t n = g.n;
-    const int par = sh.parity;
-    const int kind = sh.tp.kind, method = sh.tp.method;
-    const bool hk = method_is_hk(method);
-    const bool global = method_is_global(method);
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int lane_g = threadIdx.x % L, grp_w = lane / L;
+    const int lane_g = lane % L, grp_w = lane / L;
     const int c0 = lane_g * VEC;
-    TileState& ts = a.ts[t];
-    const int32_t* front = a.front + (int64_t)t * n;
-    const T* Pw = reinterpret_cast<const T*>(a.P) + (int64_t)t * n * W;
-    const int32_t* bsmall = a.bsmall + (int64_t)t * n;
-    const int32_t* bmed = a.bmed + (int64_t)t * n;
-    const int2* blarge = a.blarge + (int64_t)t * a.large_cap;
-    int32_t* mark = a.mark + (int64_t)t * n;
-    int32_t* next = a.cand + ((int64_t)t * 2 + (par ^ 1)) * n;
-    int* next_cnt = &ts.cand_cnt[(sh.level + 1) % 3];
-    T* Tgt;
-    if (hk) {
-        if (sh.final_level) Tgt = slab_ptr<T>(a.X, a, t);
-        else Tgt = slab_ptr<T>((sh.level & 1) ? a.R : a.R2, a, t);
-    } else {
-        Tgt = slab_ptr<T>(a.R, a, t);
-    }
-    // Does the next round scan densely?  Every block decides identically.
-    // Thresholds can drop between solves (a dynamic-graph update lowers d^(1-b)),
-    // so update pushes keep the reference's touched-only rule (allow_dense = 0).
-    const bool dense_next =
-        global || (a.allow_dense && ts.union_vol[par] * (double)a.dense_div > (double)n);
-    const bool track = !dense_next && !sh.final_level && !(method == M_HK_TAYLOR && hk_last_level(sh));
-    const bool tgt_scale = (kind == KIND_IGN);
-    const int stamp = sh.stamp;
-    // the last Taylor level only adds r into x (hk_solver.py:74-75): no push
-    const bool no_push = (method == M_HK_TAYLOR) && hk_last_level(sh);
-
-    // ---- long rows: one CTA per chunk of a.chunk edges ----
-    if (sh.large_cnt > 0 && !no_push) {
-        for (int k = blockIdx.x; k < sh.large_cnt; k += gridDim.x) {
-            int2 e = blarge[k];
-            int u = front[e.x];
-            int64_t rp = g.row_ptr[u];
-            int len = g.row_len[u];
-            int beg = e.y * a.chunk;
-            int end = min(len, beg + a.chunk);
-            Vec<T, VEC> p;
-            vload<T, VEC>(Pw + (int64_t)e.x * W + c0, p);
-            const int gidx = threadIdx.x / L;
-            for (int j0 = beg; j0 < end; j0 += kThreads / L) {
-                int j = j0 + gidx;
-                bool ok = j < end;
-                int v = ok ? g.col[rp + j] : 0;
-                if (ok) push_edge<T, VEC>(g, Tgt, a.ld, c0, v, p, tgt_scale);
-                if (track) append_once(ok && lane_g == 0, v, mark, stamp, next, next_cnt, kFull);
-            }
+    const int32_t* bmed = a.bmed + (int64_t)t * a.g.n;
+    for (long long k = beg + warp; k < end; k += kWarps) {
+        const int f = bmed[k];
+        const int u = c.front[f];
+        const int64_t rp = g.row_ptr[u];
+        const int len = g.row_len[u];
+        Vec<T, VEC> p;
+        vload<T, VEC>(c.Pw + (int64_t)f * W + c0, p);
+        for (int j0 = 0; j0 < len; j0 += GPW) {
+            const int j = j0 + grp_w;
+            const bool ok = j < len;
+            const int v = ok ? g.col[rp + j] : 0;
+            if (ok) push_edge<T, VEC>(g, c.tgt, a.ld, c0, v, p, c.tgt_scale);
+            if (c.track) append_once(ok && lane_g == 0, v, c.mark, c.stamp, c.next, c.next_cnt, kFull);
         }
-    }
-    // ---- medium rows: one warp per row ----
-    if (sh.med_cnt > 0 && !no_push) {
-        const int64_t gw = (int64_t)blockIdx.x * kWarps + warp;
-        const int64_t nw = (int64_t)gridDim.x * kWarps;
-        const int64_t wstart = (gw + (int64_t)t * 131) % nw;
-        for (int64_t k = wstart; k < sh.med_cnt; k += nw) {
-            int f = bmed[k];
-            int u = front[f];
-            int64_t rp = g.row_ptr[u];
-            int len = g.row_len[u];
-            Vec<T, VEC> p;
-            vload<T, VEC>(Pw + (int64_t)f * W + c0, p);
-            for (int j0 = 0; j0 < len; j0 += GPW) {
-                int j = j0 + grp_w;
-                bool ok = j < len;
-                int v = ok ? g.col[rp + j] : 0;
-                if (ok) push_edge<T, VEC>(g, Tgt, a.ld, c0, v, p, tgt_scale);
-                if (track) append_once(ok && lane_g == 0, v, mark, stamp, next, next_cnt, kFull);
-            }
-        }
-    }
-    // ---- short rows: one lane group per row ----
-    if (sh.small_cnt > 0 && !no_push) {
-        const int64_t nw = (int64_t)gridDim.x * kWarps;
-        const int64_t wstart = (((int64_t)blockIdx.x * kWarps + warp) + (int64_t)t * 131) % nw;
-        for (int64_t kb = wstart * GPW; kb < sh.small_cnt; kb += nw * GPW) {
-            int64_t k = kb + grp_w;
-            bool okr = k < sh.small_cnt;
-            int len = 0;
-            int64_t rp = 0;
-            Vec<T, VEC> p;
-#pragma unroll
-            for (int i = 0; i < VEC; ++i) p.v[i] = T(0);
-            if (okr) {
-                int f = bsmall[k];
-                int u = front[f];
-                rp = g.row_ptr[u];
-                len = g.row_len[u];
-                vload<T, VEC>(Pw + (int64_t)f * W + c0, p);
-            }
-            int maxlen = len;
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(kFull, maxlen, o));
-            for (int j = 0; j < maxlen; ++j) {
-                bool ok = j < len;
-                int v = ok ? g.col[rp + j] : 0;
-                if (ok) push_edge<T, VEC>(g, Tgt, a.ld, c0, v, p, tgt_scale);
-                if (track) append_once(ok && lane_g == 0, v, mark, stamp, next, next_cnt, kFull);
-            }
-        }
-    }
-    // ---- HK: drop this level's sub-threshold residuals (hk_solver.py:284) ----
-    if (hk) {
-        T* Rcur = slab_ptr<T>((sh.level & 1) ? a.R2 : a.R, a, t);
-        if (sh.dense) {
-            for (int64_t u = (int64_t)blockIdx.x * kThreads + threadIdx.x; u < n; u += (int64_t)gridDim.x * kThreads)
-                for (int c = 0; c < W; ++c) Rcur[u * a.ld + c] = T(0);
-        } else {
-            const int32_t* cand = a.cand + ((int64_t)t * 2 + par) * n;
-            for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < sh.cand_cnt;
-                 i += (int64_t)gridDim.x * kThreads) {
-                int u = cand[i];
-                for (int c = 0; c < W; ++c) Rcur[(int64_t)u * a.ld + c] = T(0);
-            }
-        }
-    }
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        ts.dense_next[par ^ 1] = dense_next ? 1 : 0;
-        atomicAdd(&a.stats->rounds, 1ull);
-        if (dense_next) atomicAdd(&a.stats->dense_rounds, 1ull);
     }
 }
 
-// Round bookkeeping by block 0 (fields read only at the next round start):
-// a local column with no active node this round is finished
+// short rows: one lane group per row, rows [beg, end) of tile t
+template <typename T, int W>
+__device__ void scatter_small(const PushArgs& a, int t, const ScatterCtx<T, W>& c, long long beg, long long end) {
+    constexpr int VEC = (sizeof(T) == 4) ? (W >= 4 ? 4 : W) : (W >= 2 ? 2 : 1);
+    constexpr int L = W / VEC;
+    constexpr int GPW = 32 / L;
+    const DevGraph& g = a.g;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane_g = lane % L, grp_w = lane / L;
+    const int c0 = lane_g * VEC;
+    const int32_t* bsmall = a.bsmall + (int64_t)t * a.g.n;
+    for (long long kb = beg + (long long)warp * GPW; kb < end; kb += (long long)kWarps * GPW) {
+        const long long k = kb + grp_w;
+        const bool okr = k < end;
+        int len = 0;
+        int64_t rp = 0;
+        Vec<T, VEC> p;
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) p.v[i] = T(0);
+        if (okr) {
+            const int f = bsmall[k];
+            const int u = c.front[f];
+            rp = g.row_ptr[u];
+            len = g.row_len[u];
+            vload<T, VEC>(c.Pw + (int64_t)f * W + c0, p);
+        }
+        int maxlen = len;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(kFull, maxlen, o));
+        for (int j = 0; j < maxlen; ++j) {
+            const bool ok = j < len;
+            const int v = ok ? g.col[rp + j] : 0;
+            if (ok) push_edge<T, VEC>(g, c.tgt, a.ld, c0, v, p, c.tgt_scale);
+            if (c.track) append_once(ok && lane_g == 0, v, c.mark, c.stamp, c.next, c.next_cnt, kFull);
+        }
+    }
+}
+
+// HK: drop this level's sub-threshold residuals (hk_solver.py:284); the
+// frontier's own entries were already moved into x.
+template <typename T, int W>
+__device__ void hk_drop(const PushArgs& a, int t, int level, bool dense, int cand_cnt) {
+    const int64_t n = a.g.n;
+    T* Rcur = slab_ptr<T>((level & 1) ? a.R2 : a.R, a, t);
+    const int64_t stride = (int64_t)gridDim.x * kThreads;
+    if (dense) {
+        for (int64_t u = (int64_t)blockIdx.x * kThreads + threadIdx.x; u < n; u += stride)
+            for (int c = 0; c < W; ++c) Rcur[u * a.ld + c] = T(0);
+    } else {
+        const int32_t* cand = a.cand + ((int64_t)t * 2 + (level & 1)) * n;
+        for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < cand_cnt; i += stride) {
+            const int u = cand[i];
+            for (int c = 0; c < W; ++c) Rcur[(int64_t)u * a.ld + c] = T(0);
+        }
+    }
+}
+
+// Round bookkeeping for tile t by block 0 (fields read only at the next
+// round's start): a local column with no active node this round is finished
 // (ppr_solver.py:266-267); a global column whose CHECK found nothing above
 // threshold is finished (:292-293); HK stops after its last level
 // (hk_solver.py:235); a tile is done when its frontier is empty.
 template <int W>
-__device__ void finish_round(const PushArgs& a, int t, const TileSh& sh) {
-    if (blockIdx.x != 0) return;
-    const int m = sh.tp.method;
+__device__ void finish_round(const PushArgs& a, int t, int level, bool dense_next) {
+    const TileParams& tp = a.tp[t];
+    const int m = tp.method;
+    const int par = level & 1;
     const bool gcheck = (m == M_GLOBAL_GD || m == M_GLOBAL_CHEBY);
-    const bool hk_end = method_is_hk(m) && hk_last_level(sh);
-    if (threadIdx.x < W && threadIdx.x < sh.tp.ncols) {
+    const bool hk_end = method_is_hk(m) && ((m == M_HK_TAYLOR) ? (level >= tp.n_levels) : (level + 1 >= tp.n_levels));
+    if (threadIdx.x < W && threadIdx.x < tp.ncols) {
         ColState& cs = a.cs[(int64_t)t * W + threadIdx.x];
         if (cs.live) {
-            bool worked = gcheck ? (cs.check_cnt[sh.parity] > 0) : (cs.round_active[sh.parity] > 0);
+            bool worked = gcheck ? (cs.check_cnt[par] > 0) : (cs.round_active[par] > 0);
             if (method_is_hk(m) && m != M_HK_LOCAL) worked = true;  // fixed sweeps per level
             if (worked) cs.rounds += 1;
             if (!worked || hk_end) {
@@ -704,43 +812,54 @@ __device__ void finish_round(const PushArgs& a, int t, const TileSh& sh) {
         }
     }
     if (threadIdx.x == 0) {
-        if (a.ts[t].front_cnt[sh.parity] == 0 || hk_end) a.ts[t].done = 1;
+        TileState& ts = a.ts[t];
+        ts.dense_next[par ^ 1] = dense_next ? 1 : 0;
+        if (ts.front_cnt[par] == 0 || hk_end) ts.done = 1;
+        atomicAdd(&a.stats->rounds, 1ull);
+        if (dense_next) atomicAdd(&a.stats->dense_rounds, 1ull);
     }
 }
 
 template <typename T, int W>
-__global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
+__global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
     __shared__ TileSh sh;
     __shared__ PrepSh ps;
+    __shared__ RoundSh rs;
     __shared__ int s_cnt[kMaxW];
-    __shared__ unsigned s_live[kMaxTiles / 32];
-    __shared__ int s_any, s_check;
+    __shared__ long long s_vals[kMaxLaunchTiles];
+    const int64_t n = a.g.n;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.stats->start_ns = globaltimer_ns();
     int it = 0;
     for (; it < a.round_budget; ++it) {
-        // ---- snapshot of live tiles for this round ----
-        if (threadIdx.x == 0) { s_any = 0; s_check = 0; }
-        for (int w = threadIdx.x; w < (a.ntiles + 31) / 32; w += kThreads) s_live[w] = 0;
-        __syncthreads();
+        // ---- live tiles of this round (identical in every block) ----
+        if (threadIdx.x == 0) rs.any_check = 0;
         for (int t = threadIdx.x; t < a.ntiles; t += kThreads) {
             const TileState& ts = a.ts[t];
-            bool live = !ts.done && (ts.round + it) < a.max_rounds;
-            if (live) {
-                atomicOr(&s_live[t >> 5], 1u << (t & 31));
-                int m = a.tp[t].method;
-                if (m == M_GLOBAL_GD || m == M_GLOBAL_CHEBY) s_check = 1;
-                s_any = 1;
-            }
+            const bool live = !ts.done && (ts.round + it) < a.max_rounds;
+            s_vals[t] = live ? 1 : 0;
         }
         __syncthreads();
-        if (!s_any) break;
+        block_exclusive_scan(s_vals, a.ntiles, rs.off[0], rs.scan_tmp);
+        for (int t = threadIdx.x; t < a.ntiles; t += kThreads) {
+            if (rs.off[0][t + 1] != rs.off[0][t]) {
+                const int k = (int)rs.off[0][t];
+                rs.tiles[k] = t;
+                rs.level[k] = a.ts[t].round + it;
+                const int m = a.tp[t].method;
+                if (m == M_GLOBAL_GD || m == M_GLOBAL_CHEBY) rs.any_check = 1;
+            }
+        }
+        if (threadIdx.x == 0) rs.ntl = (int)rs.off[0][a.ntiles];
+        __syncthreads();
+        const int ntl = rs.ntl;
+        if (ntl == 0) break;
         const bool timer = (blockIdx.x == 0 && threadIdx.x == 0);
         unsigned long long t0 = timer ? globaltimer_ns() : 0ull;
         // ---- CHECK (global GD / Chebyshev tiles) ----
-        if (s_check) {
-            for (int t = 0; t < a.ntiles; ++t) {
-                if (!(s_live[t >> 5] & (1u << (t & 31)))) continue;
-                int m = a.tp[t].method;
+        if (rs.any_check) {
+            for (int k = 0; k < ntl; ++k) {
+                const int t = rs.tiles[k];
+                const int m = a.tp[t].method;
                 if (m != M_GLOBAL_GD && m != M_GLOBAL_CHEBY) continue;
                 check_phase<T, W>(a, t, it, s_cnt);
             }
@@ -751,11 +870,29 @@ __global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
                 t0 = t1;
             }
         }
-        // ---- PREP ----
-        for (int t = 0; t < a.ntiles; ++t) {
-            if (!(s_live[t >> 5] & (1u << (t & 31)))) continue;
-            load_tile<W>(a, t, it, sh);
-            prep_phase<T, W>(a, t, sh, ps);
+        // ---- PREP: flattened candidates of all live tiles ----
+        if (blockIdx.x == 0) {
+            for (int k = 0; k < ntl; ++k) zero_next_counters<W>(a, rs.tiles[k], rs.level[k]);
+        }
+        for (int k = threadIdx.x; k < ntl; k += kThreads) {
+            const TileState& ts = a.ts[rs.tiles[k]];
+            const int lv = rs.level[k];
+            s_vals[k] = ts.dense_next[lv & 1] ? n : ts.cand_cnt[lv % 3];
+        }
+        __syncthreads();
+        block_exclusive_scan(s_vals, ntl, rs.off[0], rs.scan_tmp);
+        {
+            long long lo, hi;
+            block_share(rs.off[0][ntl], lo, hi);
+            if (lo < hi) {
+                for (int k = find_tile(rs.off[0], ntl, lo); k < ntl && rs.off[0][k] < hi; ++k) {
+                    const long long b = max(lo, rs.off[0][k]) - rs.off[0][k];
+                    const long long e = min(hi, rs.off[0][k + 1]) - rs.off[0][k];
+                    if (b >= e) continue;
+                    load_tile<W>(a, rs.tiles[k], it, sh);
+                    prep_range<T, W>(a, rs.tiles[k], sh, ps, b, e);
+                }
+            }
         }
         if (!grid_barrier(a.bar, a.err)) return;
         if (timer) {
@@ -763,13 +900,81 @@ __global__ void __launch_bounds__(kThreads) push_kernel(PushArgs a) {
             a.stats->prep_ns += t1 - t0;
             t0 = t1;
         }
-        // ---- SCATTER + bookkeeping ----
-        for (int t = 0; t < a.ntiles; ++t) {
-            if (!(s_live[t >> 5] & (1u << (t & 31)))) continue;
-            load_tile<W>(a, t, it, sh);
-            if (sh.front_cnt > 0) scatter_phase<T, W>(a, t, sh);
-            finish_round<W>(a, t, sh);
-            __syncthreads();
+        // ---- SCATTER: flattened short rows / medium rows / long-row chunks ----
+        for (int k = threadIdx.x; k < ntl; k += kThreads) {
+            const int t = rs.tiles[k];
+            const TileState& ts = a.ts[t];
+            const TileParams& tp = a.tp[t];
+            const int lv = rs.level[k];
+            const int par = lv & 1;
+            const int m = tp.method;
+            const bool hk = method_is_hk(m);
+            const bool global = method_is_global(m);
+            const bool fin = hk && (m != M_HK_TAYLOR) && (lv + 1 == tp.n_levels);
+            const bool last_taylor = (m == M_HK_TAYLOR) && (lv >= tp.n_levels);
+            const bool dnext = global || (a.allow_dense && ts.union_vol[par] * (double)a.dense_div > (double)n);
+            unsigned char f = 0;
+            if (hk) f |= SF_HK;
+            if (fin) f |= SF_FINAL;
+            if (last_taylor) f |= SF_NOPUSH;
+            if (tp.kind == KIND_IGN) f |= SF_TGTSCALE;
+            if (!dnext && !fin && !last_taylor && !(m == M_HK_TAYLOR && lv + 1 >= tp.n_levels + 1)) f |= SF_TRACK;
+            rs.flags[k] = f;
+            const bool has = ts.front_cnt[par] > 0 && !last_taylor;
+            s_vals[k] = has ? ts.small_cnt[par] : 0;
+        }
+        __syncthreads();
+        block_exclusive_scan(s_vals, ntl, rs.off[0], rs.scan_tmp);
+        for (int k = threadIdx.x; k < ntl; k += kThreads) {
+            const TileState& ts = a.ts[rs.tiles[k]];
+            const int par = rs.level[k] & 1;
+            s_vals[k] = (ts.front_cnt[par] > 0 && !(rs.flags[k] & SF_NOPUSH)) ? ts.med_cnt[par] : 0;
+        }
+        __syncthreads();
+        block_exclusive_scan(s_vals, ntl, rs.off[1], rs.scan_tmp);
+        for (int k = threadIdx.x; k < ntl; k += kThreads) {
+            const TileState& ts = a.ts[rs.tiles[k]];
+            const int par = rs.level[k] & 1;
+            s_vals[k] = (ts.front_cnt[par] > 0 && !(rs.flags[k] & SF_NOPUSH)) ? ts.large_cnt[par] : 0;
+        }
+        __syncthreads();
+        block_exclusive_scan(s_vals, ntl, rs.off[2], rs.scan_tmp);
+        // long-row chunks first (largest pieces), then medium, then short rows
+        for (int sp = 2; sp >= 0; --sp) {
+            const long long* off = rs.off[sp];
+            long long lo, hi;
+            block_share(off[ntl], lo, hi);
+            if (lo >= hi) continue;
+            for (int k = find_tile(off, ntl, lo); k < ntl && off[k] < hi; ++k) {
+                const long long b = max(lo, off[k]) - off[k];
+                const long long e = min(hi, off[k + 1]) - off[k];
+                if (b >= e) continue;
+                const int t = rs.tiles[k];
+                const ScatterCtx<T, W> c = scatter_ctx<T, W>(a, t, rs.level[k], rs.flags[k]);
+                if (sp == 2) scatter_large<T, W>(a, t, c, b, e);
+                else if (sp == 1) scatter_med<T, W>(a, t, c, b, e);
+                else scatter_small<T, W>(a, t, c, b, e);
+            }
+        }
+        // HK level drop (touches the current level's slab only)
+        for (int k = 0; k < ntl; ++k) {
+            if (!(rs.flags[k] & SF_HK)) continue;
+            const int t = rs.tiles[k];
+            const int lv = rs.level[k];
+            const TileState& ts = a.ts[t];
+            if (ts.front_cnt[lv & 1] == 0) continue;
+            hk_drop<T, W>(a, t, lv, ts.dense_next[lv & 1] != 0, ts.cand_cnt[lv % 3]);
+        }
+        if (blockIdx.x == 0) {
+            for (int k = 0; k < ntl; ++k) {
+                const int t = rs.tiles[k];
+                const int lv = rs.level[k];
+                const TileParams& tp = a.tp[t];
+                const bool dnext = method_is_global(tp.method) ||
+                                   (a.allow_dense && a.ts[t].union_vol[lv & 1] * (double)a.dense_div > (double)n);
+                finish_round<W>(a, t, lv, dnext);
+                __syncthreads();
+            }
         }
         if (!grid_barrier(a.bar, a.err)) return;
         if (timer) a.stats->scatter_ns += globaltimer_ns() - t0;
