@@ -134,6 +134,23 @@ __device__ __forceinline__ void vred<float, 2>(float* p, const Vec<float, 2>& o)
     atomicAdd(reinterpret_cast<float2*>(p), make_float2(o.v[0], o.v[1]));
 }
 
+// atomic add of VEC contiguous values returning the previous values
+template <typename T, int VEC>
+__device__ __forceinline__ void vatomic_ret(T* p, const Vec<T, VEC>& o, Vec<T, VEC>& old) {
+#pragma unroll
+    for (int i = 0; i < VEC; ++i) old.v[i] = (o.v[i] != T(0)) ? atomicAdd(p + i, o.v[i]) : T(0);
+}
+template <>
+__device__ __forceinline__ void vatomic_ret<float, 4>(float* p, const Vec<float, 4>& o, Vec<float, 4>& old) {
+    float4 r = atomicAdd(reinterpret_cast<float4*>(p), make_float4(o.v[0], o.v[1], o.v[2], o.v[3]));
+    old.v[0] = r.x; old.v[1] = r.y; old.v[2] = r.z; old.v[3] = r.w;
+}
+template <>
+__device__ __forceinline__ void vatomic_ret<float, 2>(float* p, const Vec<float, 2>& o, Vec<float, 2>& old) {
+    float2 r = atomicAdd(reinterpret_cast<float2*>(p), make_float2(o.v[0], o.v[1]));
+    old.v[0] = r.x; old.v[1] = r.y;
+}
+
 template <typename T>
 __device__ __forceinline__ T* slab_ptr(void* base, const PushArgs& a, int t) {
     return reinterpret_cast<T*>(base) + (int64_t)t * a.tile_stride;
@@ -277,7 +294,25 @@ struct RoundSh {
     long long scan_tmp[kWarps];
 };
 
-enum : unsigned char { SF_FINAL = 1, SF_TRACK = 2, SF_NOPUSH = 4, SF_TGTSCALE = 8, SF_HK = 16 };
+enum : unsigned char { SF_FINAL = 1, SF_TRACK = 2, SF_NOPUSH = 4, SF_TGTSCALE = 8, SF_HK = 16, SF_CROSS = 32 };
+
+// Local GD for PPR and Katz only ever adds non-negative values to
+// non-negative residuals, so a node enters the next frontier exactly when one
+// of the round's additions takes it from below its threshold to at or above
+// it -- the reference's own enqueue test right after `rt[v] += val`
+// (ppr_solver.py:284-288).  Such tiles append on the crossing, never scan
+// densely, and PREP visits exactly the frontier.
+__device__ __forceinline__ bool tile_crosses(const TileParams& tp) {
+    return tp.method == M_LOCAL_GD && (tp.kind == KIND_PPR || tp.kind == KIND_KATZ);
+}
+
+// Does tile t's next round scan every node?  (identical in every block)
+__device__ __forceinline__ bool dense_next_round(const PushArgs& a, const TileParams& tp, const TileState& ts,
+                                                 int par) {
+    if (method_is_global(tp.method)) return true;
+    if (tile_crosses(tp) || !a.allow_dense) return false;
+    return ts.union_vol[par] * (double)a.dense_div > (double)a.g.n;
+}
 
 // Exclusive prefix over vals[0..m) (m <= 512) written to out[0..m]; block-wide.
 __device__ void block_exclusive_scan(const long long* vals, int m, long long* out, long long* tmp) {
@@ -636,6 +671,8 @@ struct ScatterCtx {
     int stamp;
     bool track;
     bool tgt_scale;
+    bool cross;
+    const ColState* cs;     // the tile's column states (thresholds for crossing)
 };
 
 template <typename T, int W>
@@ -657,7 +694,51 @@ __device__ __forceinline__ ScatterCtx<T, W> scatter_ctx(const PushArgs& a, int t
     c.stamp = a.ts[t].stamp + level + 1;
     c.track = (flags & SF_TRACK) != 0;
     c.tgt_scale = (flags & SF_TGTSCALE) != 0;
+    c.cross = (flags & SF_CROSS) != 0;
+    c.cs = a.cs + (int64_t)t * W;
     return c;
+}
+
+template <typename T, int VEC>
+__device__ __forceinline__ void push_edge(const DevGraph& g, T* tgt, int64_t ld, int c0, int v, const Vec<T, VEC>& p,
+                                          bool tgt_scale);
+
+template <typename T, int VEC>
+__device__ __forceinline__ void load_thetas(const ColState* cs, int c0, bool cross, double (&theta)[VEC]) {
+#pragma unroll
+    for (int k = 0; k < VEC; ++k) theta[k] = cross ? cs[c0 + k].theta : 0.0;
+}
+
+// One edge of a push for the L lanes of a group: add p into row v of the
+// target; then either append v on a threshold crossing (SF_CROSS) or append
+// every touched v (sparse tracking).  Every lane of the warp must call it.
+template <typename T, int W, int VEC, int L>
+__device__ __forceinline__ void edge_step(const PushArgs& a, const ScatterCtx<T, W>& c, bool ok, int v, int c0,
+                                          int lane_g, int grp_w, const Vec<T, VEC>& p, const double (&theta)[VEC]) {
+    bool cr = false;
+    if (ok) {
+        if (c.cross) {
+            Vec<T, VEC> old;
+            vatomic_ret<T, VEC>(c.tgt + (int64_t)v * a.ld + c0, p, old);
+            const double dv = a.g.degf_exact ? (double)a.g.degf[v] : a.g.degd[v];
+#pragma unroll
+            for (int k = 0; k < VEC; ++k) {
+                if (p.v[k] == T(0)) continue;
+                const T s = old.v[k] + p.v[k];  // the value the atomic stored
+                const double thr = theta[k] * dv;
+                cr |= ((double)old.v[k] < thr) && ((double)s >= thr);
+            }
+        } else {
+            push_edge<T, VEC>(a.g, c.tgt, a.ld, c0, v, p, c.tgt_scale);
+        }
+    }
+    if (c.cross) {
+        const unsigned b = __ballot_sync(kFull, cr);
+        const unsigned gm = ((L == 32) ? kFull : ((1u << L) - 1u)) << (grp_w * L);
+        append_once(ok && lane_g == 0 && (b & gm) != 0, v, c.mark, c.stamp, c.next, c.next_cnt, kFull);
+    } else if (c.track) {
+        append_once(ok && lane_g == 0, v, c.mark, c.stamp, c.next, c.next_cnt, kFull);
+    }
 }
 
 template <typename T, int VEC>
@@ -679,9 +760,11 @@ __device__ void scatter_large(const PushArgs& a, int t, const ScatterCtx<T, W>& 
     constexpr int VEC = (sizeof(T) == 4) ? (W >= 4 ? 4 : W) : (W >= 2 ? 2 : 1);
     constexpr int L = W / VEC;
     const DevGraph& g = a.g;
-    const int lane_g = threadIdx.x % L;
+    const int lane_g = threadIdx.x % L, grp_w = (threadIdx.x & 31) / L;
     const int c0 = lane_g * VEC;
     const int2* blarge = a.blarge + (int64_t)t * a.large_cap;
+    double theta[VEC];
+    load_thetas<T, VEC>(c.cs, c0, c.cross, theta);
     for (long long k = beg; k < end; ++k) {
         const int2 e = blarge[k];
         const int u = c.front[e.x];
@@ -696,8 +779,7 @@ __device__ void scatter_large(const PushArgs& a, int t, const ScatterCtx<T, W>& 
             const int j = j0 + gidx;
             const bool ok = j < en;
             const int v = ok ? g.col[rp + j] : 0;
-            if (ok) push_edge<T, VEC>(g, c.tgt, a.ld, c0, v, p, c.tgt_scale);
-            if (c.track) append_once(ok && lane_g == 0, v, c.mark, c.stamp, c.next, c.next_cnt, kFull);
+            edge_step<T, W, VEC, L>(a, c, ok, v, c0, lane_g, grp_w, p, theta);
         }
     }
 }
@@ -713,6 +795,8 @@ __device__ void scatter_med(const PushArgs& a, int t, const ScatterCtx<T, W>& c,
     const int lane_g = lane % L, grp_w = lane / L;
     const int c0 = lane_g * VEC;
     const int32_t* bmed = a.bmed + (int64_t)t * a.g.n;
+    double theta[VEC];
+    load_thetas<T, VEC>(c.cs, c0, c.cross, theta);
     for (long long k = beg + warp; k < end; k += kWarps) {
         const int f = bmed[k];
         const int u = c.front[f];
@@ -724,8 +808,7 @@ __device__ void scatter_med(const PushArgs& a, int t, const ScatterCtx<T, W>& c,
             const int j = j0 + grp_w;
             const bool ok = j < len;
             const int v = ok ? g.col[rp + j] : 0;
-            if (ok) push_edge<T, VEC>(g, c.tgt, a.ld, c0, v, p, c.tgt_scale);
-            if (c.track) append_once(ok && lane_g == 0, v, c.mark, c.stamp, c.next, c.next_cnt, kFull);
+            edge_step<T, W, VEC, L>(a, c, ok, v, c0, lane_g, grp_w, p, theta);
         }
     }
 }
@@ -741,6 +824,8 @@ __device__ void scatter_small(const PushArgs& a, int t, const ScatterCtx<T, W>& 
     const int lane_g = lane % L, grp_w = lane / L;
     const int c0 = lane_g * VEC;
     const int32_t* bsmall = a.bsmall + (int64_t)t * a.g.n;
+    double theta[VEC];
+    load_thetas<T, VEC>(c.cs, c0, c.cross, theta);
     for (long long kb = beg + (long long)warp * GPW; kb < end; kb += (long long)kWarps * GPW) {
         const long long k = kb + grp_w;
         const bool okr = k < end;
@@ -762,8 +847,7 @@ __device__ void scatter_small(const PushArgs& a, int t, const ScatterCtx<T, W>& 
         for (int j = 0; j < maxlen; ++j) {
             const bool ok = j < len;
             const int v = ok ? g.col[rp + j] : 0;
-            if (ok) push_edge<T, VEC>(g, c.tgt, a.ld, c0, v, p, c.tgt_scale);
-            if (c.track) append_once(ok && lane_g == 0, v, c.mark, c.stamp, c.next, c.next_cnt, kFull);
+            edge_step<T, W, VEC, L>(a, c, ok, v, c0, lane_g, grp_w, p, theta);
         }
     }
 }
@@ -909,16 +993,16 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
             const int par = lv & 1;
             const int m = tp.method;
             const bool hk = method_is_hk(m);
-            const bool global = method_is_global(m);
             const bool fin = hk && (m != M_HK_TAYLOR) && (lv + 1 == tp.n_levels);
             const bool last_taylor = (m == M_HK_TAYLOR) && (lv >= tp.n_levels);
-            const bool dnext = global || (a.allow_dense && ts.union_vol[par] * (double)a.dense_div > (double)n);
+            const bool dnext = dense_next_round(a, tp, ts, par);
             unsigned char f = 0;
             if (hk) f |= SF_HK;
             if (fin) f |= SF_FINAL;
             if (last_taylor) f |= SF_NOPUSH;
             if (tp.kind == KIND_IGN) f |= SF_TGTSCALE;
-            if (!dnext && !fin && !last_taylor && !(m == M_HK_TAYLOR && lv + 1 >= tp.n_levels + 1)) f |= SF_TRACK;
+            if (tile_crosses(tp)) f |= SF_CROSS;
+            else if (!dnext && !fin && !last_taylor) f |= SF_TRACK;
             rs.flags[k] = f;
             const bool has = ts.front_cnt[par] > 0 && !last_taylor;
             s_vals[k] = has ? ts.small_cnt[par] : 0;
@@ -969,9 +1053,7 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
             for (int k = 0; k < ntl; ++k) {
                 const int t = rs.tiles[k];
                 const int lv = rs.level[k];
-                const TileParams& tp = a.tp[t];
-                const bool dnext = method_is_global(tp.method) ||
-                                   (a.allow_dense && a.ts[t].union_vol[lv & 1] * (double)a.dense_div > (double)n);
+                const bool dnext = dense_next_round(a, a.tp[t], a.ts[t], lv & 1);
                 finish_round<W>(a, t, lv, dnext);
                 __syncthreads();
             }
