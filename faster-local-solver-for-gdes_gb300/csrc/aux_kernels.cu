@@ -1,6 +1,8 @@
 // aux_kernels.cu -- column initialisation, result extraction, graph edits.
 #include <cuda_runtime.h>
 
+#include <algorithm>
+
 #include "gde_common.cuh"
 #include "gde_device.cuh"
 #include "gde_engine.h"
@@ -58,8 +60,10 @@ __global__ void extract_kernel(PushArgs a, const ExtractCol* cols, O* x_out, O* 
     T* R = reinterpret_cast<T*>(a.R) + base;
     T* R2 = a.R2 ? reinterpret_cast<T*>(a.R2) + base : nullptr;
     const int rl = ec.r_levels;
+    const int32_t* perm = a.g.perm;
+    // u runs over caller ids; the slabs are in internal (relabelled) order
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t o = u * a.ld;
+        const int64_t o = (perm ? (int64_t)perm[u] : u) * a.ld;
         if (x_out) {
             double x = (double)X[o];
             if (u == ec.seed) x = x + ec.seed_add;
@@ -75,6 +79,18 @@ __global__ void extract_kernel(PushArgs a, const ExtractCol* cols, O* x_out, O* 
             R[o] = T(0);
             if (R2) R2[o] = T(0);
         }
+    }
+}
+
+// dst row u (caller order) <- src row perm[u] (internal order), or the reverse
+template <typename T>
+__global__ void permute_rows_kernel(const T* src, int64_t sld, T* dst, int64_t dld, const int32_t* perm, int64_t n,
+                                    int64_t F, int to_internal) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * F; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = i / F, c = i % F;
+        const int64_t p = perm[u];
+        if (to_internal) dst[p * dld + c] = src[u * sld + c];
+        else dst[u * dld + c] = src[p * sld + c];
     }
 }
 
@@ -106,6 +122,20 @@ cudaError_t extract_columns(const PushArgs& a, int prec64, int W, const ExtractC
         if (out64) extract_kernel<float, double><<<grid, 256, 0, st>>>(a, d_cols, (double*)x_out, (double*)r_out, ld_out, n, clear);
         else extract_kernel<float, float><<<grid, 256, 0, st>>>(a, d_cols, (float*)x_out, (float*)r_out, ld_out, n, clear);
     }
+    return cudaGetLastError();
+}
+
+cudaError_t permute_rows(const void* src, int64_t sld, void* dst, int64_t dld, const int32_t* perm, int64_t n,
+                         int64_t F, int elem, int to_internal, cudaStream_t st) {
+    if (n == 0 || F == 0) return cudaSuccess;
+    int64_t total = n * F;
+    int blocks = (int)std::min<int64_t>((total + 255) / 256, 8192);
+    if (elem == 8)
+        permute_rows_kernel<double><<<blocks, 256, 0, st>>>((const double*)src, sld, (double*)dst, dld, perm, n, F,
+                                                             to_internal);
+    else
+        permute_rows_kernel<float><<<blocks, 256, 0, st>>>((const float*)src, sld, (float*)dst, dld, perm, n, F,
+                                                            to_internal);
     return cudaGetLastError();
 }
 

@@ -67,6 +67,14 @@ struct gde_graph {
     std::vector<int64_t> h_len;
     std::vector<double> h_deg;
     bool deg_is_len = true;
+    // Static graphs are stored relabelled by descending degree: push targets
+    // are hit in proportion to their degree, so the hot part of every
+    // residual vector is a short prefix that stays in L2.  h_perm maps a
+    // caller id to the internal id; every API id stays the caller's.
+    bool relabeled = false;
+    std::vector<int32_t> h_perm;
+    int32_t* perm_d = nullptr;
+    int32_t node_in(int64_t u) const { return relabeled ? h_perm[u] : (int32_t)u; }
 };
 
 namespace {
@@ -421,19 +429,58 @@ int gde_graph_upload(gde_ctx* ctx, int64_t n, int64_t cap, const int64_t* indptr
     CK(cudaSetDevice(ctx->device));
     gde_graph* G = new gde_graph();
     G->ctx = ctx;
-    G->h_indptr.assign(indptr, indptr + n + 1);
-    G->h_len.resize(n);
-    G->h_deg.resize(n);
+    std::vector<int64_t> len0(n);
+    std::vector<double> deg0(n);
     for (int64_t u = 0; u < n; u++) {
         int64_t len = row_len ? row_len[u] : indptr[u + 1] - indptr[u];
-        if (len < 0 || indptr[u] + len > cap || (u + 1 <= n && indptr[u] + len > indptr[u + 1])) {
+        if (len < 0 || indptr[u] + len > cap || indptr[u] + len > indptr[u + 1]) {
             delete G;
             return fail(ctx, GDE_EINVAL, "row " + std::to_string(u) + " exceeds its CSR extent");
         }
-        G->h_len[u] = len;
-        G->h_deg[u] = degree ? degree[u] : (double)len;
+        len0[u] = len;
+        deg0[u] = degree ? degree[u] : (double)len;
         if (degree && degree[u] != (double)len) G->deg_is_len = false;
     }
+    for (int64_t j = 0; j < cap; j++)
+        if (indices[j] < 0 || indices[j] >= n) {
+            // slack slots of a padded CSR may hold the sentinel n
+            if (row_len && indices[j] == n) continue;
+            delete G;
+            return fail(ctx, GDE_EINVAL, "column index out of range at position " + std::to_string(j));
+        }
+    std::vector<int32_t> col_new;
+    const int32_t* col_src = indices;
+    int64_t cap_new = cap;
+    if (!row_len) {
+        // static CSR: relabel by descending degree (stable), rows sorted
+        G->relabeled = true;
+        std::vector<int32_t> iperm(n);
+        for (int64_t u = 0; u < n; u++) iperm[u] = (int32_t)u;
+        std::stable_sort(iperm.begin(), iperm.end(), [&](int32_t a, int32_t b) { return len0[a] > len0[b]; });
+        G->h_perm.resize(n);
+        for (int64_t k = 0; k < n; k++) G->h_perm[iperm[k]] = (int32_t)k;
+        G->h_indptr.assign(n + 1, 0);
+        G->h_len.resize(n);
+        G->h_deg.resize(n);
+        for (int64_t k = 0; k < n; k++) {
+            G->h_len[k] = len0[iperm[k]];
+            G->h_deg[k] = deg0[iperm[k]];
+            G->h_indptr[k + 1] = G->h_indptr[k] + G->h_len[k];
+        }
+        cap_new = G->h_indptr[n];
+        col_new.resize(std::max<int64_t>(cap_new, 1));
+        for (int64_t k = 0; k < n; k++) {
+            const int64_t src = indptr[iperm[k]], dst = G->h_indptr[k];
+            for (int64_t j = 0; j < G->h_len[k]; j++) col_new[dst + j] = G->h_perm[indices[src + j]];
+            std::sort(col_new.begin() + dst, col_new.begin() + dst + G->h_len[k]);
+        }
+        col_src = col_new.data();
+    } else {
+        G->h_indptr.assign(indptr, indptr + n + 1);
+        G->h_len = len0;
+        G->h_deg = deg0;
+    }
+    cap = cap_new;
     G->g.n = n;
     G->g.cap = cap;
     // row_ptr gets two spare entries so aligned 16-byte windows stay in bounds
@@ -448,8 +495,14 @@ int gde_graph_upload(gde_ctx* ctx, int64_t n, int64_t cap, const int64_t* indptr
         return fail(ctx, GDE_ENOMEM, "device memory exhausted (graph)");
     }
     CK(cudaMemsetAsync(G->row_ptr, 0, (n + 3) * sizeof(int64_t), ctx->stream));
-    CK(cudaMemcpyAsync(G->row_ptr, indptr, (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, ctx->stream));
-    if (cap > 0) CK(cudaMemcpyAsync(G->col, indices, cap * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(G->row_ptr, G->h_indptr.data(), (n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice,
+                       ctx->stream));
+    if (cap > 0) CK(cudaMemcpyAsync(G->col, col_src, cap * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    if (G->relabeled) {
+        CK(cudaMalloc(&G->perm_d, n * sizeof(int32_t)));
+        CK(cudaMemcpyAsync(G->perm_d, G->h_perm.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+    }
+    G->g.perm = G->perm_d;
     G->g.row_ptr = G->row_ptr;
     G->g.col = G->col;
     G->g.row_len = G->row_len;
@@ -466,7 +519,7 @@ int gde_graph_free(gde_graph* G) {
     cudaSetDevice(G->ctx->device);
     cudaStreamSynchronize(G->ctx->stream);
     cudaFree(G->row_ptr); cudaFree(G->col); cudaFree(G->row_len); cudaFree(G->degf); cudaFree(G->degd);
-    cudaFree(G->nfac); cudaFree(G->tfac); cudaFree(G->tfac_f);
+    cudaFree(G->nfac); cudaFree(G->tfac); cudaFree(G->tfac_f); cudaFree(G->perm_d);
     delete G;
     return GDE_OK;
 }
@@ -495,7 +548,7 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
     for (int64_t q = 0; q < nq; q++) {
         if (seeds[q] < 0 || seeds[q] >= n) return fail(ctx, GDE_EINVAL, "seed out of range");
         if (!(eps[q] > 0.0)) return fail(ctx, GDE_EINVAL, "eps must be > 0");
-        if (kind == KIND_PPR && (method == M_LOCAL_GD || method == M_GLOBAL_GD) && !(eps[q] * G->h_deg[seeds[q]] <= 1.))
+        if (kind == KIND_PPR && (method == M_LOCAL_GD || method == M_GLOBAL_GD) && !(eps[q] * G->h_deg[G->node_in(seeds[q])] <= 1.))
             return fail(ctx, GDE_EINVAL, "eps * degree[s_node] > 1 (ppr_solver.py:213)");
     }
     if (hk && !(p->tau >= 1.0)) return fail(ctx, GDE_EINVAL, "tau must be >= 1 (hk_solver.py:35)");
@@ -620,15 +673,15 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
                 if (c >= P.ncols) continue;
                 int64_t q = td.qs[c];
                 C.live = 1;
-                C.seed = seeds[q];
+                C.seed = G->node_in(seeds[q]);
                 if (kind == KIND_PPR) C.theta = eps[q] * p->alpha;      // eps * alpha * degree
                 else if (kind == KIND_KATZ) C.theta = eps[q];            // eps * degree
                 else C.theta = std::exp(p->tau) * eps[q];                // np.exp(tau) * eps * degree / est_n
                 InitCol I{};
                 I.tile = t;
                 I.col = c;
-                I.seed = seeds[q];
-                const double ds = G->h_deg[seeds[q]];
+                I.seed = G->node_in(seeds[q]);
+                const double ds = G->h_deg[I.seed];
                 if (method_is_cheby(method)) {
                     if (kind == KIND_KATZ) {
                         I.x0 = 2. / (p->l_max + p->mu_min);
@@ -869,7 +922,27 @@ int gde_feature_push(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t F,
     if (cand)
         for (int64_t i = 0; i < ncand; i++)
             if (cand[i] < 0 || cand[i] >= G->g.n) return fail(ctx, GDE_EINVAL, "candidate out of range");
-    return feature_push_impl(ctx, G, p, F, Pm, Rm, ld, eps, cand, ncand, false, oper_out, stats);
+    if (!G->relabeled) return feature_push_impl(ctx, G, p, F, Pm, Rm, ld, eps, cand, ncand, false, oper_out, stats);
+    // relabelled static graph: run on internal-order copies of P and R
+    const int64_t n = G->g.n;
+    const int es = (p->prec == GDE_FP64) ? 8 : 4;
+    void* Pi = wsget(ctx, "perm_P", (size_t)n * F * es);
+    void* Ri = wsget(ctx, "perm_R", (size_t)n * F * es);
+    if (!Pi || !Ri) return fail(ctx, GDE_ENOMEM, "permuted feature matrices");
+    CK(permute_rows(Pm, ld, Pi, F, G->perm_d, n, F, es, 1, ctx->stream));
+    CK(permute_rows(Rm, ld, Ri, F, G->perm_d, n, F, es, 1, ctx->stream));
+    std::vector<int32_t> ci;
+    if (cand) {
+        ci.resize(ncand);
+        for (int64_t i = 0; i < ncand; i++) ci[i] = G->h_perm[cand[i]];
+    }
+    int rc = feature_push_impl(ctx, G, p, F, Pi, Ri, F, eps, cand ? ci.data() : nullptr, ncand, false, oper_out, stats);
+    if (rc != GDE_OK) return rc;
+    // back to caller order: dst[u] = src[perm[u]]
+    CK(permute_rows(Pi, F, Pm, ld, G->perm_d, n, F, es, 0, ctx->stream));
+    CK(permute_rows(Ri, F, Rm, ld, G->perm_d, n, F, es, 0, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    return GDE_OK;
 }
 
 int gde_plain_ppr_local(gde_ctx* ctx, gde_graph* G, int32_t seed, double alpha, double eps, float* x_out,
@@ -900,10 +973,15 @@ int gde_plain_ppr_local(gde_ctx* ctx, gde_graph* G, int32_t seed, double alpha, 
     ctx->plain.degf = G->degf;
     double oper = 0;
     int rounds = 0;
-    int rc = plain_ppr_local(G->g, ctx->plain, seed, alpha, eps, &oper, &rounds, ctx->stream);
+    int rc = plain_ppr_local(G->g, ctx->plain, G->node_in(seed), alpha, eps, &oper, &rounds, ctx->stream);
     if (rc != GDE_OK) return fail(ctx, rc, "plain baseline failed");
-    if (x_out) CK(cudaMemcpyAsync(x_out, ctx->plain.xt, n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
-    if (r_out) CK(cudaMemcpyAsync(r_out, ctx->plain.rt, n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    if (G->relabeled) {
+        if (x_out) CK(permute_rows(ctx->plain.xt, 1, x_out, 1, G->perm_d, n, 1, 4, 0, ctx->stream));
+        if (r_out) CK(permute_rows(ctx->plain.rt, 1, r_out, 1, G->perm_d, n, 1, 4, 0, ctx->stream));
+    } else {
+        if (x_out) CK(cudaMemcpyAsync(x_out, ctx->plain.xt, n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+        if (r_out) CK(cudaMemcpyAsync(r_out, ctx->plain.rt, n * 4, cudaMemcpyDeviceToDevice, ctx->stream));
+    }
     CK(cudaStreamSynchronize(ctx->stream));
     if (oper_out) *oper_out = oper;
     if (rounds_out) *rounds_out = rounds;
@@ -953,3 +1031,4 @@ int gde_internal_fail(gde_ctx* ctx, int code, const char* msg) { return fail(ctx
 cudaStream_t gde_internal_stream(gde_ctx* ctx) { return ctx->stream; }
 const double* gde_internal_npush(gde_graph* G) { return G->nfac; }
 const double* gde_internal_degd(gde_graph* G) { return G->degd; }
+bool gde_internal_relabeled(gde_graph* G) { return G->relabeled; }

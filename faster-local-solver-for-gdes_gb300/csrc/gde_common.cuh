@@ -58,6 +58,7 @@ struct DevGraph {
     const float* tfac_f;      // [n] same, FP32
     double vol;               // sum of degrees (m)
     int degf_exact;           // 1 when every degree is an integer < 2^24 (degf == degd exactly)
+    const int32_t* perm;      // caller id -> internal id (nullptr: identity)
 };
 
 // ---------------------------------------------------------------------------

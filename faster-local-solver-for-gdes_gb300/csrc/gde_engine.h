@@ -43,6 +43,11 @@ struct PlainWork {
 int plain_ppr_local(const DevGraph& g, PlainWork& w, int seed, double alpha, double eps, double* oper,
                     int* rounds, cudaStream_t st);
 
+// Row permutation between caller and internal node order (aux_kernels.cu):
+// to_internal: dst[perm[u]] = src[u]; else dst[u] = src[perm[u]] (row strides sld, dld).
+cudaError_t permute_rows(const void* src, int64_t sld, void* dst, int64_t dld, const int32_t* perm, int64_t n,
+                         int64_t F, int elem, int to_internal, cudaStream_t st);
+
 // Graph helpers (aux_kernels.cu).
 cudaError_t graph_apply_entries(int32_t* col, const int64_t* pos, const int32_t* val, int64_t k, cudaStream_t st);
 

@@ -36,6 +36,7 @@ int gde_internal_fail(gde_ctx* ctx, int code, const char* msg);
 cudaStream_t gde_internal_stream(gde_ctx* ctx);
 const double* gde_internal_npush(gde_graph* G);
 const double* gde_internal_degd(gde_graph* G);
+bool gde_internal_relabeled(gde_graph* G);
 
 namespace {
 
@@ -141,6 +142,8 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
     const int kind = p->kind;
     if (kind != KIND_IGN && kind != KIND_UPPR) return gde_internal_fail(ctx, GDE_EINVAL, "kind must be IGN or UPPR");
     if (kind == KIND_IGN && !Xm) return gde_internal_fail(ctx, GDE_EINVAL, "InstantGNN repair needs X");
+    if (gde_internal_relabeled(G))
+        return gde_internal_fail(ctx, GDE_EINVAL, "edge updates need a padded CSR graph (upload with row_len)");
     const int64_t* indptr;
     const int64_t* hlen;
     int64_t n;
