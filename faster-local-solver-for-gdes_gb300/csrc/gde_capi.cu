@@ -41,7 +41,6 @@ struct gde_ctx {
     GridBarrier* bar = nullptr;
     int* derr = nullptr;
     LaunchStats* dstats = nullptr;
-    unsigned long long* dwork = nullptr;  // [2][4] dynamic-scheduling counters
     LaunchStats* hstats = nullptr;  // pinned
     TileState* hts = nullptr;       // pinned scratch
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
@@ -212,7 +211,6 @@ int alloc_tiles(gde_ctx* ctx, gde_graph* G, int ntiles, int W, int prec64, bool 
     a.stats = ctx->dstats;
     a.bar = ctx->bar;
     a.err = ctx->derr;
-    a.work = ctx->dwork;
     return GDE_OK;
 }
 
@@ -232,7 +230,6 @@ int run_engine(gde_ctx* ctx, PushArgs& a, int prec64, int W, gde_stats* st, doub
     CK(cudaMemsetAsync(ctx->bar, 0, sizeof(GridBarrier), ctx->stream));
     CK(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->stream));
     CK(cudaMemsetAsync(ctx->dstats, 0, sizeof(LaunchStats), ctx->stream));
-    CK(cudaMemsetAsync(ctx->dwork, 0, 8 * sizeof(unsigned long long), ctx->stream));
     a.round_budget = a.max_rounds + 1;
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
     cudaError_t e = engine_launch(a, prec64, W, grid, ctx->stream);
@@ -378,7 +375,6 @@ int gde_ctx_create(int device, gde_ctx** out) {
         cudaMalloc(&ctx->bar, sizeof(GridBarrier)) != cudaSuccess ||
         cudaMalloc(&ctx->derr, sizeof(int)) != cudaSuccess ||
         cudaMalloc(&ctx->dstats, sizeof(LaunchStats)) != cudaSuccess ||
-        cudaMalloc(&ctx->dwork, 8 * sizeof(unsigned long long)) != cudaSuccess ||
         cudaMallocHost(&ctx->hstats, sizeof(LaunchStats)) != cudaSuccess ||
         cudaMallocHost(&ctx->hts, sizeof(TileState) * 4096) != cudaSuccess) {
         delete ctx;
@@ -402,7 +398,6 @@ int gde_ctx_destroy(gde_ctx* ctx) {
     cudaFree(ctx->bar);
     cudaFree(ctx->derr);
     cudaFree(ctx->dstats);
-    cudaFree(ctx->dwork);
     cudaFreeHost(ctx->hstats);
     cudaFreeHost(ctx->hts);
     for (auto& ev : ctx->ev) cudaEventDestroy(ev);

@@ -165,7 +165,6 @@ struct PushArgs {
     int round_budget;          // rounds to advance in this launch (serving ticks)
     int kahan;                 // compensated FP32 solution
     int allow_dense;           // 0: every round visits only touched nodes (dynamic updates)
-    unsigned long long* work;  // [2][4] work-distribution counters (by round parity), zeroed per launch
 };
 
 }  // namespace gde

@@ -292,7 +292,6 @@ struct RoundSh {
     int level[kMaxLaunchTiles];                 // per live tile: rounds since its start
     unsigned char flags[kMaxLaunchTiles];       // per live tile scatter flags (SF_*)
     long long scan_tmp[kWarps];
-    long long grab;                             // block_grab broadcast slot
 };
 
 enum : unsigned char { SF_FINAL = 1, SF_TRACK = 2, SF_NOPUSH = 4, SF_TGTSCALE = 8, SF_HK = 16, SF_CROSS = 32 };
@@ -354,22 +353,6 @@ __device__ __forceinline__ int find_tile(const long long* off, int ntl, long lon
         else lo = mid + 1;
     }
     return lo;
-}
-
-// Dynamic scheduling: the block takes the next `grain` items [lo, hi) of a
-// flattened space from a global counter; false when the space is exhausted.
-constexpr long long kPrepChunk = 1024;
-constexpr long long kMedChunk = 4;
-constexpr long long kSmallChunk = 512;
-
-__device__ __forceinline__ bool block_grab(unsigned long long* counter, long long grain, long long total,
-                                           long long& lo, long long& hi, long long* s_slot) {
-    __syncthreads();
-    if (threadIdx.x == 0) *s_slot = (total > 0) ? (long long)atomicAdd(counter, (unsigned long long)grain) : total;
-    __syncthreads();
-    lo = *s_slot;
-    hi = min(lo + grain, total);
-    return lo < total;
 }
 
 // This block's share [lo, hi) of a flattened space of `total` items.
@@ -982,10 +965,10 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
         }
         __syncthreads();
         block_exclusive_scan(s_vals, ntl, rs.off[0], rs.scan_tmp);
-        if (blockIdx.x == 0 && threadIdx.x < 4) a.work[(((it + 1) & 1) << 2) + threadIdx.x] = 0ull;
         {
             long long lo, hi;
-            while (block_grab(&a.work[((it & 1) << 2) + 0], kPrepChunk, rs.off[0][ntl], lo, hi, &rs.grab)) {
+            block_share(rs.off[0][ntl], lo, hi);
+            if (lo < hi) {
                 for (int k = find_tile(rs.off[0], ntl, lo); k < ntl && rs.off[0][k] < hi; ++k) {
                     const long long b = max(lo, rs.off[0][k]) - rs.off[0][k];
                     const long long e = min(hi, rs.off[0][k + 1]) - rs.off[0][k];
@@ -1040,23 +1023,21 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
         }
         __syncthreads();
         block_exclusive_scan(s_vals, ntl, rs.off[2], rs.scan_tmp);
-        // Blocks take chunks dynamically: long-row chunks first (the largest
-        // pieces), then medium rows, then short rows fill in the tail.
+        // long-row chunks first (largest pieces), then medium, then short rows
         for (int sp = 2; sp >= 0; --sp) {
             const long long* off = rs.off[sp];
-            const long long grain = (sp == 2) ? 1 : (sp == 1 ? kMedChunk : kSmallChunk);
             long long lo, hi;
-            while (block_grab(&a.work[((it & 1) << 2) + 1 + sp], grain, off[ntl], lo, hi, &rs.grab)) {
-                for (int k = find_tile(off, ntl, lo); k < ntl && off[k] < hi; ++k) {
-                    const long long b = max(lo, off[k]) - off[k];
-                    const long long e = min(hi, off[k + 1]) - off[k];
-                    if (b >= e) continue;
-                    const int t = rs.tiles[k];
-                    const ScatterCtx<T, W> c = scatter_ctx<T, W>(a, t, rs.level[k], rs.flags[k]);
-                    if (sp == 2) scatter_large<T, W>(a, t, c, b, e);
-                    else if (sp == 1) scatter_med<T, W>(a, t, c, b, e);
-                    else scatter_small<T, W>(a, t, c, b, e);
-                }
+            block_share(off[ntl], lo, hi);
+            if (lo >= hi) continue;
+            for (int k = find_tile(off, ntl, lo); k < ntl && off[k] < hi; ++k) {
+                const long long b = max(lo, off[k]) - off[k];
+                const long long e = min(hi, off[k + 1]) - off[k];
+                if (b >= e) continue;
+                const int t = rs.tiles[k];
+                const ScatterCtx<T, W> c = scatter_ctx<T, W>(a, t, rs.level[k], rs.flags[k]);
+                if (sp == 2) scatter_large<T, W>(a, t, c, b, e);
+                else if (sp == 1) scatter_med<T, W>(a, t, c, b, e);
+                else scatter_small<T, W>(a, t, c, b, e);
             }
         }
         // HK level drop (touches the current level's slab only)
