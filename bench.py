@@ -51,7 +51,8 @@ def parse():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--batch", type=int, default=512, help="queries per step")
-    ap.add_argument("--tile-w", type=int, default=8)
+    ap.add_argument("--tile-w", type=int, default=1, help="1 = served slots (continuous batching)")
+    ap.add_argument("--slots", type=int, default=32, help="concurrent queries of the served engine")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--plain-queries", type=int, default=4)
     ap.add_argument("--cpu-queries", type=int, default=0, help="CPU-baseline sample (0 = 2 per host thread)")
@@ -204,7 +205,7 @@ def run_ours(args):
     from gde import _lib as L
     from gde import api, graphs
 
-    tuning = {}
+    tuning = {"slots": args.slots}
     for kv in filter(None, args.tuning.split(",")):
         k, v = kv.split("=")
         tuning[k] = int(v)

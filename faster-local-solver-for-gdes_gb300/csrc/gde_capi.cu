@@ -230,7 +230,7 @@ int run_engine(gde_ctx* ctx, PushArgs& a, int prec64, int W, gde_stats* st, doub
     CK(cudaMemsetAsync(ctx->bar, 0, sizeof(GridBarrier), ctx->stream));
     CK(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->stream));
     CK(cudaMemsetAsync(ctx->dstats, 0, sizeof(LaunchStats), ctx->stream));
-    a.round_budget = a.max_rounds + 1;
+    if (!a.serve) a.round_budget = a.max_rounds + 1;
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
     cudaError_t e = engine_launch(a, prec64, W, grid, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "cooperative launch of the push kernel");
@@ -337,6 +337,183 @@ int upload_degrees(gde_ctx* ctx, gde_graph* G) {
     return GDE_OK;
 }
 
+// Served solve of PPR / Katz local GD: `slots` single-column tiles cycle
+// through a device queue of the nq queries inside one persistent launch.  A
+// finished query's solution row is written (caller node order) and its slot
+// cleared by the kernel itself, and the next query admitted -- continuous
+// batching, so only `slots` residual vectors are ever live and they stay
+// L2-resident.  arrival_ms (may be null): query q is not admitted before
+// arrival_ms[q] after the launch starts; latency is then measured from it.
+int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const int32_t* seeds,
+                 const double* eps, const double* arrival_ms, void* x_out, void* r_out, int out64, int out_mem,
+                 int64_t ld_out, double* oper_out, int32_t* rounds_out, float* lat_ms_out, gde_stats* stats) {
+    const int64_t n = G->g.n;
+    const int kind = p->kind;
+    const int prec64 = (p->prec == GDE_FP64);
+    if (nq >= (int64_t)1 << 31) return fail(ctx, GDE_EINVAL, "too many queries");
+    int S = p->slots > 0 ? p->slots : 32;
+    S = (int)std::min<int64_t>(std::min<int64_t>(S, nq), 512);
+    PushArgs base{};
+    fill_tuning(p, base);
+    TileWs tw;
+    tw.a = base;
+    int rc = alloc_tiles(ctx, G, S, 1, prec64, false, false, true, !prec64, tw);
+    if (rc != GDE_OK) return rc;
+    PushArgs& a = tw.a;
+    a.small_max = base.small_max; a.med_max = base.med_max; a.chunk = base.chunk;
+    a.dense_div = base.dense_div; a.max_rounds = base.max_rounds; a.allow_dense = base.allow_dense;
+    rc = alloc_large(ctx, G, S, tw);
+    if (rc != GDE_OK) return rc;
+    const size_t es = prec64 ? 8 : 4;
+    const size_t slab = (size_t)S * n * es;
+    CK(cudaEventRecord(ctx->ev[2], ctx->stream));
+    CK(cudaMemsetAsync(a.R, 0, slab, ctx->stream));
+    CK(cudaMemsetAsync(a.X, 0, slab, ctx->stream));
+    if (a.XC) CK(cudaMemsetAsync(a.XC, 0, (size_t)S * n * 4, ctx->stream));
+    // ---- the query queue on the device ----
+    std::vector<int32_t> qs(nq), qsc(nq);
+    std::vector<double> qt(nq), qr0(nq);
+    std::vector<long long> qarr(arrival_ms ? nq : 0);
+    for (int64_t q = 0; q < nq; q++) {
+        qsc[q] = seeds[q];
+        qs[q] = G->node_in(seeds[q]);
+        qt[q] = (kind == KIND_PPR) ? eps[q] * p->alpha : eps[q];  // eps*alpha*degree / eps*degree
+        qr0[q] = (kind == KIND_PPR) ? p->alpha : 1.0;
+        if (arrival_ms) qarr[q] = (long long)(arrival_ms[q] * 1e6);
+    }
+    auto dev = [&](const char* name, size_t bytes) { return wsget(ctx, name, std::max<size_t>(bytes, 8)); };
+    int32_t* d_seed = (int32_t*)dev("q_seed", nq * 4);
+    int32_t* d_sc = (int32_t*)dev("q_seed_caller", nq * 4);
+    double* d_theta = (double*)dev("q_theta", nq * 8);
+    double* d_r0 = (double*)dev("q_r0", nq * 8);
+    long long* d_arr = arrival_ms ? (long long*)dev("q_arrival", nq * 8) : nullptr;
+    double* d_oper = (double*)dev("q_oper", nq * 8);
+    int* d_rounds = (int*)dev("q_rounds", nq * 4);
+    unsigned long long* d_start = (unsigned long long*)dev("q_start", nq * 8);
+    unsigned long long* d_finish = (unsigned long long*)dev("q_finish", nq * 8);
+    int* d_next = (int*)dev("q_next", 4);
+    if (!d_seed || !d_sc || !d_theta || !d_r0 || (arrival_ms && !d_arr) || !d_oper || !d_rounds || !d_start ||
+        !d_finish || !d_next)
+        return fail(ctx, GDE_ENOMEM, "query queue");
+    CK(cudaMemcpyAsync(d_seed, qs.data(), nq * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(d_sc, qsc.data(), nq * 4, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(d_theta, qt.data(), nq * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(d_r0, qr0.data(), nq * 8, cudaMemcpyHostToDevice, ctx->stream));
+    if (d_arr) CK(cudaMemcpyAsync(d_arr, qarr.data(), nq * 8, cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemsetAsync(d_start, 0, nq * 8, ctx->stream));
+    CK(cudaMemsetAsync(d_finish, 0, nq * 8, ctx->stream));
+    const int first = S;
+    CK(cudaMemcpyAsync(d_next, &first, 4, cudaMemcpyHostToDevice, ctx->stream));
+    // ---- outputs: the caller's device rows, or staging rows copied back ----
+    const size_t oes = out64 ? 8 : 4;
+    void* dx = nullptr;
+    void* dr = nullptr;
+    if (x_out) dx = (out_mem == GDE_MEM_DEVICE) ? x_out : dev("serve_x", (size_t)nq * ld_out * oes);
+    if (r_out) dr = (out_mem == GDE_MEM_DEVICE) ? r_out : dev("serve_r", (size_t)nq * ld_out * oes);
+    if ((x_out && !dx) || (r_out && !dr)) return fail(ctx, GDE_ENOMEM, "output staging");
+    // ---- the first S queries start in the slots ----
+    std::vector<TileParams> tp(S);
+    std::vector<TileState> ts(S);
+    std::vector<ColState> cs(S);
+    std::vector<InitCol> ic(S);
+    for (int t = 0; t < S; t++) {
+        TileParams& P = tp[t];
+        memset(&P, 0, sizeof(P));
+        P.kind = kind;
+        P.method = M_LOCAL_GD;
+        P.ncols = 1;
+        P.alpha = p->alpha;
+        P.x_gain = 1.0;
+        TileState& T = ts[t];
+        memset(&T, 0, sizeof(T));
+        T.t0 = 0;
+        T.done = SLOT_LIVE;
+        T.stamp = ctx->stamp[t];
+        T.qid = t;
+        ColState& C = cs[t];
+        memset(&C, 0, sizeof(C));
+        C.live = 1;
+        C.seed = qs[t];
+        C.theta = qt[t];
+        InitCol I{};
+        I.tile = t;
+        I.col = 0;
+        I.seed = qs[t];
+        I.r0 = qr0[t];
+        ic[t] = I;
+    }
+    CK(cudaMemcpyAsync(a.tp, tp.data(), S * sizeof(TileParams), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(a.ts, ts.data(), S * sizeof(TileState), cudaMemcpyHostToDevice, ctx->stream));
+    CK(cudaMemcpyAsync(a.cs, cs.data(), S * sizeof(ColState), cudaMemcpyHostToDevice, ctx->stream));
+    InitCol* d_ic = (InitCol*)dev("initcols", S * sizeof(InitCol));
+    if (!d_ic) return fail(ctx, GDE_ENOMEM, "column tables");
+    CK(cudaMemcpyAsync(d_ic, ic.data(), S * sizeof(InitCol), cudaMemcpyHostToDevice, ctx->stream));
+    CK(init_columns(a, prec64, 1, d_ic, S, ctx->stream));
+    a.serve = 1;
+    a.round_budget = 0x3fffffff;
+    ServeQueue& Q = a.queue;
+    Q.nq = (int)nq;
+    Q.next = d_next;
+    Q.seed = d_seed;
+    Q.theta = d_theta;
+    Q.r0 = d_r0;
+    Q.arrival_ns = d_arr;
+    Q.x_out = dx;
+    Q.r_out = dr;
+    Q.ld_out = ld_out;
+    Q.out64 = out64;
+    Q.seed_caller = d_sc;
+    Q.seed_add = (kind == KIND_KATZ) ? -1.0 : 0.0;  // xt[s_node] -= 1. (katz_solver.py:243)
+    Q.oper = d_oper;
+    Q.rounds = d_rounds;
+    Q.start_ns = d_start;
+    Q.finish_ns = d_finish;
+    double kernel_ms = 0.0;
+    rc = run_engine(ctx, a, prec64, 1, stats, &kernel_ms);
+    if (rc != GDE_OK) return rc;
+    // ---- results ----
+    if (out_mem != GDE_MEM_DEVICE) {
+        if (x_out) CK(cudaMemcpyAsync(x_out, dx, (size_t)nq * ld_out * oes, cudaMemcpyDeviceToHost, ctx->stream));
+        if (r_out) CK(cudaMemcpyAsync(r_out, dr, (size_t)nq * ld_out * oes, cudaMemcpyDeviceToHost, ctx->stream));
+    }
+    std::vector<double> hop(nq);
+    std::vector<int> hro(nq);
+    std::vector<unsigned long long> hst(nq), hfi(nq);
+    CK(cudaMemcpyAsync(hop.data(), d_oper, nq * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(hro.data(), d_rounds, nq * 4, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(hst.data(), d_start, nq * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(hfi.data(), d_finish, nq * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaMemcpyAsync(ctx->hts, a.ts, S * sizeof(TileState), cudaMemcpyDeviceToHost, ctx->stream));
+    CK(cudaEventRecord(ctx->ev[3], ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));
+    const unsigned long long k0 = ctx->hstats->start_ns;
+    bool capped = false;
+    for (int t = 0; t < S; t++) {
+        const TileState& T = ctx->hts[t];
+        ctx->stamp[t] = T.stamp + (int)std::max<long long>(0, (long long)ctx->hstats->iters - T.t0) + 4;
+        if (T.done == SLOT_LIVE) capped = true;
+    }
+    for (int64_t q = 0; q < nq; q++) {
+        if (oper_out) oper_out[q] = hop[q];
+        if (rounds_out) rounds_out[q] = hro[q];
+        if (lat_ms_out) {
+            // from arrival (served) or admission (first slots: the launch start)
+            unsigned long long from = arrival_ms ? k0 + (unsigned long long)qarr[q] : (hst[q] ? hst[q] : k0);
+            lat_ms_out[q] = hfi[q] > from ? (float)((double)(hfi[q] - from) * 1e-6) : 0.f;
+        }
+    }
+    if (stats) {
+        float tot = 0.f;
+        cudaEventElapsedTime(&tot, ctx->ev[2], ctx->ev[3]);
+        stats->total_ms = tot;
+        stats->kernel_ms = kernel_ms;
+        stats->tiles = S;
+        stats->tile_w = 1;
+    }
+    if (capped) return fail(ctx, GDE_EITERCAP, "max_rounds reached before the stopping rule held");
+    return GDE_OK;
+}
+
 }  // namespace
 
 // ===========================================================================
@@ -409,6 +586,28 @@ int gde_ctx_destroy(gde_ctx* ctx) {
 const char* gde_last_error(gde_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 
 void* gde_ctx_stream(gde_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int gde_serve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const int32_t* seeds, const double* eps,
+              const double* arrival_ms, void* x_out, void* r_out, int out64, int out_mem, int64_t ld_out,
+              double* oper_out, int32_t* rounds_out, float* lat_ms_out, gde_stats* stats) {
+    if (!ctx || !G || !p || nq < 0 || (nq > 0 && (!seeds || !eps))) return fail(ctx, GDE_EINVAL, "bad serve arguments");
+    if (p->method != M_LOCAL_GD || (p->kind != KIND_PPR && p->kind != KIND_KATZ))
+        return fail(ctx, GDE_EINVAL, "served queries are PPR or Katz local GD");
+    CK(cudaSetDevice(ctx->device));
+    const int64_t n = G->g.n;
+    if (ld_out < n && (x_out || r_out)) return fail(ctx, GDE_EINVAL, "ld_out < n");
+    for (int64_t q = 0; q < nq; q++) {
+        if (seeds[q] < 0 || seeds[q] >= n) return fail(ctx, GDE_EINVAL, "seed out of range");
+        if (!(eps[q] > 0.0)) return fail(ctx, GDE_EINVAL, "eps must be > 0");
+        if (arrival_ms && !(arrival_ms[q] >= 0.0)) return fail(ctx, GDE_EINVAL, "arrival times must be >= 0");
+        if (p->kind == KIND_PPR && !(eps[q] * G->h_deg[G->node_in(seeds[q])] <= 1.))
+            return fail(ctx, GDE_EINVAL, "eps * degree[s_node] > 1 (ppr_solver.py:213)");
+    }
+    if (stats) memset(stats, 0, sizeof(*stats));
+    if (nq == 0) return GDE_OK;
+    return solve_served(ctx, G, p, nq, seeds, eps, arrival_ms, x_out, r_out, out64, out_mem, ld_out, oper_out,
+                        rounds_out, lat_ms_out, stats);
+}
 
 int gde_ctx_sync(gde_ctx* ctx) {
     if (!ctx) return GDE_EINVAL;
@@ -554,6 +753,13 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
     if (hk && !(p->tau >= 1.0)) return fail(ctx, GDE_EINVAL, "tau must be >= 1 (hk_solver.py:35)");
     if (stats) memset(stats, 0, sizeof(*stats));
     if (nq == 0) return GDE_OK;
+
+    // PPR / Katz local GD with one column per tile runs as a served queue:
+    // slots cycle through the queries inside one persistent launch.
+    const bool crossing = (method == M_LOCAL_GD) && (kind == KIND_PPR || kind == KIND_KATZ);
+    if (crossing && p->tile_w <= 1)
+        return solve_served(ctx, G, p, nq, seeds, eps, nullptr, x_out, r_out, out64, out_mem, ld_out, oper_out,
+                            rounds_out, lat_ms_out, stats);
 
     int W = p->tile_w;
     if (W <= 0) W = (nq == 1) ? 1 : (prec64 ? 4 : 8);
@@ -758,8 +964,8 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
         bool capped = false;
         for (int t = 0; t < nt; t++) {
             const TileState& S = ctx->hts[t];
-            ctx->stamp[t] = S.stamp + S.round + base.max_rounds + 4;
-            if (!S.done) capped = true;
+            ctx->stamp[t] = S.stamp + (int)std::max<long long>(0, (long long)ctx->hstats->iters - S.t0) + 4;
+            if (S.done == SLOT_LIVE) capped = true;
             const TileDef& td = tiles[t0 + t];
             for (int c = 0; c < (int)td.qs.size(); c++) {
                 const ColState& C = hcs[(size_t)t * W + c];
@@ -896,8 +1102,9 @@ static int feature_push_impl(gde_ctx* ctx, gde_graph* G, const gde_params* p, in
         CK(cudaStreamSynchronize(ctx->stream));
         bool capped = false;
         for (int t = 0; t < nt; t++) {
-            ctx->stamp[t] = ctx->hts[t].stamp + ctx->hts[t].round + base.max_rounds + 4;
-            if (!ctx->hts[t].done) capped = true;
+            ctx->stamp[t] =
+                ctx->hts[t].stamp + (int)std::max<long long>(0, (long long)ctx->hstats->iters - ctx->hts[t].t0) + 4;
+            if (ctx->hts[t].done == SLOT_LIVE) capped = true;
             for (int c = 0; c < W; c++)
                 if (oper_out) oper_out[(int64_t)(t0 + t) * W + c] = hcs[(size_t)t * W + c].oper;
         }

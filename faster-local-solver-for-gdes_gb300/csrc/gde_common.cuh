@@ -88,16 +88,43 @@ struct TileParams {           // host-written, read-only during a launch
 //   SCATTER(r) reads the p counters; appends to cand_cnt[(r+1)%3]; block 0
 //              writes ts.done / dense_next[p^1] / ColState.live, which are
 //              only read at the start of the next round.
+enum SlotState : int {
+    SLOT_LIVE = 0,    // pushing; level = it - t0
+    SLOT_DONE = 1,    // finished (batch solves: results extracted after the launch)
+    SLOT_IDLE = 2,    // served solves: result extracted and slot cleared, awaiting a query
+    SLOT_EMPTY = 3,   // served solves: no query left for this slot
+};
+
 struct TileState {            // device-updated
     int cand_cnt[3];          // candidate list sizes (by level mod 3)
     int front_cnt[2];         // frontier sizes (by parity)
     int small_cnt[2], med_cnt[2], large_cnt[2];
     int dense_next[2];        // 1: the PREP of that parity scans all nodes
-    int round;                // rounds completed before the current launch
-    int done;                 // 1 when every column finished
+    int t0;                   // launch iteration at which the tile's level 0 ran
+    int done;                 // SlotState
     int stamp;                // touch-stamp base (marks start at -1; stamps only grow)
-    int pad;
+    int qid;                  // served solves: query in this slot (-1 none)
     double union_vol[2];      // volume of the union frontier per round parity
+};
+
+// Served solves: a queue of single-column queries cycling through the slots.
+struct ServeQueue {
+    int nq;                       // queries in the queue
+    int* next;                    // next query to admit (device counter)
+    const int32_t* seed;          // internal seed id per query
+    const double* theta;          // threshold scale per query
+    const double* r0;             // initial residual at the seed
+    const long long* arrival_ns;  // admission not before kernel start + arrival (nullptr: immediately)
+    void* x_out;                  // [nq][ld_out] solution rows, caller node order
+    void* r_out;                  // [nq][ld_out] residual rows (may be null)
+    int64_t ld_out;
+    int out64;
+    const int32_t* seed_caller;   // caller seed id per query (Katz GD: x[s] -= 1)
+    double seed_add;
+    double* oper;                 // [nq] operation counts
+    int* rounds;                  // [nq]
+    unsigned long long* start_ns; // [nq] admission time
+    unsigned long long* finish_ns;// [nq] finish time
 };
 
 struct ColState {             // one per column slot
@@ -125,6 +152,7 @@ struct LaunchStats {          // roofline counters summed over a launch
     unsigned long long check_ns;       // block 0's time in CHECK phases (incl. barrier wait)
     unsigned long long prep_ns;        // ... PREP phases
     unsigned long long scatter_ns;     // ... SCATTER phases
+    unsigned long long iters;          // launch iterations run
 };
 
 struct GridBarrier {
@@ -165,6 +193,8 @@ struct PushArgs {
     int round_budget;          // rounds to advance in this launch (serving ticks)
     int kahan;                 // compensated FP32 solution
     int allow_dense;           // 0: every round visits only touched nodes (dynamic updates)
+    int serve;                 // 1: slots (W = 1 tiles) cycle through `queue`
+    ServeQueue queue;
 };
 
 }  // namespace gde

@@ -185,7 +185,7 @@ __device__ void load_tile(const PushArgs& a, int t, int it, TileSh& sh) {
     if (threadIdx.x == 0) {
         const TileState& ts = a.ts[t];
         sh.tp = a.tp[t];
-        sh.level = ts.round + it;
+        sh.level = it - ts.t0;
         int par = sh.level & 1;
         sh.parity = par;
         sh.m3 = sh.level % 3;
@@ -240,7 +240,7 @@ __device__ void check_phase(const PushArgs& a, int t, int it, int* s_cnt) {
     __shared__ int s_par;
     const int64_t n = a.g.n;
     const T* R = slab_ptr<T>(a.R, a, t);
-    if (threadIdx.x == 0) s_par = (a.ts[t].round + it) & 1;
+    if (threadIdx.x == 0) s_par = (it - a.ts[t].t0) & 1;
     if (threadIdx.x < W) {
         const ColState& c = a.cs[(int64_t)t * W + threadIdx.x];
         s_live[threadIdx.x] = (threadIdx.x < a.tp[t].ncols) && c.live;
@@ -287,8 +287,10 @@ constexpr int kMaxLaunchTiles = 512;
 struct RoundSh {
     int ntl;                                    // live tiles this round
     int any_check;                              // some live tile needs a CHECK phase
+    int any_idle;                               // served solves: some slot awaits a query
     int tiles[kMaxLaunchTiles];                 // live tile ids (ascending)
-    long long off[3][kMaxLaunchTiles + 1];      // exclusive prefix sums of the current phase's spaces
+    unsigned char idle[kMaxLaunchTiles];        // slot was idle at the round start
+    long long off[4][kMaxLaunchTiles + 1];      // exclusive prefix sums of the current phase's spaces
     int level[kMaxLaunchTiles];                 // per live tile: rounds since its start
     unsigned char flags[kMaxLaunchTiles];       // per live tile scatter flags (SF_*)
     long long scan_tmp[kWarps];
@@ -354,6 +356,8 @@ __device__ __forceinline__ int find_tile(const long long* off, int ntl, long lon
     }
     return lo;
 }
+
+constexpr long long kRetireChunk = 4096;  // nodes per extraction work item
 
 // This block's share [lo, hi) of a flattened space of `total` items.
 __device__ __forceinline__ void block_share(long long total, long long& lo, long long& hi) {
@@ -898,9 +902,97 @@ __device__ void finish_round(const PushArgs& a, int t, int level, bool dense_nex
     if (threadIdx.x == 0) {
         TileState& ts = a.ts[t];
         ts.dense_next[par ^ 1] = dense_next ? 1 : 0;
-        if (ts.front_cnt[par] == 0 || hk_end) ts.done = 1;
+        if (ts.front_cnt[par] == 0 || hk_end) {
+            if (a.serve) {
+                // served slot: the query's result is extracted and the slot
+                // cleared by every block in this SCATTER; admit next round
+                const ColState& cs = a.cs[(int64_t)t * W];
+                const int q = ts.qid;
+                a.queue.oper[q] = cs.oper;
+                a.queue.rounds[q] = cs.rounds;
+                a.queue.finish_ns[q] = globaltimer_ns();
+                ts.done = SLOT_IDLE;
+            } else {
+                ts.done = SLOT_DONE;
+            }
+        }
         atomicAdd(&a.stats->rounds, 1ull);
         if (dense_next) atomicAdd(&a.stats->dense_rounds, 1ull);
+    }
+}
+
+// Served solves: block 0 puts the next queued query into an idle slot (the
+// slot's vectors were cleared when its previous query retired, a round ago).
+// Everything written here is read only from the next round on.
+template <typename T, int W>
+__device__ void admit_query(const PushArgs& a, int t, int it) {
+    if (threadIdx.x != 0) return;
+    TileState& ts = a.ts[t];
+    const ServeQueue& q = a.queue;
+    const int qid = *q.next;
+    if (qid >= q.nq) {
+        ts.done = SLOT_EMPTY;
+        return;
+    }
+    const unsigned long long now = globaltimer_ns();
+    if (q.arrival_ns && now < a.stats->start_ns + (unsigned long long)q.arrival_ns[qid]) return;
+    *q.next = qid + 1;
+    const int64_t n = a.g.n;
+    const int seed = q.seed[qid];
+    // stamps must keep growing within the slot: skip past the last query's
+    ts.stamp = ts.stamp + (it - ts.t0) + 2;
+    for (int i = 0; i < 3; ++i) ts.cand_cnt[i] = 0;
+    for (int i = 0; i < 2; ++i) {
+        ts.front_cnt[i] = ts.small_cnt[i] = ts.med_cnt[i] = ts.large_cnt[i] = 0;
+        ts.dense_next[i] = 0;
+        ts.union_vol[i] = 0.0;
+    }
+    a.cand[((int64_t)t * 2 + 0) * n] = seed;  // level-0 candidates: the seed
+    ts.cand_cnt[0] = 1;
+    ts.t0 = it + 1;
+    ts.qid = qid;
+    ColState& cs = a.cs[(int64_t)t * W];
+    cs.theta = q.theta[qid];
+    cs.oper = 0.0;
+    cs.fsum = 0;
+    cs.live = 1;
+    cs.rounds = 0;
+    cs.round_active[0] = cs.round_active[1] = 0;
+    cs.check_cnt[0] = cs.check_cnt[1] = 0;
+    cs.seed = seed;
+    cs.finish_ns = 0;
+    slab_ptr<T>(a.R, a, t)[(int64_t)seed * a.ld] = (T)q.r0[qid];
+    q.start_ns[qid] = now;
+    __threadfence();
+    ts.done = SLOT_LIVE;
+}
+
+// Served solves: write a retiring slot's solution row (caller node order)
+// and clear the slot's vectors, nodes [beg, end) in caller order.
+template <typename T, int W>
+__device__ void retire_range(const PushArgs& a, int t, long long beg, long long end) {
+    const ServeQueue& q = a.queue;
+    const int qid = a.ts[t].qid;
+    T* X = slab_ptr<T>(a.X, a, t);
+    T* R = slab_ptr<T>(a.R, a, t);
+    float* XC = a.kahan ? slab_ptr<float>(a.XC, a, t) : nullptr;
+    const int32_t* perm = a.g.perm;
+    const int sc = q.seed_caller[qid];
+    for (long long u = beg + threadIdx.x; u < end; u += kThreads) {
+        const int64_t v = (perm ? (int64_t)perm[u] : u) * a.ld;
+        double x = (double)X[v];
+        if (u == sc) x = x + q.seed_add;
+        if (q.x_out) {
+            if (q.out64) reinterpret_cast<double*>(q.x_out)[(int64_t)qid * q.ld_out + u] = x;
+            else reinterpret_cast<float*>(q.x_out)[(int64_t)qid * q.ld_out + u] = (float)x;
+        }
+        if (q.r_out) {
+            if (q.out64) reinterpret_cast<double*>(q.r_out)[(int64_t)qid * q.ld_out + u] = (double)R[v];
+            else reinterpret_cast<float*>(q.r_out)[(int64_t)qid * q.ld_out + u] = (float)R[v];
+        }
+        X[v] = T(0);
+        R[v] = T(0);
+        if (XC) XC[v] = 0.f;
     }
 }
 
@@ -916,11 +1008,14 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
     int it = 0;
     for (; it < a.round_budget; ++it) {
         // ---- live tiles of this round (identical in every block) ----
-        if (threadIdx.x == 0) rs.any_check = 0;
+        if (threadIdx.x == 0) { rs.any_check = 0; rs.any_idle = 0; }
+        __syncthreads();
         for (int t = threadIdx.x; t < a.ntiles; t += kThreads) {
             const TileState& ts = a.ts[t];
-            const bool live = !ts.done && (ts.round + it) < a.max_rounds;
+            const bool live = ts.done == SLOT_LIVE && it >= ts.t0 && (it - ts.t0) < a.max_rounds;
             s_vals[t] = live ? 1 : 0;
+            rs.idle[t] = (ts.done == SLOT_IDLE) ? 1 : 0;
+            if (ts.done == SLOT_IDLE) rs.any_idle = 1;
         }
         __syncthreads();
         block_exclusive_scan(s_vals, a.ntiles, rs.off[0], rs.scan_tmp);
@@ -928,7 +1023,7 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
             if (rs.off[0][t + 1] != rs.off[0][t]) {
                 const int k = (int)rs.off[0][t];
                 rs.tiles[k] = t;
-                rs.level[k] = a.ts[t].round + it;
+                rs.level[k] = it - a.ts[t].t0;
                 const int m = a.tp[t].method;
                 if (m == M_GLOBAL_GD || m == M_GLOBAL_CHEBY) rs.any_check = 1;
             }
@@ -936,7 +1031,7 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
         if (threadIdx.x == 0) rs.ntl = (int)rs.off[0][a.ntiles];
         __syncthreads();
         const int ntl = rs.ntl;
-        if (ntl == 0) break;
+        if (ntl == 0 && !rs.any_idle) break;
         const bool timer = (blockIdx.x == 0 && threadIdx.x == 0);
         unsigned long long t0 = timer ? globaltimer_ns() : 0ull;
         // ---- CHECK (global GD / Chebyshev tiles) ----
@@ -1023,6 +1118,25 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
         }
         __syncthreads();
         block_exclusive_scan(s_vals, ntl, rs.off[2], rs.scan_tmp);
+        if (a.serve) {
+            // slots whose query finished this round: extract + clear, chunked
+            for (int k = threadIdx.x; k < ntl; k += kThreads) {
+                const TileState& ts = a.ts[rs.tiles[k]];
+                s_vals[k] = (ts.front_cnt[rs.level[k] & 1] == 0) ? (n + kRetireChunk - 1) / kRetireChunk : 0;
+            }
+            __syncthreads();
+            block_exclusive_scan(s_vals, ntl, rs.off[3], rs.scan_tmp);
+            long long lo, hi;
+            block_share(rs.off[3][ntl], lo, hi);
+            if (lo < hi) {
+                for (int k = find_tile(rs.off[3], ntl, lo); k < ntl && rs.off[3][k] < hi; ++k) {
+                    const long long b = max(lo, rs.off[3][k]) - rs.off[3][k];
+                    const long long e = min(hi, rs.off[3][k + 1]) - rs.off[3][k];
+                    if (b >= e) continue;
+                    retire_range<T, W>(a, rs.tiles[k], b * kRetireChunk, min((long long)n, e * kRetireChunk));
+                }
+            }
+        }
         // long-row chunks first (largest pieces), then medium, then short rows
         for (int sp = 2; sp >= 0; --sp) {
             const long long* off = rs.off[sp];
@@ -1049,6 +1163,10 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
             if (ts.front_cnt[lv & 1] == 0) continue;
             hk_drop<T, W>(a, t, lv, ts.dense_next[lv & 1] != 0, ts.cand_cnt[lv % 3]);
         }
+        if (blockIdx.x == 0 && a.serve && rs.any_idle) {
+            for (int t = 0; t < a.ntiles; ++t)
+                if (rs.idle[t]) admit_query<T, W>(a, t, it);
+        }
         if (blockIdx.x == 0) {
             for (int k = 0; k < ntl; ++k) {
                 const int t = rs.tiles[k];
@@ -1061,15 +1179,9 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
         if (!grid_barrier(a.bar, a.err)) return;
         if (timer) a.stats->scatter_ns += globaltimer_ns() - t0;
     }
-    // Record the rounds advanced by this launch (all blocks are past their
-    // last read of ts.round once the final barrier completes).
-    if (it > 0 && !grid_barrier(a.bar, a.err)) return;
-    if (blockIdx.x == 0) {
-        for (int t = threadIdx.x; t < a.ntiles; t += kThreads) {
-            TileState& ts = a.ts[t];
-            if (!ts.done) ts.round = min(ts.round + it, a.max_rounds);
-        }
-    }
+    // A tile still SLOT_LIVE after the launch stopped at max_rounds (the host
+    // reports GDE_EITERCAP for it).
+    if (blockIdx.x == 0 && threadIdx.x == 0) a.stats->iters = (unsigned long long)it;
 }
 
 }  // namespace

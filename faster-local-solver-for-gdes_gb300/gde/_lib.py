@@ -27,7 +27,8 @@ MEM_HOST, MEM_DEVICE = 0, 1
 class Params(ctypes.Structure):
     _fields_ = [("kind", _int), ("method", _int), ("prec", _int), ("tile_w", _int),
                 ("alpha", _dbl), ("tau", _dbl), ("l_max", _dbl), ("mu_min", _dbl), ("beta", _dbl), ("omega", _dbl),
-                ("max_rounds", _int), ("small_max", _int), ("med_max", _int), ("chunk", _int), ("dense_div", _int)]
+                ("max_rounds", _int), ("small_max", _int), ("med_max", _int), ("chunk", _int), ("dense_div", _int),
+                ("slots", _int)]
 
 
 class Stats(ctypes.Structure):
@@ -54,6 +55,8 @@ SIGNATURES = {
     "gde_solve": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _p, _p, _int, _int, _i64, _p, _p, _p,
                          ctypes.POINTER(Stats)]),
     "gde_ctx_stream": (_p, [_p]),
+    "gde_serve": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _p, _p, _p, _int, _int, _i64, _p, _p, _p,
+                         ctypes.POINTER(Stats)]),
     "gde_hk_estimate_n": (_i64, [_dbl, _dbl]),
     "gde_feature_push": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _i64, _dbl, _p, _i64, _p,
                                 ctypes.POINTER(Stats)]),

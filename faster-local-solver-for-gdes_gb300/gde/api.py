@@ -94,6 +94,7 @@ def make_params(kind: int, method: int, prec: str = "fp64", tile_w: int = 0, alp
     p.med_max = int(t.get("med_max", 0))
     p.chunk = int(t.get("chunk", 0))
     p.dense_div = int(t.get("dense_div", 0))
+    p.slots = int(t.get("slots", 0))
     return p
 
 
@@ -142,6 +143,50 @@ def solve(graph: Graph, kind: int, method: int, seeds, eps, *, prec: str = "fp64
     L.check(graph.ctx.ptr, status, "gde_solve")
     return {"x": x_out if want_x else None, "r": r_out if want_r else None, "oper": oper, "rounds": rounds,
             "latency_ms": lat, "stats": st.as_dict()}
+
+
+def serve(graph: Graph, kind: int, seeds, eps, *, arrival_ms=None, prec: str = "fp32", out64: bool | None = None,
+          want_x: bool = True, want_r: bool = False, x_out=None, r_out=None, device_out: bool = False,
+          alpha: float = 0.0, slots: int = 0, max_rounds: int = 0, tuning: dict | None = None) -> dict:
+    """Served PPR / Katz local GD (continuous batching); returns dict(x, r, oper, rounds, latency_ms, stats).
+
+    ``arrival_ms[q]``: query q arrives that many ms after the launch starts
+    and its latency is measured from its arrival (None: all at time 0).
+    """
+    lib = L.load()
+    seeds = np.ascontiguousarray(np.atleast_1d(seeds), dtype=np.int32)
+    nq = seeds.shape[0]
+    eps = np.ascontiguousarray(np.broadcast_to(np.asarray(eps, dtype=np.float64), (nq,)))
+    arr = None if arrival_ms is None else np.ascontiguousarray(arrival_ms, dtype=np.float64)
+    if out64 is None:
+        out64 = prec == "fp64"
+    n = graph.n
+    if want_x and x_out is None:
+        x_out = _alloc((nq, n), out64, device_out, graph)
+    if want_r and r_out is None:
+        r_out = _alloc((nq, n), out64, device_out, graph)
+    oper = np.zeros(nq, dtype=np.float64)
+    rounds = np.zeros(nq, dtype=np.int32)
+    lat = np.zeros(nq, dtype=np.float32)
+    t = dict(tuning or {})
+    if slots:
+        t["slots"] = slots
+    p = make_params(kind, L.LOCAL_GD, prec, 1, alpha, max_rounds=max_rounds, tuning=t)
+    st = L.Stats()
+    status = lib.gde_serve(graph.ctx.ptr, graph.ptr, ctypes.byref(p), nq, _ptr(seeds), _ptr(eps), _ptr(arr),
+                           _ptr(x_out) if want_x else None, _ptr(r_out) if want_r else None, int(out64),
+                           L.MEM_DEVICE if device_out else L.MEM_HOST, n, _ptr(oper), _ptr(rounds), _ptr(lat),
+                           ctypes.byref(st))
+    L.check(graph.ctx.ptr, status, "gde_serve")
+    return {"x": x_out if want_x else None, "r": r_out if want_r else None, "oper": oper, "rounds": rounds,
+            "latency_ms": lat, "stats": st.as_dict()}
+
+
+def _alloc(shape, out64: bool, device: bool, graph: Graph):
+    if device:
+        import torch
+        return torch.empty(shape, dtype=torch.float64 if out64 else torch.float32, device=f"cuda:{graph.ctx.device}")
+    return np.empty(shape, dtype=np.float64 if out64 else np.float32)
 
 
 def ctx_stream(ctx: Context | None = None) -> int:

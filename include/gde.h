@@ -74,6 +74,7 @@ typedef struct {
     int med_max;       /* <= med_max warp per row, else CTA chunks; 0 = default */
     int chunk;         /* edges per CTA chunk; 0 = default */
     int dense_div;     /* next round scans all nodes when vol(frontier) > n/dense_div; 0 = default */
+    int slots;         /* served PPR/Katz local GD: concurrent queries (one residual vector each); 0 = default */
 } gde_params;
 
 typedef struct {
@@ -138,6 +139,19 @@ int gde_solve(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t nq, const
 /* The context's CUDA stream (a cudaStream_t), for callers that order their
  * own work or CUDA events with the library's. */
 void *gde_ctx_stream(gde_ctx *ctx);
+
+/* ---- served queries (continuous batching) ----
+ * PPR / Katz local GD queries served by p->slots concurrent slots inside one
+ * persistent launch: a finished query's row is written and its slot handed
+ * to the next query on the device.  arrival_ms (host, may be NULL): query q
+ * is admitted no earlier than arrival_ms[q] after the launch starts, and its
+ * latency (lat_ms_out) is measured from that arrival.  gde_solve uses this
+ * path for PPR / Katz local GD with tile_w <= 1.  Replaces a loop of
+ * ppr_gd_local_gpu / katz_gd_local_gpu calls (ppr_solver.py:82-146,
+ * katz_solver.py:81-146) with a request stream. */
+int gde_serve(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t nq, const int32_t *seeds, const double *eps,
+              const double *arrival_ms, void *x_out, void *r_out, int out64, int out_mem, int64_t ld_out,
+              double *oper_out, int32_t *rounds_out, float *lat_ms_out, gde_stats *stats);
 
 /* heat-kernel Taylor length, hk_solver.py:28-48 (estimate_n) */
 int64_t gde_hk_estimate_n(double tau, double eps);
