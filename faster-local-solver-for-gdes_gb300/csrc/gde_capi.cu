@@ -702,6 +702,11 @@ int gde_graph_upload(gde_ctx* ctx, int64_t n, int64_t cap, const int64_t* indptr
         CK(cudaMemcpyAsync(G->perm_d, G->h_perm.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
     }
     G->g.perm = G->perm_d;
+    // hubs: the degree-sorted prefix of nodes with more than 64 neighbours;
+    // pushes into them are combined per warp before the atomic
+    G->g.hub_cut = 0;
+    if (G->relabeled)
+        while (G->g.hub_cut < n && G->h_len[G->g.hub_cut] > 64) G->g.hub_cut++;
     G->g.row_ptr = G->row_ptr;
     G->g.col = G->col;
     G->g.row_len = G->row_len;

@@ -59,6 +59,7 @@ struct DevGraph {
     double vol;               // sum of degrees (m)
     int degf_exact;           // 1 when every degree is an integer < 2^24 (degf == degd exactly)
     const int32_t* perm;      // caller id -> internal id (nullptr: identity)
+    int32_t hub_cut;          // internal ids < hub_cut are hubs (degree-sorted graphs; 0: none)
 };
 
 // ---------------------------------------------------------------------------

@@ -720,7 +720,43 @@ template <typename T, int W, int VEC, int L>
 __device__ __forceinline__ void edge_step(const PushArgs& a, const ScatterCtx<T, W>& c, bool ok, int v, int c0,
                                           int lane_g, int grp_w, const Vec<T, VEC>& p, const double (&theta)[VEC]) {
     bool cr = false;
-    if (ok) {
+    bool combined = false;
+    if constexpr (VEC == 1 && L == 1) {
+        // Hubs (degree-sorted prefix) receive pushes from many frontier leaves
+        // in the same round; lanes of a warp that target the same hub add in
+        // shared memory first and one lane issues the global atomic.  The
+        // crossing test on the combined add is the same test on the stored
+        // value (all additions are non-negative).
+        if (!c.tgt_scale) {
+            const bool hub = ok && v < a.g.hub_cut;
+            if (__any_sync(kFull, hub)) {
+                const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+                const unsigned peers = __match_any_sync(kFull, hub ? v : -1 - lane);
+                const int leader = __ffs(peers) - 1;
+                __shared__ T agg[kWarps][32];
+                if (hub && lane == leader) agg[warp][lane] = T(0);
+                __syncwarp();
+                if (hub) atomicAdd(&agg[warp][leader], p.v[0]);
+                __syncwarp();
+                if (hub && lane == leader) {
+                    const T tot = agg[warp][lane];
+                    T* addr = c.tgt + (int64_t)v * a.ld;
+                    if (c.cross) {
+                        const T old = atomicAdd(addr, tot);
+                        const T s = old + tot;
+                        const double dv = a.g.degf_exact ? (double)a.g.degf[v] : a.g.degd[v];
+                        const double thr = theta[0] * dv;
+                        cr = ((double)old < thr) && ((double)s >= thr);
+                    } else {
+                        atomicAdd(addr, tot);
+                    }
+                }
+                __syncwarp();
+                combined = hub;
+            }
+        }
+    }
+    if (ok && !combined) {
         if (c.cross) {
             Vec<T, VEC> old;
             vatomic_ret<T, VEC>(c.tgt + (int64_t)v * a.ld + c0, p, old);
@@ -880,26 +916,43 @@ __device__ void hk_drop(const PushArgs& a, int t, int level, bool dense, int can
 // (ppr_solver.py:266-267); a global column whose CHECK found nothing above
 // threshold is finished (:292-293); HK stops after its last level
 // (hk_solver.py:235); a tile is done when its frontier is empty.
-template <int W>
-__device__ void finish_round(const PushArgs& a, int t, int level, bool dense_next) {
-    const TileParams& tp = a.tp[t];
+__device__ __forceinline__ bool hk_end_level(const TileParams& tp, int level) {
     const int m = tp.method;
-    const int par = level & 1;
-    const bool gcheck = (m == M_GLOBAL_GD || m == M_GLOBAL_CHEBY);
-    const bool hk_end = method_is_hk(m) && ((m == M_HK_TAYLOR) ? (level >= tp.n_levels) : (level + 1 >= tp.n_levels));
-    if (threadIdx.x < W && threadIdx.x < tp.ncols) {
-        ColState& cs = a.cs[(int64_t)t * W + threadIdx.x];
+    return method_is_hk(m) && ((m == M_HK_TAYLOR) ? (level >= tp.n_levels) : (level + 1 >= tp.n_levels));
+}
+
+// Column part of the bookkeeping: one thread per (live tile, column).
+template <int W>
+__device__ void finish_columns_all(const PushArgs& a, const RoundSh& rs, int ntl) {
+    for (int idx = threadIdx.x; idx < ntl * W; idx += kThreads) {
+        const int k = idx / W, c = idx % W;
+        const int t = rs.tiles[k];
+        const int level = rs.level[k];
+        const TileParams& tp = a.tp[t];
+        if (c >= tp.ncols) continue;
+        const int m = tp.method;
+        const int par = level & 1;
+        const bool gcheck = (m == M_GLOBAL_GD || m == M_GLOBAL_CHEBY);
+        ColState& cs = a.cs[(int64_t)t * W + c];
         if (cs.live) {
             bool worked = gcheck ? (cs.check_cnt[par] > 0) : (cs.round_active[par] > 0);
             if (method_is_hk(m) && m != M_HK_LOCAL) worked = true;  // fixed sweeps per level
             if (worked) cs.rounds += 1;
-            if (!worked || hk_end) {
+            if (!worked || hk_end_level(tp, level)) {
                 cs.live = 0;
                 cs.finish_ns = globaltimer_ns();
             }
         }
     }
-    if (threadIdx.x == 0) {
+}
+
+// Tile part of the bookkeeping (after the column part): one thread per tile.
+template <int W>
+__device__ void finish_round(const PushArgs& a, int t, int level, bool dense_next) {
+    const TileParams& tp = a.tp[t];
+    const int par = level & 1;
+    const bool hk_end = hk_end_level(tp, level);
+    {
         TileState& ts = a.ts[t];
         ts.dense_next[par ^ 1] = dense_next ? 1 : 0;
         if (ts.front_cnt[par] == 0 || hk_end) {
@@ -1168,12 +1221,13 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
                 if (rs.idle[t]) admit_query<T, W>(a, t, it);
         }
         if (blockIdx.x == 0) {
-            for (int k = 0; k < ntl; ++k) {
+            finish_columns_all<W>(a, rs, ntl);
+            __syncthreads();
+            for (int k = threadIdx.x; k < ntl; k += kThreads) {
                 const int t = rs.tiles[k];
                 const int lv = rs.level[k];
                 const bool dnext = dense_next_round(a, a.tp[t], a.ts[t], lv & 1);
                 finish_round<W>(a, t, lv, dnext);
-                __syncthreads();
             }
         }
         if (!grid_barrier(a.bar, a.err)) return;
