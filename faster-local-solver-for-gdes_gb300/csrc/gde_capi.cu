@@ -139,7 +139,10 @@ int64_t estimate_n(double t, double eps) {
 }
 
 struct Defaults {
-    int small_max = 8, med_max = 2048, chunk = 2048, dense_div = 2;
+    // every piece of push work is at most 8 dependent warp iterations (W = 1):
+    // short rows one lane each, medium rows one warp each, long rows split
+    // into warp-sized chunks
+    int small_max = 8, med_max = 256, chunk = 256, dense_div = 2;
 };
 
 void fill_tuning(const gde_params* p, PushArgs& a) {

@@ -794,18 +794,22 @@ __device__ __forceinline__ void push_edge(const DevGraph& g, T* tgt, int64_t ld,
     vred<T, VEC>(tgt + (int64_t)v * ld + c0, q);
 }
 
-// long rows: the whole CTA pushes chunks [beg, end) of tile t
+// long rows: one warp per chunk of a.chunk edges, chunks [beg, end) of tile
+// t (every piece of work is a few dependent warp iterations, so no single
+// hub row becomes the round's critical path)
 template <typename T, int W>
 __device__ void scatter_large(const PushArgs& a, int t, const ScatterCtx<T, W>& c, long long beg, long long end) {
     constexpr int VEC = (sizeof(T) == 4) ? (W >= 4 ? 4 : W) : (W >= 2 ? 2 : 1);
     constexpr int L = W / VEC;
+    constexpr int GPW = 32 / L;
     const DevGraph& g = a.g;
-    const int lane_g = threadIdx.x % L, grp_w = (threadIdx.x & 31) / L;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int lane_g = lane % L, grp_w = lane / L;
     const int c0 = lane_g * VEC;
     const int2* blarge = a.blarge + (int64_t)t * a.large_cap;
     double theta[VEC];
     load_thetas<T, VEC>(c.cs, c0, c.cross, theta);
-    for (long long k = beg; k < end; ++k) {
+    for (long long k = beg + warp; k < end; k += kWarps) {
         const int2 e = blarge[k];
         const int u = c.front[e.x];
         const int64_t rp = g.row_ptr[u];
@@ -814,9 +818,8 @@ __device__ void scatter_large(const PushArgs& a, int t, const ScatterCtx<T, W>& 
         const int en = min(len, b + a.chunk);
         Vec<T, VEC> p;
         vload<T, VEC>(c.Pw + (int64_t)e.x * W + c0, p);
-        const int gidx = threadIdx.x / L;
-        for (int j0 = b; j0 < en; j0 += kThreads / L) {
-            const int j = j0 + gidx;
+        for (int j0 = b; j0 < en; j0 += GPW) {
+            const int j = j0 + grp_w;
             const bool ok = j < en;
             const int v = ok ? g.col[rp + j] : 0;
             edge_step<T, W, VEC, L>(a, c, ok, v, c0, lane_g, grp_w, p, theta);
