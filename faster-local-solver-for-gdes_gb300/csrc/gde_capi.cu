@@ -195,11 +195,10 @@ int alloc_tiles(gde_ctx* ctx, gde_graph* G, int ntiles, int W, int prec64, bool 
     a.P = wsget(ctx, "P", slab);
     a.cand = (int32_t*)wsget(ctx, "cand", (size_t)ntiles * 2 * n * 4);
     a.front = (int32_t*)wsget(ctx, "front", (size_t)ntiles * n * 4);
-    a.bsmall = (int32_t*)wsget(ctx, "bsmall", (size_t)ntiles * n * 4);
-    a.bmed = (int32_t*)wsget(ctx, "bmed", (size_t)ntiles * n * 4);
+    a.bsmall = (PushItem*)wsget(ctx, "items", (size_t)ntiles * n * sizeof(PushItem));
     bool fresh = false;
     a.mark = (int32_t*)wsget(ctx, "mark", (size_t)ntiles * n * 4, &fresh);
-    if (!a.P || !a.cand || !a.front || !a.bsmall || !a.bmed || !a.mark)
+    if (!a.P || !a.cand || !a.front || !a.bsmall || !a.mark)
         return fail(ctx, GDE_ENOMEM, "device memory exhausted (frontier lists)");
     if (fresh) {
         CK(cudaMemsetAsync(a.mark, 0xff, ctx->ws["mark"].bytes, ctx->stream));
@@ -221,7 +220,7 @@ int alloc_large(gde_ctx* ctx, gde_graph* G, int ntiles, TileWs& tw) {
     PushArgs& a = tw.a;
     int64_t cap = G->g.cap;
     a.large_cap = cap / std::max(a.chunk, 1) + cap / std::max(a.med_max, 1) + 64;
-    a.blarge = (int2*)wsget(ctx, "blarge", (size_t)ntiles * a.large_cap * sizeof(int2));
+    a.blarge = (PushItem*)wsget(ctx, "blarge", (size_t)ntiles * a.large_cap * sizeof(PushItem));
     if (!a.blarge) return fail(ctx, GDE_ENOMEM, "device memory exhausted (chunk list)");
     return GDE_OK;
 }

@@ -156,9 +156,22 @@ struct LaunchStats {          // roofline counters summed over a launch
     unsigned long long iters;          // launch iterations run
 };
 
+// Arrival counter and generation word on separate 128-byte lines: waiting
+// blocks poll `gen` without slowing the arrivals on `count`.
 struct GridBarrier {
     unsigned int count;
+    unsigned int pad0[31];
     unsigned int gen;
+    unsigned int pad1[31];
+};
+
+// A piece of push work: `len` edges of one frontier row starting at col[rp]
+// (a whole short/medium row, or one chunk of a long row), and the row's
+// frontier index (its push values are P[fidx][0..W)).
+struct PushItem {
+    long long rp;
+    int len;
+    int fidx;
 };
 
 // Engine launch parameters (passed by value to the persistent kernel).
@@ -175,9 +188,8 @@ struct PushArgs {
     int32_t* cand;             // [ntiles][2][n] (list storage by parity)
     int32_t* front;            // [ntiles][n]
     void* P;                   // [ntiles][n][W] push rows
-    int32_t* bsmall;           // [ntiles][n]
-    int32_t* bmed;             // [ntiles][n]
-    int2* blarge;              // [ntiles][large_cap]
+    PushItem* bsmall;          // [ntiles][n]   short rows from index 0 up, medium rows from n-1 down
+    PushItem* blarge;          // [ntiles][large_cap]  chunks of long rows
     int64_t large_cap;
     int32_t* mark;             // [ntiles][n]
     TileParams* tp;            // [ntiles]

@@ -373,6 +373,9 @@ struct PrepSh {
     int col_nodes[kMaxW];
     double vol;
     int nodes;
+    // this block's launch totals (LaunchStats fields), flushed at kernel end
+    unsigned long long acc_col_nodes, acc_union_nodes;
+    double acc_col_vol, acc_union_vol;
 };
 
 template <typename T, int W>
@@ -396,9 +399,9 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
     int32_t* mark = a.mark + (int64_t)t * n;
     int32_t* front = a.front + (int64_t)t * n;
     T* Pw = reinterpret_cast<T*>(a.P) + (int64_t)t * n * W;
-    int32_t* bsmall = a.bsmall + (int64_t)t * n;
-    int32_t* bmed = a.bmed + (int64_t)t * n;
-    int2* blarge = a.blarge + (int64_t)t * a.large_cap;
+    PushItem* bsmall = a.bsmall + (int64_t)t * n;       // short rows grow up from 0,
+    PushItem* bmed_end = bsmall + (n - 1);               // medium rows down from n-1
+    PushItem* blarge = a.blarge + (int64_t)t * a.large_cap;
     TileState& ts = a.ts[t];
     T* R = slab_ptr<T>((hk && (sh.level & 1)) ? a.R2 : a.R, a, t);
     T* X = slab_ptr<T>(a.X, a, t);
@@ -565,9 +568,11 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
         const bool node_in = node_act && !absorb;  // absorbed nodes do not push
         int len = 0;
         int nch = 0;
+        long long rp = 0;
         int bucket = -1;  // 0 short, 1 medium, 2 long
         if (node_in && leader) {
             len = g.row_len[u];
+            rp = g.row_ptr[u];
             if (len <= a.small_max) bucket = 0;
             else if (len <= a.med_max) bucket = 1;
             else { bucket = 2; nch = (len + a.chunk - 1) / a.chunk; }
@@ -600,11 +605,19 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
         if (leader && node_in) {
             fidx = b0 + __popc(bf & below);
             front[fidx] = u;
-            if (bucket == 0) bsmall[b1 + __popc(bs & below)] = fidx;
-            else if (bucket == 1) bmed[b2 + __popc(bm & below)] = fidx;
+            PushItem item;
+            item.rp = rp;
+            item.len = len;
+            item.fidx = fidx;
+            if (bucket == 0) bsmall[b1 + __popc(bs & below)] = item;
+            else if (bucket == 1) bmed_end[-(b2 + __popc(bm & below))] = item;
             else {
                 int lb = b3 + (sc - lch);
-                for (int ch = 0; ch < nch; ++ch) blarge[lb + ch] = make_int2(fidx, ch);
+                for (int ch = 0; ch < nch; ++ch) {
+                    item.rp = rp + (long long)ch * a.chunk;
+                    item.len = min(a.chunk, len - ch * a.chunk);
+                    blarge[lb + ch] = item;
+                }
             }
             my_vol += du;
             my_cnt += 1;
@@ -630,13 +643,13 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
         atomicAdd(&cs.round_active[par], ps.col_nodes[threadIdx.x]);
         atomicAdd(&cs.oper, ps.col_oper[threadIdx.x]);
         atomicAdd((unsigned long long*)&cs.fsum, (unsigned long long)ps.col_nodes[threadIdx.x]);
-        atomicAdd(&a.stats->col_nodes, (unsigned long long)ps.col_nodes[threadIdx.x]);
-        atomicAdd(&a.stats->col_vol, ps.col_oper[threadIdx.x]);
+        atomicAdd(&ps.acc_col_nodes, (unsigned long long)ps.col_nodes[threadIdx.x]);
+        atomicAdd(&ps.acc_col_vol, ps.col_oper[threadIdx.x]);
     }
     if (threadIdx.x == 0 && ps.nodes) {
         atomicAdd(&ts.union_vol[par], ps.vol);
-        atomicAdd(&a.stats->union_nodes, (unsigned long long)ps.nodes);
-        atomicAdd(&a.stats->union_vol, ps.vol);
+        ps.acc_union_nodes += (unsigned long long)ps.nodes;
+        ps.acc_union_vol += ps.vol;
     }
     __syncthreads();
 }
@@ -794,11 +807,15 @@ __device__ __forceinline__ void push_edge(const DevGraph& g, T* tgt, int64_t ld,
     vred<T, VEC>(tgt + (int64_t)v * ld + c0, q);
 }
 
-// long rows: one warp per chunk of a.chunk edges, chunks [beg, end) of tile
-// t (every piece of work is a few dependent warp iterations, so no single
-// hub row becomes the round's critical path)
+// Medium rows and chunks of long rows: one warp per work item, items
+// [beg, end) of `items` read with stride `step` (+1 for chunks, -1 for
+// medium rows, which fill the short-row array from its end; each item is at most a.med_max / a.chunk edges, a
+// few dependent warp iterations, so no hub row becomes the round's critical
+// path).  The item carries the row's start and length, so the warp goes
+// straight from the item to the column indices.
 template <typename T, int W>
-__device__ void scatter_large(const PushArgs& a, int t, const ScatterCtx<T, W>& c, long long beg, long long end) {
+__device__ void scatter_warp_items(const PushArgs& a, const PushItem* items, int step,
+                                   const ScatterCtx<T, W>& c, long long beg, long long end) {
     constexpr int VEC = (sizeof(T) == 4) ? (W >= 4 ? 4 : W) : (W >= 2 ? 2 : 1);
     constexpr int L = W / VEC;
     constexpr int GPW = 32 / L;
@@ -806,51 +823,16 @@ __device__ void scatter_large(const PushArgs& a, int t, const ScatterCtx<T, W>& 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int lane_g = lane % L, grp_w = lane / L;
     const int c0 = lane_g * VEC;
-    const int2* blarge = a.blarge + (int64_t)t * a.large_cap;
     double theta[VEC];
     load_thetas<T, VEC>(c.cs, c0, c.cross, theta);
     for (long long k = beg + warp; k < end; k += kWarps) {
-        const int2 e = blarge[k];
-        const int u = c.front[e.x];
-        const int64_t rp = g.row_ptr[u];
-        const int len = g.row_len[u];
-        const int b = e.y * a.chunk;
-        const int en = min(len, b + a.chunk);
+        const PushItem it = items[k * step];
         Vec<T, VEC> p;
-        vload<T, VEC>(c.Pw + (int64_t)e.x * W + c0, p);
-        for (int j0 = b; j0 < en; j0 += GPW) {
+        vload<T, VEC>(c.Pw + (int64_t)it.fidx * W + c0, p);
+        for (int j0 = 0; j0 < it.len; j0 += GPW) {
             const int j = j0 + grp_w;
-            const bool ok = j < en;
-            const int v = ok ? g.col[rp + j] : 0;
-            edge_step<T, W, VEC, L>(a, c, ok, v, c0, lane_g, grp_w, p, theta);
-        }
-    }
-}
-
-// medium rows: one warp per row, rows [beg, end) of tile t
-template <typename T, int W>
-__device__ void scatter_med(const PushArgs& a, int t, const ScatterCtx<T, W>& c, long long beg, long long end) {
-    constexpr int VEC = (sizeof(T) == 4) ? (W >= 4 ? 4 : W) : (W >= 2 ? 2 : 1);
-    constexpr int L = W / VEC;
-    constexpr int GPW = 32 / L;
-    const DevGraph& g = a.g;
-    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const int lane_g = lane % L, grp_w = lane / L;
-    const int c0 = lane_g * VEC;
-    const int32_t* bmed = a.bmed + (int64_t)t * a.g.n;
-    double theta[VEC];
-    load_thetas<T, VEC>(c.cs, c0, c.cross, theta);
-    for (long long k = beg + warp; k < end; k += kWarps) {
-        const int f = bmed[k];
-        const int u = c.front[f];
-        const int64_t rp = g.row_ptr[u];
-        const int len = g.row_len[u];
-        Vec<T, VEC> p;
-        vload<T, VEC>(c.Pw + (int64_t)f * W + c0, p);
-        for (int j0 = 0; j0 < len; j0 += GPW) {
-            const int j = j0 + grp_w;
-            const bool ok = j < len;
-            const int v = ok ? g.col[rp + j] : 0;
+            const bool ok = j < it.len;
+            const int v = ok ? g.col[it.rp + j] : 0;
             edge_step<T, W, VEC, L>(a, c, ok, v, c0, lane_g, grp_w, p, theta);
         }
     }
@@ -866,7 +848,7 @@ __device__ void scatter_small(const PushArgs& a, int t, const ScatterCtx<T, W>& 
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const int lane_g = lane % L, grp_w = lane / L;
     const int c0 = lane_g * VEC;
-    const int32_t* bsmall = a.bsmall + (int64_t)t * a.g.n;
+    const PushItem* bsmall = a.bsmall + (int64_t)t * a.g.n;
     double theta[VEC];
     load_thetas<T, VEC>(c.cs, c0, c.cross, theta);
     for (long long kb = beg + (long long)warp * GPW; kb < end; kb += (long long)kWarps * GPW) {
@@ -878,11 +860,10 @@ __device__ void scatter_small(const PushArgs& a, int t, const ScatterCtx<T, W>& 
 #pragma unroll
         for (int i = 0; i < VEC; ++i) p.v[i] = T(0);
         if (okr) {
-            const int f = bsmall[k];
-            const int u = c.front[f];
-            rp = g.row_ptr[u];
-            len = g.row_len[u];
-            vload<T, VEC>(c.Pw + (int64_t)f * W + c0, p);
+            const PushItem it = bsmall[k];
+            rp = it.rp;
+            len = it.len;
+            vload<T, VEC>(c.Pw + (int64_t)it.fidx * W + c0, p);
         }
         int maxlen = len;
 #pragma unroll
@@ -1061,6 +1042,10 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
     __shared__ long long s_vals[kMaxLaunchTiles];
     const int64_t n = a.g.n;
     if (blockIdx.x == 0 && threadIdx.x == 0) a.stats->start_ns = globaltimer_ns();
+    if (threadIdx.x == 0) {
+        ps.acc_col_nodes = 0; ps.acc_union_nodes = 0;
+        ps.acc_col_vol = 0.0; ps.acc_union_vol = 0.0;
+    }
     int it = 0;
     for (; it < a.round_budget; ++it) {
         // ---- live tiles of this round (identical in every block) ----
@@ -1205,8 +1190,8 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
                 if (b >= e) continue;
                 const int t = rs.tiles[k];
                 const ScatterCtx<T, W> c = scatter_ctx<T, W>(a, t, rs.level[k], rs.flags[k]);
-                if (sp == 2) scatter_large<T, W>(a, t, c, b, e);
-                else if (sp == 1) scatter_med<T, W>(a, t, c, b, e);
+                if (sp == 2) scatter_warp_items<T, W>(a, a.blarge + (int64_t)t * a.large_cap, 1, c, b, e);
+                else if (sp == 1) scatter_warp_items<T, W>(a, a.bsmall + (int64_t)t * n + (n - 1), -1, c, b, e);
                 else scatter_small<T, W>(a, t, c, b, e);
             }
         }
@@ -1239,6 +1224,12 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
     // A tile still SLOT_LIVE after the launch stopped at max_rounds (the host
     // reports GDE_EITERCAP for it).
     if (blockIdx.x == 0 && threadIdx.x == 0) a.stats->iters = (unsigned long long)it;
+    if (threadIdx.x == 0 && ps.acc_union_nodes) {
+        atomicAdd(&a.stats->col_nodes, ps.acc_col_nodes);
+        atomicAdd(&a.stats->col_vol, ps.acc_col_vol);
+        atomicAdd(&a.stats->union_nodes, ps.acc_union_nodes);
+        atomicAdd(&a.stats->union_vol, ps.acc_union_vol);
+    }
 }
 
 }  // namespace
