@@ -11,8 +11,8 @@
  *
  * The reference exposes these operations as Python functions
  * (ppr_solver.py, katz_solver.py, hk_solver.py, InstantGNN.py); each entry
- * point below names the functions it replaces.  The ctypes binding used by
- * the drop-in Python modules is shown in INTEGRATION.md.
+ * point below names the functions it replaces.  The drop-in Python modules
+ * bind these entry points with ctypes (gde/_lib.py).
  */
 #ifndef GDE_H_
 #define GDE_H_
