@@ -1246,3 +1246,13 @@ cudaStream_t gde_internal_stream(gde_ctx* ctx) { return ctx->stream; }
 const double* gde_internal_npush(gde_graph* G) { return G->nfac; }
 const double* gde_internal_degd(gde_graph* G) { return G->degd; }
 bool gde_internal_relabeled(gde_graph* G) { return G->relabeled; }
+
+// ---------------------------------------------------------------------------
+// Internals shared with noalloc.cu
+// ---------------------------------------------------------------------------
+int gde_internal_device(gde_ctx* ctx) { return ctx->device; }
+int gde_internal_sms(gde_ctx* ctx) { return ctx->sms; }
+const DevGraph* gde_internal_devgraph(gde_graph* G) { return &G->g; }
+int32_t gde_internal_node_in(gde_graph* G, int64_t u) { return G->node_in(u); }
+double gde_internal_host_degree(gde_graph* G, int32_t u) { return G->h_deg[u]; }
+void gde_internal_fill_tuning(const gde_params* p, PushArgs* a) { fill_tuning(p, *a); }

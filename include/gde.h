@@ -189,6 +189,24 @@ int gde_feature_update(gde_ctx *ctx, gde_graph *g, int32_t *h_indices, int64_t *
 int gde_plain_ppr_local(gde_ctx *ctx, gde_graph *g, int32_t seed, double alpha, double eps, float *x_out,
                         float *r_out, double *oper_out, int32_t *rounds_out);
 
+/* ---- single-query solve that allocates no device memory ----
+ * No counterpart in the reference: an addition of this library for callers
+ * that must not allocate device memory while serving a request (a host that
+ * owns all GPU memory through its own pool, a latency-bound loop where
+ * cudaMalloc/cudaFree would synchronise the device, a process close to its
+ * memory limit).  One PPR or Katz query (p->kind GDE_PPR / GDE_KATZ, p->method
+ * GDE_LOCAL_GD / GDE_GLOBAL_GD, p->prec FP32 / FP64; same results as gde_solve
+ * for that query) whose workspace is a fixed 64 MiB device array inside the
+ * library: about 48 bytes per node in FP32 (56 in FP64) plus cap / 8 bytes;
+ * larger graphs are rejected with GDE_EINVAL.  Calls no cudaMalloc, cudaFree
+ * or other allocating routine.  Every call on a device shares the array, so
+ * calls whose GPU work overlaps race: serialise them.  The first call on a
+ * device looks the array up (cudaGetSymbolAddress); make it before any stream
+ * capture.  x_out / r_out: device [n] in caller node order (FP64 if out64,
+ * else FP32; may be NULL); oper_out / rounds_out: host (may be NULL). */
+int gde_solve_noalloc(gde_ctx *ctx, gde_graph *g, const gde_params *p, int32_t seed, double eps, void *x_out,
+                      void *r_out, int out64, double *oper_out, int32_t *rounds_out);
+
 #ifdef __cplusplus
 }
 #endif
