@@ -838,6 +838,188 @@ __device__ void scatter_warp_items(const PushArgs& a, const PushItem* items, int
     }
 }
 
+// ---------------------------------------------------------------------------
+// Single-column tiles (W = 1: served queries, single-column feature pushes).
+// Each lane keeps kEdgeILP independent edges in flight -- column loads, then
+// residual atomics, then threshold tests -- instead of one dependent chain
+// per edge: the kernel is bound by memory latency, not bandwidth.
+// ---------------------------------------------------------------------------
+constexpr int kEdgeILP = 4;
+
+// Warp-aggregated append of up to kEdgeILP crossing targets per lane (one
+// global atomic per warp).  On a W = 1 crossing tile every node crosses its
+// threshold at most once per round (additions are non-negative and every
+// residual starts the round below threshold), so no dedup mark is needed.
+__device__ __forceinline__ void append_crossings(const bool (&cr)[kEdgeILP], const int (&v)[kEdgeILP], int32_t* list,
+                                                 int* cnt) {
+    int mine = 0;
+#pragma unroll
+    for (int u = 0; u < kEdgeILP; ++u) mine += cr[u] ? 1 : 0;
+    if (__ballot_sync(kFull, mine != 0) == 0) return;
+    const int lane = threadIdx.x & 31;
+    int incl = mine;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, incl, o);
+        if (lane >= o) incl += y;
+    }
+    const int total = __shfl_sync(kFull, incl, 31);
+    int base = 0;
+    if (lane == 0) base = atomicAdd(cnt, total);
+    int pos = __shfl_sync(kFull, base, 0) + incl - mine;
+#pragma unroll
+    for (int u = 0; u < kEdgeILP; ++u)
+        if (cr[u]) list[pos++] = v[u];
+}
+
+// Push value p along kEdgeILP edges per lane (targets v[u] where ok[u]);
+// `hub_ok[u]` marks edges already added through the warp's hub combine
+// (their crossing result is in hub_cr[u]).
+template <typename T>
+__device__ __forceinline__ void edges_w1(const PushArgs& a, const ScatterCtx<T, 1>& c, const bool (&ok)[kEdgeILP],
+                                         const int (&v)[kEdgeILP], const T (&p)[kEdgeILP], double theta,
+                                         const bool (&hub_done)[kEdgeILP], const bool (&hub_cr)[kEdgeILP]) {
+    const DevGraph& g = a.g;
+    if (c.cross) {
+        float df[kEdgeILP];
+        T old[kEdgeILP];
+#pragma unroll
+        for (int u = 0; u < kEdgeILP; ++u) df[u] = (ok[u] && !hub_done[u]) ? g.degf[v[u]] : 1.f;
+#pragma unroll
+        for (int u = 0; u < kEdgeILP; ++u)
+            old[u] = (ok[u] && !hub_done[u]) ? atomicAdd(c.tgt + (int64_t)v[u] * a.ld, p[u]) : T(0);
+        bool cr[kEdgeILP];
+#pragma unroll
+        for (int u = 0; u < kEdgeILP; ++u) {
+            cr[u] = hub_cr[u];
+            if (ok[u] && !hub_done[u]) {
+                const double dv = g.degf_exact ? (double)df[u] : g.degd[v[u]];
+                const double thr = theta * dv;
+                const T s = old[u] + p[u];  // the value the atomic stored
+                cr[u] = ((double)old[u] < thr) && ((double)s >= thr);
+            }
+        }
+        append_crossings(cr, v, c.next, c.next_cnt);
+    } else {
+#pragma unroll
+        for (int u = 0; u < kEdgeILP; ++u) {
+            if (!ok[u] || hub_done[u] || p[u] == T(0)) continue;
+            T q = p[u];
+            if (c.tgt_scale) q = q / ((sizeof(T) == 4) ? (T)g.tfac_f[v[u]] : (T)g.tfac[v[u]]);  // InstantGNN.py:31
+            atomicAdd(c.tgt + (int64_t)v[u] * a.ld, q);
+        }
+        if (c.track) {
+#pragma unroll
+            for (int u = 0; u < kEdgeILP; ++u) append_once(ok[u], v[u], c.mark, c.stamp, c.next, c.next_cnt, kFull);
+        }
+    }
+}
+
+// W = 1 medium rows and long-row chunks: one warp per item, 32 * kEdgeILP
+// edges per warp iteration.  Lanes of one item target distinct nodes, so no
+// hub combine applies here.
+template <typename T>
+__device__ void scatter_warp_items_w1(const PushArgs& a, const PushItem* items, int step, const ScatterCtx<T, 1>& c,
+                                      long long beg, long long end) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const double theta = c.cross ? c.cs[0].theta : 0.0;
+    bool none[kEdgeILP];
+#pragma unroll
+    for (int u = 0; u < kEdgeILP; ++u) none[u] = false;
+    for (long long k = beg + warp; k < end; k += kWarps) {
+        const PushItem it = items[k * step];
+        const T pv = c.Pw[it.fidx];
+        T p[kEdgeILP];
+#pragma unroll
+        for (int u = 0; u < kEdgeILP; ++u) p[u] = pv;
+        for (int j0 = 0; j0 < it.len; j0 += 32 * kEdgeILP) {
+            bool ok[kEdgeILP];
+            int v[kEdgeILP];
+#pragma unroll
+            for (int u = 0; u < kEdgeILP; ++u) {
+                const int j = j0 + u * 32 + lane;
+                ok[u] = j < it.len;
+                v[u] = ok[u] ? a.g.col[it.rp + j] : 0;
+            }
+            edges_w1<T>(a, c, ok, v, p, theta, none, none);
+        }
+    }
+}
+
+// W = 1 short rows: one lane per row, kEdgeILP consecutive edges of the row
+// per step.  Lanes of a warp whose edges hit the same hub (degree-sorted
+// prefix) in a step add in shared memory first and one lane issues the
+// global atomic; the crossing test on the combined add is the same test on
+// the stored value.
+template <typename T>
+__device__ void scatter_small_w1(const PushArgs& a, int t, const ScatterCtx<T, 1>& c, long long beg, long long end) {
+    const DevGraph& g = a.g;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const PushItem* bsmall = a.bsmall + (int64_t)t * g.n;
+    const double theta = c.cross ? c.cs[0].theta : 0.0;
+    __shared__ T agg[kWarps][32];
+    for (long long kb = beg + (long long)warp * 32; kb < end; kb += (long long)kWarps * 32) {
+        const long long k = kb + lane;
+        int len = 0;
+        int64_t rp = 0;
+        T pv = T(0);
+        if (k < end) {
+            const PushItem it = bsmall[k];
+            rp = it.rp;
+            len = it.len;
+            pv = c.Pw[it.fidx];
+        }
+        int maxlen = len;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(kFull, maxlen, o));
+        T p[kEdgeILP];
+#pragma unroll
+        for (int u = 0; u < kEdgeILP; ++u) p[u] = pv;
+        for (int j0 = 0; j0 < maxlen; j0 += kEdgeILP) {
+            bool ok[kEdgeILP], hub_done[kEdgeILP], hub_cr[kEdgeILP];
+            int v[kEdgeILP];
+#pragma unroll
+            for (int u = 0; u < kEdgeILP; ++u) {
+                ok[u] = j0 + u < len;
+                v[u] = ok[u] ? g.col[rp + j0 + u] : 0;
+                hub_done[u] = false;
+                hub_cr[u] = false;
+            }
+            if (!c.tgt_scale) {
+#pragma unroll
+                for (int u = 0; u < kEdgeILP; ++u) {
+                    const bool hub = ok[u] && v[u] < g.hub_cut;
+                    if (!__any_sync(kFull, hub)) continue;
+                    const unsigned peers = __match_any_sync(kFull, hub ? v[u] : -1 - lane);
+                    const int leader = __ffs(peers) - 1;
+                    if (hub && lane == leader) agg[warp][lane] = T(0);
+                    __syncwarp();
+                    if (hub) atomicAdd(&agg[warp][leader], pv);
+                    __syncwarp();
+                    if (hub && lane == leader) {
+                        const T tot = agg[warp][lane];
+                        T* addr = c.tgt + (int64_t)v[u] * a.ld;
+                        if (c.cross) {
+                            const T old = atomicAdd(addr, tot);
+                            const T s = old + tot;
+                            const double dv = g.degf_exact ? (double)g.degf[v[u]] : g.degd[v[u]];
+                            const double thr = theta * dv;
+                            hub_cr[u] = ((double)old < thr) && ((double)s >= thr);
+                        } else {
+                            atomicAdd(addr, tot);
+                        }
+                    }
+                    __syncwarp();
+                    // non-leader hub lanes are done; the leader keeps ok[u] for
+                    // the (deduplicated) touch append when tracking
+                    hub_done[u] = hub;
+                }
+            }
+            edges_w1<T>(a, c, ok, v, p, theta, hub_done, hub_cr);
+        }
+    }
+}
+
 // short rows: one lane group per row, rows [beg, end) of tile t
 template <typename T, int W>
 __device__ void scatter_small(const PushArgs& a, int t, const ScatterCtx<T, W>& c, long long beg, long long end) {
@@ -1190,9 +1372,15 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
                 if (b >= e) continue;
                 const int t = rs.tiles[k];
                 const ScatterCtx<T, W> c = scatter_ctx<T, W>(a, t, rs.level[k], rs.flags[k]);
-                if (sp == 2) scatter_warp_items<T, W>(a, a.blarge + (int64_t)t * a.large_cap, 1, c, b, e);
-                else if (sp == 1) scatter_warp_items<T, W>(a, a.bsmall + (int64_t)t * n + (n - 1), -1, c, b, e);
-                else scatter_small<T, W>(a, t, c, b, e);
+                if constexpr (W == 1) {
+                    if (sp == 2) scatter_warp_items_w1<T>(a, a.blarge + (int64_t)t * a.large_cap, 1, c, b, e);
+                    else if (sp == 1) scatter_warp_items_w1<T>(a, a.bsmall + (int64_t)t * n + (n - 1), -1, c, b, e);
+                    else scatter_small_w1<T>(a, t, c, b, e);
+                } else {
+                    if (sp == 2) scatter_warp_items<T, W>(a, a.blarge + (int64_t)t * a.large_cap, 1, c, b, e);
+                    else if (sp == 1) scatter_warp_items<T, W>(a, a.bsmall + (int64_t)t * n + (n - 1), -1, c, b, e);
+                    else scatter_small<T, W>(a, t, c, b, e);
+                }
             }
         }
         // HK level drop (touches the current level's slab only)
