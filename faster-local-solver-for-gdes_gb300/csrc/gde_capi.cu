@@ -48,6 +48,10 @@ struct gde_ctx {
     std::vector<int> stamp;         // per-tile stamp bases (valid while "mark" is allocated)
     PlainWork plain{};
     int64_t plain_n = -1;
+    // opt-in push-kernel phase trace (gde_ctx_trace)
+    unsigned long long* trace = nullptr;
+    int trace_iters = 0;
+    int trace_grid = 0;
 };
 
 struct gde_graph {
@@ -74,6 +78,8 @@ struct gde_graph {
     bool relabeled = false;
     std::vector<int32_t> h_perm;
     int32_t* perm_d = nullptr;
+    uint32_t* col_deg = nullptr;
+    NodeRec* rec = nullptr;
     int32_t node_in(int64_t u) const { return relabeled ? h_perm[u] : (int32_t)u; }
 };
 
@@ -194,11 +200,10 @@ int alloc_tiles(gde_ctx* ctx, gde_graph* G, int ntiles, int W, int prec64, bool 
     }
     a.P = wsget(ctx, "P", slab);
     a.cand = (int32_t*)wsget(ctx, "cand", (size_t)ntiles * 2 * n * 4);
-    a.front = (int32_t*)wsget(ctx, "front", (size_t)ntiles * n * 4);
     a.bsmall = (PushItem*)wsget(ctx, "items", (size_t)ntiles * n * sizeof(PushItem));
     bool fresh = false;
     a.mark = (int32_t*)wsget(ctx, "mark", (size_t)ntiles * n * 4, &fresh);
-    if (!a.P || !a.cand || !a.front || !a.bsmall || !a.mark)
+    if (!a.P || !a.cand || !a.bsmall || !a.mark)
         return fail(ctx, GDE_ENOMEM, "device memory exhausted (frontier lists)");
     if (fresh) {
         CK(cudaMemsetAsync(a.mark, 0xff, ctx->ws["mark"].bytes, ctx->stream));
@@ -211,6 +216,8 @@ int alloc_tiles(gde_ctx* ctx, gde_graph* G, int ntiles, int W, int prec64, bool 
     a.cs = (ColState*)wsget(ctx, "cs", (size_t)ntiles * W * sizeof(ColState));
     if (!a.tp || !a.ts || !a.cs) return fail(ctx, GDE_ENOMEM, "device memory exhausted (tile state)");
     a.stats = ctx->dstats;
+    a.trace = ctx->trace;
+    a.trace_iters = ctx->trace ? ctx->trace_iters : 0;
     a.bar = ctx->bar;
     a.err = ctx->derr;
     return GDE_OK;
@@ -232,6 +239,10 @@ int run_engine(gde_ctx* ctx, PushArgs& a, int prec64, int W, gde_stats* st, doub
     CK(cudaMemsetAsync(ctx->bar, 0, sizeof(GridBarrier), ctx->stream));
     CK(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->stream));
     CK(cudaMemsetAsync(ctx->dstats, 0, sizeof(LaunchStats), ctx->stream));
+    if (ctx->trace) {
+        CK(cudaMemsetAsync(ctx->trace, 0, (size_t)ctx->trace_iters * grid * kTracePoints * 8, ctx->stream));
+        ctx->trace_grid = grid;
+    }
     if (!a.serve) a.round_budget = a.max_rounds + 1;
     CK(cudaEventRecord(ctx->ev[0], ctx->stream));
     cudaError_t e = engine_launch(a, prec64, W, grid, ctx->stream);
@@ -336,6 +347,50 @@ int upload_degrees(gde_ctx* ctx, gde_graph* G) {
     for (int64_t u = 0; u < n; u++)
         if ((double)df[u] != G->h_deg[u]) { exact = 0; break; }
     G->g.degf_exact = exact;
+    return GDE_OK;
+}
+
+// Static graphs: node records {row start, length, degree} and, when every
+// degree is an exact integer, column words carrying the target's degree in
+// the bits above the node id.  A graph that is edited later never gets them.
+int build_static_records(gde_ctx* ctx, gde_graph* G, const int32_t* col) {
+    const int64_t n = G->g.n, cap = G->g.cap;
+    std::vector<NodeRec> rec(n);
+    for (int64_t u = 0; u < n; u++) {
+        rec[u].rp = G->h_indptr[u];
+        rec[u].len = (int)G->h_len[u];
+        rec[u].degf = (float)G->h_deg[u];
+    }
+    if (cudaMalloc(&G->rec, n * sizeof(NodeRec)) != cudaSuccess) {
+        cudaGetLastError();
+        G->rec = nullptr;
+        return fail(ctx, GDE_ENOMEM, "device memory exhausted (node records)");
+    }
+    CK(cudaMemcpyAsync(G->rec, rec.data(), n * sizeof(NodeRec), cudaMemcpyHostToDevice, ctx->stream));
+    G->g.rec = G->rec;
+    int bits = 1;
+    while (((int64_t)1 << bits) < n) bits++;
+    const int dbits = 32 - bits;
+    if (G->g.degf_exact && dbits >= 4 && cap > 0) {
+        const uint32_t esc = (1u << dbits) - 1u;
+        std::vector<uint32_t> packed(cap);
+        for (int64_t j = 0; j < cap; j++) {
+            const int32_t v = col[j];
+            const double d = G->h_deg[v];
+            const uint32_t code = (d >= 0.0 && d < (double)esc && d == std::floor(d)) ? (uint32_t)d : esc;
+            packed[j] = (uint32_t)v | (code << bits);
+        }
+        if (cudaMalloc(&G->col_deg, cap * sizeof(uint32_t)) != cudaSuccess) {
+            cudaGetLastError();
+            G->col_deg = nullptr;
+            return fail(ctx, GDE_ENOMEM, "device memory exhausted (packed columns)");
+        }
+        CK(cudaMemcpyAsync(G->col_deg, packed.data(), cap * sizeof(uint32_t), cudaMemcpyHostToDevice, ctx->stream));
+        G->g.col_deg = G->col_deg;
+        G->g.idx_bits = bits;
+        G->g.deg_esc = esc;
+    }
+    CK(cudaStreamSynchronize(ctx->stream));
     return GDE_OK;
 }
 
@@ -574,6 +629,7 @@ int gde_ctx_destroy(gde_ctx* ctx) {
         cudaFree(ctx->plain.eps_vec); cudaFree(ctx->plain.queue); cudaFree(ctx->plain.nz);
         cudaFree(ctx->plain.d_count); cudaFree(ctx->plain.d_oper); cudaFreeHost(ctx->plain.h_count);
     }
+    if (ctx->trace) cudaFree(ctx->trace);
     cudaFree(ctx->bar);
     cudaFree(ctx->derr);
     cudaFree(ctx->dstats);
@@ -588,6 +644,40 @@ int gde_ctx_destroy(gde_ctx* ctx) {
 const char* gde_last_error(gde_ctx* ctx) { return ctx ? ctx->err.c_str() : "no context"; }
 
 void* gde_ctx_stream(gde_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+int gde_ctx_trace(gde_ctx* ctx, int iters) {
+    if (!ctx || iters < 0) return fail(ctx, GDE_EINVAL, "bad trace arguments");
+    CK(cudaSetDevice(ctx->device));
+    CK(cudaStreamSynchronize(ctx->stream));
+    if (ctx->trace) cudaFree(ctx->trace);
+    ctx->trace = nullptr;
+    ctx->trace_iters = 0;
+    ctx->trace_grid = 0;
+    if (iters == 0) return GDE_OK;
+    // room for the largest co-resident grid of any push-kernel instantiation
+    const size_t bytes = (size_t)iters * ctx->sms * 32 * kTracePoints * 8;
+    if (cudaMalloc(&ctx->trace, bytes) != cudaSuccess) {
+        cudaGetLastError();
+        ctx->trace = nullptr;
+        return fail(ctx, GDE_ENOMEM, "trace buffer");
+    }
+    CK(cudaMemsetAsync(ctx->trace, 0, bytes, ctx->stream));
+    ctx->trace_iters = iters;
+    return GDE_OK;
+}
+
+int gde_ctx_trace_read(gde_ctx* ctx, uint64_t* out, int64_t cap, int* iters, int* grid, int* points) {
+    if (!ctx) return GDE_EINVAL;
+    if (iters) *iters = ctx->trace_iters;
+    if (grid) *grid = ctx->trace_grid;
+    if (points) *points = kTracePoints;
+    if (!ctx->trace || !out) return GDE_OK;
+    const int64_t need = (int64_t)ctx->trace_iters * ctx->trace_grid * kTracePoints;
+    if (cap < need) return fail(ctx, GDE_EINVAL, "trace output too small");
+    CK(cudaStreamSynchronize(ctx->stream));
+    CK(cudaMemcpy(out, ctx->trace, (size_t)need * 8, cudaMemcpyDeviceToHost));
+    return GDE_OK;
+}
 
 int gde_serve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const int32_t* seeds, const double* eps,
               const double* arrival_ms, void* x_out, void* r_out, int out64, int out_mem, int64_t ld_out,
@@ -716,6 +806,10 @@ int gde_graph_upload(gde_ctx* ctx, int64_t n, int64_t cap, const int64_t* indptr
     G->g.degd = G->degd;
     int rc = upload_degrees(ctx, G);
     if (rc != GDE_OK) { gde_graph_free(G); return rc; }
+    if (G->relabeled) {
+        rc = build_static_records(ctx, G, col_src);
+        if (rc != GDE_OK) { gde_graph_free(G); return rc; }
+    }
     *out = G;
     return GDE_OK;
 }
@@ -726,6 +820,7 @@ int gde_graph_free(gde_graph* G) {
     cudaStreamSynchronize(G->ctx->stream);
     cudaFree(G->row_ptr); cudaFree(G->col); cudaFree(G->row_len); cudaFree(G->degf); cudaFree(G->degd);
     cudaFree(G->nfac); cudaFree(G->tfac); cudaFree(G->tfac_f); cudaFree(G->perm_d);
+    cudaFree(G->col_deg); cudaFree(G->rec);
     delete G;
     return GDE_OK;
 }

@@ -44,6 +44,14 @@ __host__ __device__ inline bool method_is_hk(int m) { return m == M_HK_LOCAL || 
 // ---------------------------------------------------------------------------
 // Device graph
 // ---------------------------------------------------------------------------
+// Per-node record of a static graph: one 16-byte load gives a frontier
+// node's row and degree.
+struct __align__(16) NodeRec {
+    long long rp;             // row start in col[]
+    int len;                  // row length
+    float degf;               // arithmetic degree
+};
+
 struct DevGraph {
     int64_t n;
     int64_t cap;              // capacity of col[] (nnz, or padded capacity)
@@ -60,6 +68,13 @@ struct DevGraph {
     int degf_exact;           // 1 when every degree is an integer < 2^24 (degf == degd exactly)
     const int32_t* perm;      // caller id -> internal id (nullptr: identity)
     int32_t hub_cut;          // internal ids < hub_cut are hubs (degree-sorted graphs; 0: none)
+    // Static graphs with exact integer degrees: col_deg[j] = col[j] | code << idx_bits,
+    // code = the target's degree, or deg_esc when it does not fit (read degf).
+    // Lets a push test the target's threshold without a second random load.
+    const uint32_t* col_deg;  // [cap] (nullptr: not built)
+    int idx_bits;
+    uint32_t deg_esc;
+    const NodeRec* rec;       // [n] (nullptr: not built)
 };
 
 // ---------------------------------------------------------------------------
@@ -186,7 +201,6 @@ struct PushArgs {
     float* XC;                 // Kahan compensation (FP32 solution), may be null
     void* DX;                  // Chebyshev delta-x slab
     int32_t* cand;             // [ntiles][2][n] (list storage by parity)
-    int32_t* front;            // [ntiles][n]
     void* P;                   // [ntiles][n][W] push rows
     PushItem* bsmall;          // [ntiles][n]   short rows from index 0 up, medium rows from n-1 down
     PushItem* blarge;          // [ntiles][large_cap]  chunks of long rows
@@ -208,6 +222,21 @@ struct PushArgs {
     int allow_dense;           // 0: every round visits only touched nodes (dynamic updates)
     int serve;                 // 1: slots (W = 1 tiles) cycle through `queue`
     ServeQueue queue;
+    unsigned long long* trace; // [trace_iters][grid][kTracePoints] %globaltimer stamps (nullptr: off)
+    int trace_iters;
+};
+
+// Phase boundaries stamped per block and launch iteration when tracing is on.
+enum TracePoint : int {
+    TP_ITER = 0,        // iteration start
+    TP_PREP_WORK,       // after the round set-up, PREP work begins
+    TP_PREP_DONE,       // PREP work done, entering the grid barrier
+    TP_PREP_BAR,        // PREP barrier passed
+    TP_SCAT_WORK,       // SCATTER set-up (scans, retire) done, push work begins
+    TP_SCAT_DONE,       // push work done (before HK drop / block-0 bookkeeping)
+    TP_SCAT_ENTER,      // entering the SCATTER grid barrier
+    TP_SCAT_BAR,        // SCATTER barrier passed
+    kTracePoints
 };
 
 }  // namespace gde

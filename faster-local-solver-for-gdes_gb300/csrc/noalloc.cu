@@ -16,8 +16,8 @@
 //  * One query, one column: the push engine runs one tile of width 1 (the
 //    batch path of gde_solve, not its served queue), kinds GDE_PPR and
 //    GDE_KATZ, methods GDE_LOCAL_GD and GDE_GLOBAL_GD, FP32 or FP64.
-//  * The graph's workspace must fit the array: about 48 bytes per node in
-//    FP32 (56 in FP64) plus cap / 8 bytes for the long-row chunk list; larger
+//  * The graph's workspace must fit the array: about 44 bytes per node in
+//    FP32 (52 in FP64) plus cap / 8 bytes for the long-row chunk list; larger
 //    graphs are rejected with GDE_EINVAL and a message naming both sizes.
 //  * Every call on a device shares the one array.  Calls whose GPU work
 //    overlaps (other streams, other contexts on the same device, other host
@@ -127,7 +127,7 @@ extern "C" int gde_solve_noalloc(gde_ctx* ctx, gde_graph* G, const gde_params* p
     Carve c;
     const size_t oR = c.take(n * es), oX = c.take(n * es), oP = c.take(n * es);
     const size_t oXC = prec64 ? 0 : c.take(n * 4);
-    const size_t oCand = c.take((size_t)2 * n * 4), oFront = c.take(n * 4), oMark = c.take(n * 4);
+    const size_t oCand = c.take((size_t)2 * n * 4), oMark = c.take(n * 4);
     const size_t oItems = c.take(n * sizeof(PushItem));
     const size_t oLarge = c.take((size_t)a.large_cap * sizeof(PushItem));
     const size_t oTp = c.take(sizeof(TileParams)), oTs = c.take(sizeof(TileState)), oCs = c.take(sizeof(ColState));
@@ -160,7 +160,6 @@ extern "C" int gde_solve_noalloc(gde_ctx* ctx, gde_graph* G, const gde_params* p
     a.XC = prec64 ? nullptr : (float*)(base + oXC);
     a.kahan = prec64 ? 0 : 1;
     a.cand = (int32_t*)(base + oCand);
-    a.front = (int32_t*)(base + oFront);
     a.mark = (int32_t*)(base + oMark);
     a.bsmall = (PushItem*)(base + oItems);
     a.blarge = (PushItem*)(base + oLarge);

@@ -378,6 +378,154 @@ struct PrepSh {
     double acc_col_vol, acc_union_vol;
 };
 
+// Frontier compaction of one node per lane (W = 1): front index, degree
+// bucket, work items and the push row P[fidx].
+template <typename T>
+__device__ __forceinline__ void emit_node_w1(const PushArgs& a, int t, int par, bool node_in, int len, long long rp,
+                                             T push) {
+    const int lane = threadIdx.x & 31;
+    const int64_t n = a.g.n;
+    TileState& ts = a.ts[t];
+    const unsigned bf = __ballot_sync(kFull, node_in);
+    if (bf == 0) return;
+    int bucket = -1, nch = 0;
+    if (node_in) {
+        if (len <= a.small_max) bucket = 0;
+        else if (len <= a.med_max) bucket = 1;
+        else { bucket = 2; nch = (len + a.chunk - 1) / a.chunk; }
+    }
+    const unsigned bs = __ballot_sync(kFull, bucket == 0);
+    const unsigned bm = __ballot_sync(kFull, bucket == 1);
+    int sc = nch;  // inclusive warp scan of chunk counts
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(kFull, sc, o);
+        if (lane >= o) sc += y;
+    }
+    const int wch = __shfl_sync(kFull, sc, 31);
+    int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+    if (lane == 0) {
+        b0 = atomicAdd(&ts.front_cnt[par], __popc(bf));
+        if (bs) b1 = atomicAdd(&ts.small_cnt[par], __popc(bs));
+        if (bm) b2 = atomicAdd(&ts.med_cnt[par], __popc(bm));
+        if (wch) b3 = atomicAdd(&ts.large_cnt[par], wch);
+    }
+    b0 = __shfl_sync(kFull, b0, 0);
+    b1 = __shfl_sync(kFull, b1, 0);
+    b2 = __shfl_sync(kFull, b2, 0);
+    b3 = __shfl_sync(kFull, b3, 0);
+    if (!node_in) return;
+    const unsigned below = (1u << lane) - 1u;
+    const int fidx = b0 + __popc(bf & below);
+    PushItem item;
+    item.rp = rp;
+    item.len = len;
+    item.fidx = fidx;
+    PushItem* bsmall = a.bsmall + (int64_t)t * n;
+    if (bucket == 0) {
+        bsmall[b1 + __popc(bs & below)] = item;
+    } else if (bucket == 1) {
+        bsmall[(n - 1) - (b2 + __popc(bm & below))] = item;
+    } else {
+        PushItem* blarge = a.blarge + (int64_t)t * a.large_cap;
+        const int lb = b3 + (sc - nch);
+        for (int ch = 0; ch < nch; ++ch) {
+            item.rp = rp + (long long)ch * a.chunk;
+            item.len = min(a.chunk, len - ch * a.chunk);
+            blarge[lb + ch] = item;
+        }
+    }
+    reinterpret_cast<T*>(a.P)[(int64_t)t * n + fidx] = push;
+}
+
+// PREP of a W = 1 PPR/Katz local GD tile over candidates [beg, end): the
+// candidates are exactly last round's threshold crossings.  Each lane takes
+// kPrepILP candidates and issues every per-node load (residual, degree,
+// solution, Kahan term, row start and length) before using any of them.
+constexpr int kPrepILP = 2;
+
+template <typename T>
+__device__ void prep_w1_cross(const PushArgs& a, int t, const TileSh& sh, long long beg, long long end,
+                              double& my_oper, int& my_nodes, double& my_vol, int& my_cnt) {
+    const DevGraph& g = a.g;
+    const int64_t n = g.n;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int par = sh.parity;
+    const int32_t* cand = a.cand + ((int64_t)t * 2 + par) * n;
+    T* R = slab_ptr<T>(a.R, a, t);
+    T* X = slab_ptr<T>(a.X, a, t);
+    float* XC = a.kahan ? slab_ptr<float>(a.XC, a, t) : nullptr;
+    const double alpha = sh.tp.alpha;
+    const bool katz = sh.tp.kind == KIND_KATZ;
+    const double theta = sh.col_theta[0];
+    const int64_t ld = a.ld;
+    for (long long base = beg + (long long)warp * 32 * kPrepILP; base < end;
+         base += (long long)kWarps * 32 * kPrepILP) {
+        bool val[kPrepILP];
+        int u[kPrepILP];
+#pragma unroll
+        for (int q = 0; q < kPrepILP; ++q) {
+            const long long i = base + q * 32 + lane;
+            val[q] = i < end;
+            u[q] = val[q] ? cand[i] : 0;
+        }
+        T r[kPrepILP], xv[kPrepILP];
+        float df[kPrepILP], xc[kPrepILP];
+        int len[kPrepILP];
+        long long rp[kPrepILP];
+#pragma unroll
+        for (int q = 0; q < kPrepILP; ++q) {
+            r[q] = T(0); xv[q] = T(0); df[q] = 1.f; xc[q] = 0.f; len[q] = 0; rp[q] = 0;
+            if (val[q]) {
+                const int64_t off = (int64_t)u[q] * ld;
+                r[q] = R[off];
+                xv[q] = X[off];
+                if (XC) xc[q] = XC[off];
+                if (g.rec) {
+                    const NodeRec nr = g.rec[u[q]];
+                    rp[q] = nr.rp;
+                    len[q] = nr.len;
+                    df[q] = nr.degf;
+                } else {
+                    df[q] = g.degf[u[q]];
+                    len[q] = g.row_len[u[q]];
+                    rp[q] = g.row_ptr[u[q]];
+                }
+            }
+        }
+#pragma unroll
+        for (int q = 0; q < kPrepILP; ++q) {
+            bool act = false;
+            T push = T(0);
+            if (val[q]) {
+                const double du = g.degf_exact ? (double)df[q] : g.degd[u[q]];
+                const double rv = (double)r[q];
+                act = fabs(rv) >= theta * du;
+                if (act) {
+                    // ppr_solver.py:276-281 / katz_solver.py:226-231
+                    push = (T)(katz ? alpha * rv : ((1. - alpha) * rv) / du);
+                    const int64_t off = (int64_t)u[q] * ld;
+                    R[off] = T(0);
+                    if (XC) {
+                        // Kahan-compensated FP32 accumulation of the solution
+                        const float y = (float)r[q] - xc[q];
+                        const float s = (float)xv[q] + y;
+                        XC[off] = (s - (float)xv[q]) - y;
+                        X[off] = (T)s;
+                    } else {
+                        X[off] = xv[q] + r[q];
+                    }
+                    my_nodes += 1;
+                    my_oper += du;
+                    my_vol += du;
+                    my_cnt += 1;
+                }
+            }
+            emit_node_w1<T>(a, t, par, act, len[q], rp[q], push);
+        }
+    }
+}
+
 template <typename T, int W>
 __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& ps, long long beg, long long end) {
     constexpr int VEC = (sizeof(T) == 4) ? (W >= 4 ? 4 : W) : (W >= 2 ? 2 : 1);
@@ -397,7 +545,6 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
     const int32_t* cand = a.cand + ((int64_t)t * 2 + par) * n;
     int32_t* next = a.cand + ((int64_t)t * 2 + (par ^ 1)) * n;
     int32_t* mark = a.mark + (int64_t)t * n;
-    int32_t* front = a.front + (int64_t)t * n;
     T* Pw = reinterpret_cast<T*>(a.P) + (int64_t)t * n * W;
     PushItem* bsmall = a.bsmall + (int64_t)t * n;       // short rows grow up from 0,
     PushItem* bmed_end = bsmall + (n - 1);               // medium rows down from n-1
@@ -428,202 +575,210 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
     double my_vol = 0.0;
     int my_cnt = 0;
 
-    for (long long base = beg + (long long)warp * GPW; base < end; base += (long long)kWarps * GPW) {
-        const long long i = base + grp_w;
-        const bool valid = i < end;
-        int u = 0;
-        bool act[VEC];
-        Vec<T, VEC> push;
-#pragma unroll
-        for (int k = 0; k < VEC; ++k) { act[k] = false; push.v[k] = T(0); }
-        double du = 1.0;
-        bool absorb = false;
-        bool any = false;
-        Vec<T, VEC> r;
-        if (valid) {
-            u = sh.dense ? (int)i : cand[i];
-            const int64_t off = (int64_t)u * a.ld + c0;
-            vload<T, VEC>(R + off, r);
-            // fast test first: most scanned nodes are below every threshold
-            du = g.degf_exact ? (double)g.degf[u] : g.degd[u];
-            const double thr_base = (kind == KIND_IGN) ? g.nfac[u] : du;
-#pragma unroll
-            for (int k = 0; k < VEC; ++k) {
-                if (!live[k]) continue;
-                const double rv = (double)r.v[k];
-                bool a_k;
-                if (global) {
-                    a_k = (rv != 0.0);
-                } else {
-                    double thr;
-                    if (hk) thr = ((thr_scale[k] * thr_base) / (double)sh.tp.n_levels) / sh.psi;
-                    else thr = thr_scale[k] * thr_base;
-                    a_k = fabs(rv) >= thr;
-                }
-                act[k] = a_k;
-                any |= a_k;
-            }
-            if (cheby && global) {
-                // global Chebyshev updates every node whose three-term step is non-zero
-                Vec<T, VEC> dxv;
-                vload<T, VEC>(DX + off, dxv);
-#pragma unroll
+    // A W = 1 crossing tile visits exactly the nodes that crossed their
+    // threshold last round: every candidate is active, so all its loads are
+    // issued at once (prep_w1_cross).
+    bool fast = false;
+    if constexpr (W == 1) fast = tile_crosses(sh.tp) && !sh.dense && live[0];
+    if (fast) {
+        if constexpr (W == 1) prep_w1_cross<T>(a, t, sh, beg, end, my_oper[0], my_nodes[0], my_vol, my_cnt);
+    } else {
+        for (long long base = beg + (long long)warp * GPW; base < end; base += (long long)kWarps * GPW) {
+            const long long i = base + grp_w;
+            const bool valid = i < end;
+            int u = 0;
+            bool act[VEC];
+            Vec<T, VEC> push;
+    #pragma unroll
+            for (int k = 0; k < VEC; ++k) { act[k] = false; push.v[k] = T(0); }
+            double du = 1.0;
+            bool absorb = false;
+            bool any = false;
+            Vec<T, VEC> r;
+            if (valid) {
+                u = sh.dense ? (int)i : cand[i];
+                const int64_t off = (int64_t)u * a.ld + c0;
+                vload<T, VEC>(R + off, r);
+                // fast test first: most scanned nodes are below every threshold
+                du = g.degf_exact ? (double)g.degf[u] : g.degd[u];
+                const double thr_base = (kind == KIND_IGN) ? g.nfac[u] : du;
+    #pragma unroll
                 for (int k = 0; k < VEC; ++k) {
                     if (!live[k]) continue;
-                    act[k] = ((double)r.v[k] != 0.0) || ((double)dxv.v[k] != 0.0);
-                    any |= act[k];
-                }
-            }
-            if (any) {
-                du = g.degd[u];
-                absorb = ign && is_absorbing(g, u);
-                Vec<T, VEC> dxv;
-                if (cheby) vload<T, VEC>(DX + off, dxv);
-                Vec<T, VEC> xadd;
-                bool wrote = false;
-#pragma unroll
-                for (int k = 0; k < VEC; ++k) {
-                    xadd.v[k] = T(0);
-                    if (!act[k]) continue;
                     const double rv = (double)r.v[k];
-                    if (cheby) {
-                        // ppr_solver.py:642-646 / katz_solver.py:407-411
-                        double tmp;
-                        if (kind == KIND_KATZ) tmp = sh.coef1 * rv - sh.coef2 * (double)dxv.v[k];
-                        else tmp = sh.coef1 * rv + (sh.coef1 - 1.) * (double)dxv.v[k];
-                        if (global && tmp == 0.0) { act[k] = false; continue; }
-                        T tmpT = (T)tmp;
-                        xadd.v[k] = tmpT;
-                        dxv.v[k] = tmpT;
-                        r.v[k] = (T)(rv - (double)tmpT);  // rt[u] += -delta_xt[u] (:657)
-                        double pv = (kind == KIND_KATZ) ? alpha * (double)tmpT : ((1. - alpha) * (double)tmpT) / du;
-                        push.v[k] = (T)pv;
+                    bool a_k;
+                    if (global) {
+                        a_k = (rv != 0.0);
                     } else {
-                        // An absorbing node (threshold 0) is visited once by the
-                        // reference's initial scan and never re-enqueued; with a
-                        // zero residual it has nothing to absorb.
-                        if (absorb && rv == 0.0) { act[k] = false; continue; }
-                        double pv;
-                        if (kind == KIND_PPR || kind == KIND_UPPR) pv = ((1. - alpha) * rv) / du;
-                        else if (kind == KIND_KATZ) pv = alpha * rv;
-                        else if (kind == KIND_HK) {
-                            if (sh.final_level) pv = rv / du;  // hk_solver.py:254-256
-                            else pv = ((sh.tp.tau / ((double)sh.level + 1.)) * rv) / du;
+                        double thr;
+                        if (hk) thr = ((thr_scale[k] * thr_base) / (double)sh.tp.n_levels) / sh.psi;
+                        else thr = thr_scale[k] * thr_base;
+                        a_k = fabs(rv) >= thr;
+                    }
+                    act[k] = a_k;
+                    any |= a_k;
+                }
+                if (cheby && global) {
+                    // global Chebyshev updates every node whose three-term step is non-zero
+                    Vec<T, VEC> dxv;
+                    vload<T, VEC>(DX + off, dxv);
+    #pragma unroll
+                    for (int k = 0; k < VEC; ++k) {
+                        if (!live[k]) continue;
+                        act[k] = ((double)r.v[k] != 0.0) || ((double)dxv.v[k] != 0.0);
+                        any |= act[k];
+                    }
+                }
+                if (any) {
+                    du = g.degd[u];
+                    absorb = ign && is_absorbing(g, u);
+                    Vec<T, VEC> dxv;
+                    if (cheby) vload<T, VEC>(DX + off, dxv);
+                    Vec<T, VEC> xadd;
+                    bool wrote = false;
+    #pragma unroll
+                    for (int k = 0; k < VEC; ++k) {
+                        xadd.v[k] = T(0);
+                        if (!act[k]) continue;
+                        const double rv = (double)r.v[k];
+                        if (cheby) {
+                            // ppr_solver.py:642-646 / katz_solver.py:407-411
+                            double tmp;
+                            if (kind == KIND_KATZ) tmp = sh.coef1 * rv - sh.coef2 * (double)dxv.v[k];
+                            else tmp = sh.coef1 * rv + (sh.coef1 - 1.) * (double)dxv.v[k];
+                            if (global && tmp == 0.0) { act[k] = false; continue; }
+                            T tmpT = (T)tmp;
+                            xadd.v[k] = tmpT;
+                            dxv.v[k] = tmpT;
+                            r.v[k] = (T)(rv - (double)tmpT);  // rt[u] += -delta_xt[u] (:657)
+                            double pv = (kind == KIND_KATZ) ? alpha * (double)tmpT : ((1. - alpha) * (double)tmpT) / du;
+                            push.v[k] = (T)pv;
                         } else {
-                            pv = ((1. - alpha) * rv) / g.npush[u];  // InstantGNN.py:28
+                            // An absorbing node (threshold 0) is visited once by the
+                            // reference's initial scan and never re-enqueued; with a
+                            // zero residual it has nothing to absorb.
+                            if (absorb && rv == 0.0) { act[k] = false; continue; }
+                            double pv;
+                            if (kind == KIND_PPR || kind == KIND_UPPR) pv = ((1. - alpha) * rv) / du;
+                            else if (kind == KIND_KATZ) pv = alpha * rv;
+                            else if (kind == KIND_HK) {
+                                if (sh.final_level) pv = rv / du;  // hk_solver.py:254-256
+                                else pv = ((sh.tp.tau / ((double)sh.level + 1.)) * rv) / du;
+                            } else {
+                                pv = ((1. - alpha) * rv) / g.npush[u];  // InstantGNN.py:28
+                            }
+                            if (absorb) pv = 0.0;
+                            push.v[k] = (T)pv;
+                            xadd.v[k] = (kind == KIND_IGN && !absorb) ? (T)(sh.tp.x_gain * rv) : r.v[k];
+                            r.v[k] = T(0);
                         }
-                        if (absorb) pv = 0.0;
-                        push.v[k] = (T)pv;
-                        xadd.v[k] = (kind == KIND_IGN && !absorb) ? (T)(sh.tp.x_gain * rv) : r.v[k];
-                        r.v[k] = T(0);
+                        wrote = true;
+                        my_nodes[k] += 1;
+                        if (!absorb) my_oper[k] += du;
                     }
-                    wrote = true;
-                    my_nodes[k] += 1;
-                    if (!absorb) my_oper[k] += du;
-                }
-                if (wrote) {
-                    vstore<T, VEC>(R + off, r);
-                    if (cheby) vstore<T, VEC>(DX + off, dxv);
-                    Vec<T, VEC> xv;
-                    vload<T, VEC>(X + off, xv);
-                    if (absorb) {
-                        // p[u] = r[u]; r[u] = 0 for an absorbing node (InstantGNN.py:22-25)
-#pragma unroll
-                        for (int k = 0; k < VEC; ++k)
-                            if (act[k]) {
-                                xv.v[k] = xadd.v[k];
-                                if (XC) XC[off + k] = 0.f;
-                            }
-                    } else if (XC) {
-                        // Kahan-compensated FP32 accumulation of the solution
-#pragma unroll
-                        for (int k = 0; k < VEC; ++k)
-                            if (act[k]) {
-                                float cc = XC[off + k];
-                                float y = (float)xadd.v[k] - cc;
-                                float s = (float)xv.v[k] + y;
-                                XC[off + k] = (s - (float)xv.v[k]) - y;
-                                xv.v[k] = (T)s;
-                            }
-                    } else {
-#pragma unroll
-                        for (int k = 0; k < VEC; ++k)
-                            if (act[k]) xv.v[k] = xv.v[k] + xadd.v[k];
+                    if (wrote) {
+                        vstore<T, VEC>(R + off, r);
+                        if (cheby) vstore<T, VEC>(DX + off, dxv);
+                        Vec<T, VEC> xv;
+                        vload<T, VEC>(X + off, xv);
+                        if (absorb) {
+                            // p[u] = r[u]; r[u] = 0 for an absorbing node (InstantGNN.py:22-25)
+    #pragma unroll
+                            for (int k = 0; k < VEC; ++k)
+                                if (act[k]) {
+                                    xv.v[k] = xadd.v[k];
+                                    if (XC) XC[off + k] = 0.f;
+                                }
+                        } else if (XC) {
+                            // Kahan-compensated FP32 accumulation of the solution
+    #pragma unroll
+                            for (int k = 0; k < VEC; ++k)
+                                if (act[k]) {
+                                    float cc = XC[off + k];
+                                    float y = (float)xadd.v[k] - cc;
+                                    float s = (float)xv.v[k] + y;
+                                    XC[off + k] = (s - (float)xv.v[k]) - y;
+                                    xv.v[k] = (T)s;
+                                }
+                        } else {
+    #pragma unroll
+                            for (int k = 0; k < VEC; ++k)
+                                if (act[k]) xv.v[k] = xv.v[k] + xadd.v[k];
+                        }
+                        vstore<T, VEC>(X + off, xv);
                     }
-                    vstore<T, VEC>(X + off, xv);
-                }
-                any = false;
-#pragma unroll
-                for (int k = 0; k < VEC; ++k) any |= act[k];
-            }
-        }
-        // ---- node-level frontier decision (OR over the lane group) ----
-        const unsigned bal = __ballot_sync(kFull, any);
-        if (bal == 0) continue;  // warp-uniform: nothing active in this warp
-        const unsigned gmask = ((L == 32) ? kFull : ((1u << L) - 1u)) << (grp_w * L);
-        const bool node_act = valid && (bal & gmask) != 0;
-        const bool leader = (lane_g == 0);
-        // Chebyshev moves r[u] by -dx[u]: u itself is a candidate next round
-        if (cheby && !global) append_once(leader && node_act, u, mark, sh.stamp, next, next_cnt, kFull);
-        const bool node_in = node_act && !absorb;  // absorbed nodes do not push
-        int len = 0;
-        int nch = 0;
-        long long rp = 0;
-        int bucket = -1;  // 0 short, 1 medium, 2 long
-        if (node_in && leader) {
-            len = g.row_len[u];
-            rp = g.row_ptr[u];
-            if (len <= a.small_max) bucket = 0;
-            else if (len <= a.med_max) bucket = 1;
-            else { bucket = 2; nch = (len + a.chunk - 1) / a.chunk; }
-        }
-        const unsigned bf = __ballot_sync(kFull, leader && node_in);
-        if (bf == 0) continue;
-        const unsigned bs = __ballot_sync(kFull, bucket == 0);
-        const unsigned bm = __ballot_sync(kFull, bucket == 1);
-        int lch = (bucket == 2) ? nch : 0;
-        int sc = lch;  // inclusive warp scan of chunk counts
-#pragma unroll
-        for (int o = 1; o < 32; o <<= 1) {
-            int y = __shfl_up_sync(kFull, sc, o);
-            if (lane >= o) sc += y;
-        }
-        const int wch = __shfl_sync(kFull, sc, 31);
-        int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
-        if (lane == 0) {
-            b0 = atomicAdd(&ts.front_cnt[par], __popc(bf));
-            if (bs) b1 = atomicAdd(&ts.small_cnt[par], __popc(bs));
-            if (bm) b2 = atomicAdd(&ts.med_cnt[par], __popc(bm));
-            if (wch) b3 = atomicAdd(&ts.large_cnt[par], wch);
-        }
-        b0 = __shfl_sync(kFull, b0, 0);
-        b1 = __shfl_sync(kFull, b1, 0);
-        b2 = __shfl_sync(kFull, b2, 0);
-        b3 = __shfl_sync(kFull, b3, 0);
-        const unsigned below = (1u << lane) - 1u;
-        int fidx = 0;
-        if (leader && node_in) {
-            fidx = b0 + __popc(bf & below);
-            front[fidx] = u;
-            PushItem item;
-            item.rp = rp;
-            item.len = len;
-            item.fidx = fidx;
-            if (bucket == 0) bsmall[b1 + __popc(bs & below)] = item;
-            else if (bucket == 1) bmed_end[-(b2 + __popc(bm & below))] = item;
-            else {
-                int lb = b3 + (sc - lch);
-                for (int ch = 0; ch < nch; ++ch) {
-                    item.rp = rp + (long long)ch * a.chunk;
-                    item.len = min(a.chunk, len - ch * a.chunk);
-                    blarge[lb + ch] = item;
+                    any = false;
+    #pragma unroll
+                    for (int k = 0; k < VEC; ++k) any |= act[k];
                 }
             }
-            my_vol += du;
-            my_cnt += 1;
+            // ---- node-level frontier decision (OR over the lane group) ----
+            const unsigned bal = __ballot_sync(kFull, any);
+            if (bal == 0) continue;  // warp-uniform: nothing active in this warp
+            const unsigned gmask = ((L == 32) ? kFull : ((1u << L) - 1u)) << (grp_w * L);
+            const bool node_act = valid && (bal & gmask) != 0;
+            const bool leader = (lane_g == 0);
+            // Chebyshev moves r[u] by -dx[u]: u itself is a candidate next round
+            if (cheby && !global) append_once(leader && node_act, u, mark, sh.stamp, next, next_cnt, kFull);
+            const bool node_in = node_act && !absorb;  // absorbed nodes do not push
+            int len = 0;
+            int nch = 0;
+            long long rp = 0;
+            int bucket = -1;  // 0 short, 1 medium, 2 long
+            if (node_in && leader) {
+                len = g.row_len[u];
+                rp = g.row_ptr[u];
+                if (len <= a.small_max) bucket = 0;
+                else if (len <= a.med_max) bucket = 1;
+                else { bucket = 2; nch = (len + a.chunk - 1) / a.chunk; }
+            }
+            const unsigned bf = __ballot_sync(kFull, leader && node_in);
+            if (bf == 0) continue;
+            const unsigned bs = __ballot_sync(kFull, bucket == 0);
+            const unsigned bm = __ballot_sync(kFull, bucket == 1);
+            int lch = (bucket == 2) ? nch : 0;
+            int sc = lch;  // inclusive warp scan of chunk counts
+    #pragma unroll
+            for (int o = 1; o < 32; o <<= 1) {
+                int y = __shfl_up_sync(kFull, sc, o);
+                if (lane >= o) sc += y;
+            }
+            const int wch = __shfl_sync(kFull, sc, 31);
+            int b0 = 0, b1 = 0, b2 = 0, b3 = 0;
+            if (lane == 0) {
+                b0 = atomicAdd(&ts.front_cnt[par], __popc(bf));
+                if (bs) b1 = atomicAdd(&ts.small_cnt[par], __popc(bs));
+                if (bm) b2 = atomicAdd(&ts.med_cnt[par], __popc(bm));
+                if (wch) b3 = atomicAdd(&ts.large_cnt[par], wch);
+            }
+            b0 = __shfl_sync(kFull, b0, 0);
+            b1 = __shfl_sync(kFull, b1, 0);
+            b2 = __shfl_sync(kFull, b2, 0);
+            b3 = __shfl_sync(kFull, b3, 0);
+            const unsigned below = (1u << lane) - 1u;
+            int fidx = 0;
+            if (leader && node_in) {
+                fidx = b0 + __popc(bf & below);
+                PushItem item;
+                item.rp = rp;
+                item.len = len;
+                item.fidx = fidx;
+                if (bucket == 0) bsmall[b1 + __popc(bs & below)] = item;
+                else if (bucket == 1) bmed_end[-(b2 + __popc(bm & below))] = item;
+                else {
+                    int lb = b3 + (sc - lch);
+                    for (int ch = 0; ch < nch; ++ch) {
+                        item.rp = rp + (long long)ch * a.chunk;
+                        item.len = min(a.chunk, len - ch * a.chunk);
+                        blarge[lb + ch] = item;
+                    }
+                }
+                my_vol += du;
+                my_cnt += 1;
+            }
+            fidx = __shfl_sync(kFull, fidx, grp_w * L);
+            if (node_in) vstore<T, VEC>(Pw + (int64_t)fidx * W + c0, push);
         }
-        fidx = __shfl_sync(kFull, fidx, grp_w * L);
-        if (node_in) vstore<T, VEC>(Pw + (int64_t)fidx * W + c0, push);
     }
     // ---- flush per-column counters (one global atomic per column per block) ----
 #pragma unroll
@@ -681,7 +836,6 @@ template <typename T, int W>
 struct ScatterCtx {
     T* tgt;
     const T* Pw;
-    const int32_t* front;
     int32_t* mark;
     int32_t* next;
     int* next_cnt;
@@ -704,7 +858,6 @@ __device__ __forceinline__ ScatterCtx<T, W> scatter_ctx(const PushArgs& a, int t
         c.tgt = slab_ptr<T>(a.R, a, t);
     }
     c.Pw = reinterpret_cast<const T*>(a.P) + (int64_t)t * n * W;
-    c.front = a.front + (int64_t)t * n;
     c.mark = a.mark + (int64_t)t * n;
     c.next = a.cand + ((int64_t)t * 2 + (par ^ 1)) * n;
     c.next_cnt = &a.ts[t].cand_cnt[(level + 1) % 3];
@@ -877,22 +1030,29 @@ __device__ __forceinline__ void append_crossings(const bool (&cr)[kEdgeILP], con
 // (their crossing result is in hub_cr[u]).
 template <typename T>
 __device__ __forceinline__ void edges_w1(const PushArgs& a, const ScatterCtx<T, 1>& c, const bool (&ok)[kEdgeILP],
-                                         const int (&v)[kEdgeILP], const T (&p)[kEdgeILP], double theta,
-                                         const bool (&hub_done)[kEdgeILP], const bool (&hub_cr)[kEdgeILP]) {
+                                         const int (&v)[kEdgeILP], const uint32_t (&dcode)[kEdgeILP],
+                                         const T (&p)[kEdgeILP], double theta, const bool (&hub_done)[kEdgeILP],
+                                         const bool (&hub_cr)[kEdgeILP]) {
     const DevGraph& g = a.g;
     if (c.cross) {
+        bool glob[kEdgeILP];
+#pragma unroll
+        for (int u = 0; u < kEdgeILP; ++u) glob[u] = ok[u] && !hub_done[u];
         float df[kEdgeILP];
         T old[kEdgeILP];
 #pragma unroll
-        for (int u = 0; u < kEdgeILP; ++u) df[u] = (ok[u] && !hub_done[u]) ? g.degf[v[u]] : 1.f;
+        for (int u = 0; u < kEdgeILP; ++u) {
+            df[u] = 1.f;
+            if (glob[u]) df[u] = (dcode[u] != g.deg_esc) ? (float)dcode[u] : g.degf[v[u]];
+        }
 #pragma unroll
         for (int u = 0; u < kEdgeILP; ++u)
-            old[u] = (ok[u] && !hub_done[u]) ? atomicAdd(c.tgt + (int64_t)v[u] * a.ld, p[u]) : T(0);
+            old[u] = glob[u] ? atomicAdd(c.tgt + (int64_t)v[u] * a.ld, p[u]) : T(0);
         bool cr[kEdgeILP];
 #pragma unroll
         for (int u = 0; u < kEdgeILP; ++u) {
             cr[u] = hub_cr[u];
-            if (ok[u] && !hub_done[u]) {
+            if (glob[u]) {
                 const double dv = g.degf_exact ? (double)df[u] : g.degd[v[u]];
                 const double thr = theta * dv;
                 const T s = old[u] + p[u];  // the value the atomic stored
@@ -912,6 +1072,18 @@ __device__ __forceinline__ void edges_w1(const PushArgs& a, const ScatterCtx<T, 
 #pragma unroll
             for (int u = 0; u < kEdgeILP; ++u) append_once(ok[u], v[u], c.mark, c.stamp, c.next, c.next_cnt, kFull);
         }
+    }
+}
+
+// Target id and degree code of edge position j (code == deg_esc: read degf).
+__device__ __forceinline__ void load_edge(const DevGraph& g, long long j, int& v, uint32_t& dcode) {
+    if (g.col_deg) {
+        const uint32_t w = g.col_deg[j];
+        v = (int)(w & ((1u << g.idx_bits) - 1u));
+        dcode = w >> g.idx_bits;
+    } else {
+        v = g.col[j];
+        dcode = g.deg_esc;
     }
 }
 
@@ -935,13 +1107,16 @@ __device__ void scatter_warp_items_w1(const PushArgs& a, const PushItem* items, 
         for (int j0 = 0; j0 < it.len; j0 += 32 * kEdgeILP) {
             bool ok[kEdgeILP];
             int v[kEdgeILP];
+            uint32_t dc[kEdgeILP];
 #pragma unroll
             for (int u = 0; u < kEdgeILP; ++u) {
                 const int j = j0 + u * 32 + lane;
                 ok[u] = j < it.len;
-                v[u] = ok[u] ? a.g.col[it.rp + j] : 0;
+                v[u] = 0;
+                dc[u] = 0;
+                if (ok[u]) load_edge(a.g, it.rp + j, v[u], dc[u]);
             }
-            edges_w1<T>(a, c, ok, v, p, theta, none, none);
+            edges_w1<T>(a, c, ok, v, dc, p, theta, none, none);
         }
     }
 }
@@ -978,10 +1153,13 @@ __device__ void scatter_small_w1(const PushArgs& a, int t, const ScatterCtx<T, 1
         for (int j0 = 0; j0 < maxlen; j0 += kEdgeILP) {
             bool ok[kEdgeILP], hub_done[kEdgeILP], hub_cr[kEdgeILP];
             int v[kEdgeILP];
+            uint32_t dc[kEdgeILP];
 #pragma unroll
             for (int u = 0; u < kEdgeILP; ++u) {
                 ok[u] = j0 + u < len;
-                v[u] = ok[u] ? g.col[rp + j0 + u] : 0;
+                v[u] = 0;
+                dc[u] = 0;
+                if (ok[u]) load_edge(g, rp + j0 + u, v[u], dc[u]);
                 hub_done[u] = false;
                 hub_cr[u] = false;
             }
@@ -1002,7 +1180,8 @@ __device__ void scatter_small_w1(const PushArgs& a, int t, const ScatterCtx<T, 1
                         if (c.cross) {
                             const T old = atomicAdd(addr, tot);
                             const T s = old + tot;
-                            const double dv = g.degf_exact ? (double)g.degf[v[u]] : g.degd[v[u]];
+                            const double dv = (dc[u] != g.deg_esc) ? (double)dc[u]
+                                              : (g.degf_exact ? (double)g.degf[v[u]] : g.degd[v[u]]);
                             const double thr = theta * dv;
                             hub_cr[u] = ((double)old < thr) && ((double)s >= thr);
                         } else {
@@ -1015,7 +1194,7 @@ __device__ void scatter_small_w1(const PushArgs& a, int t, const ScatterCtx<T, 1
                     hub_done[u] = hub;
                 }
             }
-            edges_w1<T>(a, c, ok, v, p, theta, hub_done, hub_cr);
+            edges_w1<T>(a, c, ok, v, dc, p, theta, hub_done, hub_cr);
         }
     }
 }
@@ -1215,6 +1394,12 @@ __device__ void retire_range(const PushArgs& a, int t, long long beg, long long 
     }
 }
 
+// Opt-in per-block phase timeline (thread 0, first trace_iters iterations).
+__device__ __forceinline__ void trace_point(const PushArgs& a, int it, int k) {
+    if (a.trace && it < a.trace_iters && threadIdx.x == 0)
+        a.trace[((size_t)it * gridDim.x + blockIdx.x) * kTracePoints + k] = globaltimer_ns();
+}
+
 template <typename T, int W>
 __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
     __shared__ TileSh sh;
@@ -1230,6 +1415,7 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
     }
     int it = 0;
     for (; it < a.round_budget; ++it) {
+        trace_point(a, it, TP_ITER);
         // ---- live tiles of this round (identical in every block) ----
         if (threadIdx.x == 0) { rs.any_check = 0; rs.any_idle = 0; }
         __syncthreads();
@@ -1283,6 +1469,7 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
         }
         __syncthreads();
         block_exclusive_scan(s_vals, ntl, rs.off[0], rs.scan_tmp);
+        trace_point(a, it, TP_PREP_WORK);
         {
             long long lo, hi;
             block_share(rs.off[0][ntl], lo, hi);
@@ -1296,7 +1483,9 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
                 }
             }
         }
+        trace_point(a, it, TP_PREP_DONE);
         if (!grid_barrier(a.bar, a.err)) return;
+        trace_point(a, it, TP_PREP_BAR);
         if (timer) {
             unsigned long long t1 = globaltimer_ns();
             a.stats->prep_ns += t1 - t0;
@@ -1360,6 +1549,7 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
                 }
             }
         }
+        trace_point(a, it, TP_SCAT_WORK);
         // long-row chunks first (largest pieces), then medium, then short rows
         for (int sp = 2; sp >= 0; --sp) {
             const long long* off = rs.off[sp];
@@ -1383,6 +1573,7 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
                 }
             }
         }
+        trace_point(a, it, TP_SCAT_DONE);
         // HK level drop (touches the current level's slab only)
         for (int k = 0; k < ntl; ++k) {
             if (!(rs.flags[k] & SF_HK)) continue;
@@ -1406,7 +1597,9 @@ __global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
                 finish_round<W>(a, t, lv, dnext);
             }
         }
+        trace_point(a, it, TP_SCAT_ENTER);
         if (!grid_barrier(a.bar, a.err)) return;
+        trace_point(a, it, TP_SCAT_BAR);
         if (timer) a.stats->scatter_ns += globaltimer_ns() - t0;
     }
     // A tile still SLOT_LIVE after the launch stopped at max_rounds (the host

@@ -195,6 +195,25 @@ def ctx_stream(ctx: Context | None = None) -> int:
     return int(L.load().gde_ctx_stream(c.ptr) or 0)
 
 
+def trace(iters: int, ctx: Context | None = None) -> None:
+    """Record per-block phase stamps for the first ``iters`` iterations of later push launches (0 = off)."""
+    c = ctx or Context.get(0)
+    L.check(c.ptr, L.load().gde_ctx_trace(c.ptr, int(iters)), "gde_ctx_trace")
+
+
+def trace_read(ctx: Context | None = None) -> np.ndarray:
+    """Stamps (ns) of the last push launch as [iters, grid, points]; 0 = point not reached."""
+    c = ctx or Context.get(0)
+    lib = L.load()
+    it, gr, pt = ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+    L.check(c.ptr, lib.gde_ctx_trace_read(c.ptr, None, 0, ctypes.byref(it), ctypes.byref(gr), ctypes.byref(pt)),
+            "gde_ctx_trace_read")
+    out = np.zeros((it.value, gr.value, pt.value), dtype=np.uint64)
+    if out.size:
+        L.check(c.ptr, lib.gde_ctx_trace_read(c.ptr, _ptr(out), out.size, None, None, None), "gde_ctx_trace_read")
+    return out
+
+
 def feature_push(graph: Graph, kind: int, P, R, eps: float, *, alpha: float, beta: float = 0.0, prec: str = "fp64",
                  cand=None, tile_w: int = 0, max_rounds: int = 0, tuning: dict | None = None) -> dict:
     """Multi-column push on device matrices P, R ([n, F] torch tensors), in place."""

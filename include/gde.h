@@ -101,6 +101,19 @@ int gde_ctx_destroy(gde_ctx *ctx);
 const char *gde_last_error(gde_ctx *ctx);
 int gde_ctx_sync(gde_ctx *ctx);
 
+/* ---- push-kernel phase trace (diagnostics; no counterpart in the reference) ----
+ * gde_ctx_trace(ctx, iters) turns tracing on for the first `iters` launch
+ * iterations of every later push launch on this context (0 turns it off).
+ * Each block's thread 0 then records %globaltimer (ns) at 8 phase
+ * boundaries per iteration: iteration start, PREP work start, PREP work
+ * done, PREP barrier passed, SCATTER work start, SCATTER work done,
+ * SCATTER barrier entered, SCATTER barrier passed.  gde_ctx_trace_read
+ * copies the last launch's stamps to host `out` as
+ * out[(iter * grid + block) * points + point] (0 = not reached) and returns
+ * the shape; call it with out == NULL to get the shape only. */
+int gde_ctx_trace(gde_ctx *ctx, int iters);
+int gde_ctx_trace_read(gde_ctx *ctx, uint64_t *out, int64_t cap, int *iters, int *grid, int *points);
+
 /* ---- graph ----
  * Uploads a CSR graph.  Row u's neighbours are indices[indptr[u] ..
  * indptr[u]+row_len[u]); row_len == NULL means indptr[u+1]-indptr[u] (the
@@ -197,7 +210,7 @@ int gde_plain_ppr_local(gde_ctx *ctx, gde_graph *g, int32_t seed, double alpha, 
  * memory limit).  One PPR or Katz query (p->kind GDE_PPR / GDE_KATZ, p->method
  * GDE_LOCAL_GD / GDE_GLOBAL_GD, p->prec FP32 / FP64; same results as gde_solve
  * for that query) whose workspace is a fixed 64 MiB device array inside the
- * library: about 48 bytes per node in FP32 (56 in FP64) plus cap / 8 bytes;
+ * library: about 44 bytes per node in FP32 (52 in FP64) plus cap / 8 bytes;
  * larger graphs are rejected with GDE_EINVAL.  Calls no cudaMalloc, cudaFree
  * or other allocating routine.  Every call on a device shares the array, so
  * calls whose GPU work overlaps race: serialise them.  The first call on a

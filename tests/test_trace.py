@@ -1,0 +1,45 @@
+"""The opt-in push-kernel phase trace (gde_ctx_trace / gde_ctx_trace_read).
+
+Checks the shape and ordering of the stamps and that the grid barrier is a
+barrier in the timeline: no block leaves a phase barrier before the last
+block has entered it.  Tracing must not change results.
+"""
+import numpy as np
+import pytest
+
+from gde import _lib as L
+from gde import api, graphs
+
+pytestmark = pytest.mark.gpu
+
+TICK_NS = 2_000  # slack for %globaltimer granularity across SMs
+
+
+def test_trace_timeline_is_ordered_and_barriers_hold():
+    g = graphs.chung_lu(3000, 2.1, 8.0, 300.0, seed=3)
+    Gd = api.Graph(g.indptr, g.indices)
+    seeds = graphs.uniform_seeds(g, 8, seed=5)
+    ref = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, 1e-6, prec="fp64", alpha=0.1)
+    api.trace(6)
+    try:
+        res = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, 1e-6, prec="fp64", alpha=0.1)
+        tr = api.trace_read()
+    finally:
+        api.trace(0)
+    np.testing.assert_array_equal(res["oper"], ref["oper"])
+    np.testing.assert_allclose(res["x"], ref["x"], rtol=0, atol=1e-14)
+    iters, grid, points = tr.shape
+    assert iters == 6 and points == 8 and grid > 0
+    ran = tr[:, :, 0] != 0
+    assert ran.all(), "every block stamps every traced iteration of a 6+ round solve"
+    t = tr.astype(np.int64)
+    # within a block and iteration the phase stamps never go back
+    assert (np.diff(t, axis=2) >= 0).all()
+    # iterations follow one another
+    assert (t[1:, :, 0] >= t[:-1, :, 7]).all()
+    # barriers: every block leaves after the last block entered
+    for enter, leave in ((2, 3), (6, 7)):
+        last_in = t[:, :, enter].max(axis=1)
+        first_out = t[:, :, leave].min(axis=1)
+        assert (first_out + TICK_NS >= last_in).all()
+    assert api.trace_read().size == 0
