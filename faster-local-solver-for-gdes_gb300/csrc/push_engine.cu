@@ -29,6 +29,16 @@ namespace gde {
 
 namespace {
 
+// Resident blocks per SM requested from the compiler (bounds registers) and
+// independent edges in flight per lane in the W = 1 scatter; both can be
+// overridden at build time for tuning.
+#ifndef GDE_MIN_BLOCKS
+#define GDE_MIN_BLOCKS 3
+#endif
+#ifndef GDE_EDGE_ILP
+#define GDE_EDGE_ILP 4
+#endif
+
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr unsigned kFull = 0xffffffffu;
@@ -69,6 +79,21 @@ __device__ bool grid_barrier(GridBarrier* bar, int* err) {
     }
     __syncthreads();
     return s_ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Threshold test r >= theta * d without FP64 arithmetic in the common case.
+// GB300 issues FP64 at a small fraction of the FP32 rate, so the FP32 path
+// decides in FP32 whenever r is clearly on one side: t32 = fl32(fl32(theta) *
+// d) is within 2^-23 (relative) of theta * d for an integer degree d < 2^24,
+// so r >= t32 * (1 + 2^-20) implies r > theta * d and r < t32 * (1 - 2^-20)
+// implies r < theta * d.  Only inside that band is the FP64 product formed.
+// The result is exactly that of (double)r >= theta * d.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ bool ge_threshold(float r, float t32, double theta, double d) {
+    if (r >= t32 * (1.f + 0x1p-20f)) return true;
+    if (r < t32 * (1.f - 0x1p-20f)) return false;
+    return (double)r >= theta * d;
 }
 
 // ---------------------------------------------------------------------------
@@ -458,7 +483,10 @@ __device__ void prep_w1_cross(const PushArgs& a, int t, const TileSh& sh, long l
     const double alpha = sh.tp.alpha;
     const bool katz = sh.tp.kind == KIND_KATZ;
     const double theta = sh.col_theta[0];
+    const float theta_f = (float)theta;
+    const float alpha_f = (float)alpha, omalpha_f = (float)(1. - alpha);
     const int64_t ld = a.ld;
+    long long ideg = 0;  // sum of (integer) degrees of the pushed nodes
     for (long long base = beg + (long long)warp * 32 * kPrepILP; base < end;
          base += (long long)kWarps * 32 * kPrepILP) {
         bool val[kPrepILP];
@@ -499,11 +527,18 @@ __device__ void prep_w1_cross(const PushArgs& a, int t, const TileSh& sh, long l
             T push = T(0);
             if (val[q]) {
                 const double du = g.degf_exact ? (double)df[q] : g.degd[u[q]];
-                const double rv = (double)r[q];
-                act = fabs(rv) >= theta * du;
-                if (act) {
+                if constexpr (sizeof(T) == 4) {
+                    // FP32 tile: exact threshold test mostly in FP32; push value in FP32
+                    if (g.degf_exact) act = ge_threshold(fabsf(r[q]), theta_f * df[q], theta, du);
+                    else act = fabs((double)r[q]) >= theta * du;
+                    if (act) push = katz ? alpha_f * r[q] : (omalpha_f * r[q]) / df[q];
+                } else {
+                    const double rv = (double)r[q];
+                    act = fabs(rv) >= theta * du;
                     // ppr_solver.py:276-281 / katz_solver.py:226-231
-                    push = (T)(katz ? alpha * rv : ((1. - alpha) * rv) / du);
+                    if (act) push = (T)(katz ? alpha * rv : ((1. - alpha) * rv) / du);
+                }
+                if (act) {
                     const int64_t off = (int64_t)u[q] * ld;
                     R[off] = T(0);
                     if (XC) {
@@ -516,14 +551,16 @@ __device__ void prep_w1_cross(const PushArgs& a, int t, const TileSh& sh, long l
                         X[off] = xv[q] + r[q];
                     }
                     my_nodes += 1;
-                    my_oper += du;
-                    my_vol += du;
+                    if (g.degf_exact) ideg += (long long)df[q];
+                    else { my_oper += du; my_vol += du; }
                     my_cnt += 1;
                 }
             }
             emit_node_w1<T>(a, t, par, act, len[q], rp[q], push);
         }
     }
+    my_oper += (double)ideg;
+    my_vol += (double)ideg;
 }
 
 template <typename T, int W>
@@ -997,7 +1034,7 @@ __device__ void scatter_warp_items(const PushArgs& a, const PushItem* items, int
 // residual atomics, then threshold tests -- instead of one dependent chain
 // per edge: the kernel is bound by memory latency, not bandwidth.
 // ---------------------------------------------------------------------------
-constexpr int kEdgeILP = 4;
+constexpr int kEdgeILP = GDE_EDGE_ILP;
 
 // Warp-aggregated append of up to kEdgeILP crossing targets per lane (one
 // global atomic per warp).  On a W = 1 crossing tile every node crosses its
@@ -1035,6 +1072,7 @@ __device__ __forceinline__ void edges_w1(const PushArgs& a, const ScatterCtx<T, 
                                          const bool (&hub_cr)[kEdgeILP]) {
     const DevGraph& g = a.g;
     if (c.cross) {
+        const float theta_f = (float)theta;
         bool glob[kEdgeILP];
 #pragma unroll
         for (int u = 0; u < kEdgeILP; ++u) glob[u] = ok[u] && !hub_done[u];
@@ -1053,9 +1091,17 @@ __device__ __forceinline__ void edges_w1(const PushArgs& a, const ScatterCtx<T, 
         for (int u = 0; u < kEdgeILP; ++u) {
             cr[u] = hub_cr[u];
             if (glob[u]) {
+                const T s = old[u] + p[u];  // the value the atomic stored
+                if constexpr (sizeof(T) == 4) {
+                    if (g.degf_exact) {
+                        const float t32 = theta_f * df[u];
+                        cr[u] = !ge_threshold(old[u], t32, theta, (double)df[u]) &&
+                                ge_threshold(s, t32, theta, (double)df[u]);
+                        continue;
+                    }
+                }
                 const double dv = g.degf_exact ? (double)df[u] : g.degd[v[u]];
                 const double thr = theta * dv;
-                const T s = old[u] + p[u];  // the value the atomic stored
                 cr[u] = ((double)old[u] < thr) && ((double)s >= thr);
             }
         }
@@ -1182,8 +1228,17 @@ __device__ void scatter_small_w1(const PushArgs& a, int t, const ScatterCtx<T, 1
                             const T s = old + tot;
                             const double dv = (dc[u] != g.deg_esc) ? (double)dc[u]
                                               : (g.degf_exact ? (double)g.degf[v[u]] : g.degd[v[u]]);
-                            const double thr = theta * dv;
-                            hub_cr[u] = ((double)old < thr) && ((double)s >= thr);
+                            if constexpr (sizeof(T) == 4) {
+                                if (g.degf_exact) {
+                                    const float t32 = (float)theta * (float)dv;
+                                    hub_cr[u] = !ge_threshold(old, t32, theta, dv) && ge_threshold(s, t32, theta, dv);
+                                } else {
+                                    hub_cr[u] = ((double)old < theta * dv) && ((double)s >= theta * dv);
+                                }
+                            } else {
+                                const double thr = theta * dv;
+                                hub_cr[u] = ((double)old < thr) && ((double)s >= thr);
+                            }
                         } else {
                             atomicAdd(addr, tot);
                         }
@@ -1401,7 +1456,7 @@ __device__ __forceinline__ void trace_point(const PushArgs& a, int it, int k) {
 }
 
 template <typename T, int W>
-__global__ void __launch_bounds__(kThreads, 3) push_kernel(PushArgs a) {
+__global__ void __launch_bounds__(kThreads, GDE_MIN_BLOCKS) push_kernel(PushArgs a) {
     __shared__ TileSh sh;
     __shared__ PrepSh ps;
     __shared__ RoundSh rs;

@@ -45,7 +45,8 @@ def _digest(extra_flags: list[str]) -> str:
 
 
 def build(force: bool = False, verbose: bool = False, extra_flags: list[str] | None = None) -> str:
-    extra_flags = list(extra_flags or [])
+    # GDE_NVCC_EXTRA: extra nvcc flags (e.g. tuning macros) for experiments
+    extra_flags = list(extra_flags or []) + os.environ.get("GDE_NVCC_EXTRA", "").split()
     os.makedirs(BUILD, exist_ok=True)
     stamp = os.path.join(BUILD, "libgde.stamp")
     dig = _digest(extra_flags)

@@ -16,8 +16,20 @@ from oracle import oracle as O
 pytestmark = pytest.mark.gpu
 
 FP64_L1 = 1e-12      # relative l1 of FP64 solutions vs the oracle
-FP32_L1 = 2e-6       # relative l1 of FP32 solutions vs the FP64 oracle
+FP32_L1 = 2e-6       # mean relative l1 of FP32 solutions vs the FP64 oracle
 OPER_RTOL = 1e-12
+
+
+def fp32_flip_bound(g, eps, alpha):
+    """Largest relative l1 an FP32 solve may show against the FP64 oracle.
+
+    FP32 residual rounding can move a node whose FP64 residual lies within
+    rounding of its threshold eps*alpha*d_u to the other side; the node then
+    pushes a round earlier or later (or, at the end, not at all), which moves
+    about 2*eps*alpha*d_u of mass in l1 (sum(x) ~ 1).  Allow a few such flips
+    at the largest degree on top of the rounding error itself.
+    """
+    return FP32_L1 + 3 * 2 * eps * alpha * float(g.degree.max())
 
 
 @pytest.fixture(scope="module")
@@ -61,11 +73,14 @@ def test_ppr_gd_fp32_within_tolerance(cl, W):
     eps = 1e-6
     res = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, eps, prec="fp32", alpha=0.1, tile_w=W)
     assert res["x"].dtype == np.float32
+    errs = []
     for i, s in enumerate(seeds):
         xo, _, oo = O.ppr_gd(g.n, g.indptr, g.indices, deg, int(s), 0.1, eps, True)
-        assert rel_l1(res["x"][i], xo) < FP32_L1
+        errs.append(rel_l1(res["x"][i], xo))
+        assert errs[-1] < fp32_flip_bound(g, eps, 0.1), (i, errs[-1])
         # FP32 residuals can flip a threshold tie: opers agree to a few edges
         assert abs(res["oper"][i] - oo) <= 1e-3 * oo
+    assert np.mean(errs) < FP32_L1, errs
 
 
 def test_ppr_gd_against_reference_golden(golden_graphs):

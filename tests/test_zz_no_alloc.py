@@ -19,7 +19,7 @@ from gde import api, graphs
 pytestmark = pytest.mark.gpu
 
 FP64_L1 = 1e-12      # relative l1 of FP64 solutions (same bar as the parity tests)
-FP32_L1 = 2e-6       # relative l1 between FP32 solutions
+FP32_L1 = 2e-6       # relative l1 between FP32 solutions, plus a few threshold flips (below)
 OPER_RTOL = 1e-12
 
 
@@ -80,13 +80,18 @@ def test_noalloc_matches_gde_solve_twice(cl, name, kind, method, alpha, eps, pre
             assert rel_l1(x, xe) < FP64_L1, (name, call)
             assert np.abs(r - re_).sum() < 1e-12 * max(np.abs(re_).sum(), 1.0), (name, call)
         else:
-            assert rel_l1(x, xe) < FP32_L1, (name, call, rel_l1(x, xe))
+            # two FP32 runs add residuals in different orders, so a node within
+            # rounding of its threshold may push a round apart in the two: each
+            # such flip moves about 2*theta*d_u of mass (sum(x) ~ 1)
+            theta = eps * (alpha if kind == L.PPR else 1.0)
+            flips = 3 * 2 * theta * float(g.degree.max())
+            assert rel_l1(x, xe) < FP32_L1 + flips, (name, call, rel_l1(x, xe))
             # FP32 residuals can flip a threshold tie: opers agree to a few edges
             assert abs(o - oe) <= 1e-3 * oe, (name, call, o, oe)
 
 
 def test_noalloc_rejects_graph_above_the_fixed_scratch():
-    n = 2_000_000                    # ~96 MB of FP32 workspace > the 64 MiB array
+    n = 2_000_000                    # ~90 MB of FP32 workspace > the 64 MiB array
     u = np.arange(n - 1, dtype=np.int64)
     g, _ = graphs._csr_from_undirected(n, u, u + 1, drop_isolated=False)   # a path
     Gd = api.Graph(g.indptr, g.indices)
