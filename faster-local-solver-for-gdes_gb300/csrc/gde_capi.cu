@@ -459,7 +459,13 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     if (d_arr) CK(cudaMemcpyAsync(d_arr, qarr.data(), nq * 8, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemsetAsync(d_start, 0, nq * 8, ctx->stream));
     CK(cudaMemsetAsync(d_finish, 0, nq * 8, ctx->stream));
-    const int first = S;
+    // the leading queries that have arrived at launch start go straight into
+    // slots; the other slots start idle and admit queries as they arrive
+    int first = S;
+    if (arrival_ms) {
+        first = 0;
+        while (first < S && qarr[first] <= 0) first++;
+    }
     CK(cudaMemcpyAsync(d_next, &first, 4, cudaMemcpyHostToDevice, ctx->stream));
     // ---- outputs: the caller's device rows, or staging rows copied back ----
     const size_t oes = out64 ? 8 : 4;
@@ -472,7 +478,7 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     std::vector<TileParams> tp(S);
     std::vector<TileState> ts(S);
     std::vector<ColState> cs(S);
-    std::vector<InitCol> ic(S);
+    std::vector<InitCol> ic(first);
     for (int t = 0; t < S; t++) {
         TileParams& P = tp[t];
         memset(&P, 0, sizeof(P));
@@ -484,11 +490,17 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
         TileState& T = ts[t];
         memset(&T, 0, sizeof(T));
         T.t0 = 0;
-        T.done = SLOT_LIVE;
         T.stamp = ctx->stamp[t];
-        T.qid = t;
         ColState& C = cs[t];
         memset(&C, 0, sizeof(C));
+        if (t >= first) {
+            T.done = SLOT_IDLE;
+            T.qid = -1;
+            C.seed = -1;
+            continue;
+        }
+        T.done = SLOT_LIVE;
+        T.qid = t;
         C.live = 1;
         C.seed = qs[t];
         C.theta = qt[t];
@@ -502,10 +514,12 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     CK(cudaMemcpyAsync(a.tp, tp.data(), S * sizeof(TileParams), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(a.ts, ts.data(), S * sizeof(TileState), cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(a.cs, cs.data(), S * sizeof(ColState), cudaMemcpyHostToDevice, ctx->stream));
-    InitCol* d_ic = (InitCol*)dev("initcols", S * sizeof(InitCol));
+    InitCol* d_ic = (InitCol*)dev("initcols", std::max(first, 1) * sizeof(InitCol));
     if (!d_ic) return fail(ctx, GDE_ENOMEM, "column tables");
-    CK(cudaMemcpyAsync(d_ic, ic.data(), S * sizeof(InitCol), cudaMemcpyHostToDevice, ctx->stream));
-    CK(init_columns(a, prec64, 1, d_ic, S, ctx->stream));
+    if (first > 0) {
+        CK(cudaMemcpyAsync(d_ic, ic.data(), first * sizeof(InitCol), cudaMemcpyHostToDevice, ctx->stream));
+        CK(init_columns(a, prec64, 1, d_ic, first, ctx->stream));
+    }
     a.serve = 1;
     a.round_budget = 0x3fffffff;
     ServeQueue& Q = a.queue;
@@ -692,6 +706,8 @@ int gde_serve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
         if (seeds[q] < 0 || seeds[q] >= n) return fail(ctx, GDE_EINVAL, "seed out of range");
         if (!(eps[q] > 0.0)) return fail(ctx, GDE_EINVAL, "eps must be > 0");
         if (arrival_ms && !(arrival_ms[q] >= 0.0)) return fail(ctx, GDE_EINVAL, "arrival times must be >= 0");
+        if (arrival_ms && q > 0 && arrival_ms[q] < arrival_ms[q - 1])
+            return fail(ctx, GDE_EINVAL, "arrival times must be non-decreasing (queries are admitted in order)");
         if (p->kind == KIND_PPR && !(eps[q] * G->h_deg[G->node_in(seeds[q])] <= 1.))
             return fail(ctx, GDE_EINVAL, "eps * degree[s_node] > 1 (ppr_solver.py:213)");
     }

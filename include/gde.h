@@ -156,9 +156,10 @@ void *gde_ctx_stream(gde_ctx *ctx);
 /* ---- served queries (continuous batching) ----
  * PPR / Katz local GD queries served by p->slots concurrent slots inside one
  * persistent launch: a finished query's row is written and its slot handed
- * to the next query on the device.  arrival_ms (host, may be NULL): query q
- * is admitted no earlier than arrival_ms[q] after the launch starts, and its
- * latency (lat_ms_out) is measured from that arrival.  gde_solve uses this
+ * to the next query on the device.  arrival_ms (host, may be NULL;
+ * non-decreasing, queries are admitted in index order): query q is admitted
+ * no earlier than arrival_ms[q] after the launch starts, and its latency
+ * (lat_ms_out) is measured from that arrival.  gde_solve uses this
  * path for PPR / Katz local GD with tile_w <= 1.  Replaces a loop of
  * ppr_gd_local_gpu / katz_gd_local_gpu calls (ppr_solver.py:82-146,
  * katz_solver.py:81-146) with a request stream. */
