@@ -59,6 +59,7 @@ __global__ void extract_kernel(PushArgs a, const ExtractCol* cols, O* x_out, O* 
     T* X = reinterpret_cast<T*>(a.X) + base;
     T* R = reinterpret_cast<T*>(a.R) + base;
     T* R2 = a.R2 ? reinterpret_cast<T*>(a.R2) + base : nullptr;
+    float* XC = a.XC ? a.XC + base : nullptr;  // Kahan compensation: the sum is X - XC
     const int rl = ec.r_levels;
     const int32_t* perm = a.g.perm;
     // u runs over caller ids; the slabs are in internal (relabelled) order
@@ -66,6 +67,7 @@ __global__ void extract_kernel(PushArgs a, const ExtractCol* cols, O* x_out, O* 
         const int64_t o = (perm ? (int64_t)perm[u] : u) * a.ld;
         if (x_out) {
             double x = (double)X[o];
+            if (XC) x -= (double)XC[o];
             if (u == ec.seed) x = x + ec.seed_add;
             if (ec.scale != 1.0) x = x / ec.scale;
             x_out[ec.out_row * ld_out + u] = (O)x;
@@ -78,6 +80,7 @@ __global__ void extract_kernel(PushArgs a, const ExtractCol* cols, O* x_out, O* 
             X[o] = T(0);
             R[o] = T(0);
             if (R2) R2[o] = T(0);
+            if (XC) XC[o] = 0.f;
         }
     }
 }

@@ -1434,6 +1434,7 @@ __device__ void retire_range(const PushArgs& a, int t, long long beg, long long 
     for (long long u = beg + threadIdx.x; u < end; u += kThreads) {
         const int64_t v = (perm ? (int64_t)perm[u] : u) * a.ld;
         double x = (double)X[v];
+        if (XC) x -= (double)XC[v];  // Kahan: the sum is X - XC
         if (u == sc) x = x + q.seed_add;
         if (q.x_out) {
             if (q.out64) reinterpret_cast<double*>(q.x_out)[(int64_t)qid * q.ld_out + u] = x;

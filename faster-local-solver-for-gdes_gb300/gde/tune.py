@@ -1,0 +1,91 @@
+"""Autotuner for batched solves: tile width, serving slots and degree buckets.
+
+Times ``api.solve`` on a sample of the caller's queries for each candidate
+configuration (device time of the call, best of ``reps``) and keeps the
+fastest.  The search is two-stage: first the execution shape (served slots
+for single-column tiles, or node x column tiles of width 4..32), then the
+degree-bucket thresholds (rows per lane / per warp, long-row chunk) for the
+winning shape.  Results are cached per graph, kind, precision and sample
+size in a JSON file next to the graph cache, so a workload is tuned once.
+"""
+from __future__ import annotations
+
+import hashlib
+import json
+import os
+
+import numpy as np
+
+from gde import _lib as L
+from gde import api
+
+SHAPES = [
+    {"tile_w": 1, "slots": 32},
+    {"tile_w": 1, "slots": 64},
+    {"tile_w": 4},
+    {"tile_w": 8},
+    {"tile_w": 16},
+    {"tile_w": 32},
+]
+BUCKETS = [
+    {},
+    {"small_max": 16},
+    {"small_max": 4},
+    {"med_max": 1024, "chunk": 1024},
+    {"med_max": 128, "chunk": 128},
+]
+
+
+def _cache_path(graph: api.Graph, key: str) -> str:
+    d = os.environ.get("GDE_GRAPH_CACHE") or os.path.join(
+        os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)))), ".graph_cache")
+    os.makedirs(os.path.join(d, "tune"), exist_ok=True)
+    return os.path.join(d, "tune", key + ".json")
+
+
+def _graph_key(graph: api.Graph, kind: int, prec: str, n_sample: int) -> str:
+    h = hashlib.sha1(f"{graph.n}:{graph.cap}:{graph.vol}:{kind}:{prec}:{n_sample}".encode()).hexdigest()[:16]
+    return f"g{graph.n}_{h}"
+
+
+def _time(graph, kind, seeds, eps, prec, alpha, cfg, reps) -> float:
+    tuning = {k: v for k, v in cfg.items() if k != "tile_w"}
+    best = float("inf")
+    for _ in range(reps):
+        r = api.solve(graph, kind, L.LOCAL_GD, seeds, eps, prec=prec, alpha=alpha, tile_w=cfg["tile_w"],
+                      want_x=False, want_r=False, tuning=tuning)
+        best = min(best, r["stats"]["total_ms"])
+    return best
+
+
+def autotune(graph: api.Graph, kind: int, seeds, eps, *, prec: str = "fp32", alpha: float = 0.1, reps: int = 2,
+             shapes=None, buckets=None, use_cache: bool = True) -> dict:
+    """Best configuration for solving queries like (seeds, eps) on ``graph``.
+
+    Returns ``{"tile_w": W, "tuning": {...}, "ms": t, "table": [(cfg, ms), ...]}``;
+    pass ``tile_w`` and ``tuning`` to ``api.solve``.
+    """
+    seeds = np.ascontiguousarray(seeds, dtype=np.int32)
+    eps = np.ascontiguousarray(np.broadcast_to(np.asarray(eps, np.float64), seeds.shape))
+    path = _cache_path(graph, _graph_key(graph, kind, prec, seeds.shape[0]))
+    if use_cache and os.path.exists(path):
+        with open(path) as fh:
+            return json.load(fh)
+    table = []
+    _time(graph, kind, seeds[:8], eps[:8], prec, alpha, {"tile_w": 1}, 1)  # warm-up
+    for cfg in (shapes or SHAPES):
+        table.append((dict(cfg), _time(graph, kind, seeds, eps, prec, alpha, cfg, reps)))
+    shape = min(table, key=lambda t: t[1])[0]
+    for b in (buckets or BUCKETS)[1:]:
+        cfg = dict(shape)
+        cfg.update(b)
+        table.append((cfg, _time(graph, kind, seeds, eps, prec, alpha, cfg, reps)))
+    best, ms = min(table, key=lambda t: t[1])
+    out = {"tile_w": best["tile_w"], "tuning": {k: v for k, v in best.items() if k != "tile_w"}, "ms": ms,
+           "queries": int(seeds.shape[0]), "table": table}
+    if use_cache:
+        tmp = path + f".{os.getpid()}.tmp"
+        with open(tmp, "w") as fh:
+            json.dump(out, fh)
+        os.replace(tmp, path)
+    return out
