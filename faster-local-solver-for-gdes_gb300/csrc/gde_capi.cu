@@ -401,20 +401,41 @@ int build_static_records(gde_ctx* ctx, gde_graph* G, const int32_t* col) {
 // batching, so only `slots` residual vectors are ever live and they stay
 // L2-resident.  arrival_ms (may be null): query q is not admitted before
 // arrival_ms[q] after the launch starts; latency is then measured from it.
+// kinds / alphas (may be null): a mixed queue of PPR, Katz and heat-kernel
+// queries, each slot taking the kind of the query it admits.
+// budget_bytes > 0 caps the slot count so the slots' vectors fit in it.
+int64_t served_slot_bytes(int64_t n, int64_t cap, int prec64, bool hk, const PushArgs& tun) {
+    const int64_t es = prec64 ? 8 : 4;
+    const int64_t large_cap = cap / std::max(tun.chunk, 1) + cap / std::max(tun.med_max, 1) + 64;
+    return n * es * (3 + (hk ? 1 : 0)) + (prec64 ? 0 : n * 4) + n * 4 * 3 + n * (int64_t)sizeof(PushItem) +
+           large_cap * (int64_t)sizeof(PushItem);
+}
+
 int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const int32_t* seeds,
                  const double* eps, const double* arrival_ms, void* x_out, void* r_out, int out64, int out_mem,
-                 int64_t ld_out, double* oper_out, int32_t* rounds_out, float* lat_ms_out, gde_stats* stats) {
+                 int64_t ld_out, double* oper_out, int32_t* rounds_out, float* lat_ms_out, gde_stats* stats,
+                 const int32_t* kinds = nullptr, const double* alphas = nullptr, double budget_bytes = 0.0) {
     const int64_t n = G->g.n;
     const int kind = p->kind;
     const int prec64 = (p->prec == GDE_FP64);
     if (nq >= (int64_t)1 << 31) return fail(ctx, GDE_EINVAL, "too many queries");
+    bool any_hk = false;
+    if (kinds)
+        for (int64_t q = 0; q < nq; q++) any_hk |= (kinds[q] == KIND_HK);
     int S = p->slots > 0 ? p->slots : 32;
     S = (int)std::min<int64_t>(std::min<int64_t>(S, nq), 512);
     PushArgs base{};
     fill_tuning(p, base);
+    if (budget_bytes > 0.0) {
+        // admission by memory budget: only as many slots as fit
+        const int64_t per = served_slot_bytes(n, G->g.cap, prec64, any_hk, base);
+        const int64_t fit = (int64_t)(budget_bytes / (double)per);
+        if (fit < 1) return fail(ctx, GDE_ENOMEM, "the HBM budget does not hold one query slot");
+        S = (int)std::min<int64_t>(S, fit);
+    }
     TileWs tw;
     tw.a = base;
-    int rc = alloc_tiles(ctx, G, S, 1, prec64, false, false, true, !prec64, tw);
+    int rc = alloc_tiles(ctx, G, S, 1, prec64, any_hk, false, true, !prec64, tw);
     if (rc != GDE_OK) return rc;
     PushArgs& a = tw.a;
     a.small_max = base.small_max; a.med_max = base.med_max; a.chunk = base.chunk;
@@ -426,16 +447,35 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     CK(cudaEventRecord(ctx->ev[2], ctx->stream));
     CK(cudaMemsetAsync(a.R, 0, slab, ctx->stream));
     CK(cudaMemsetAsync(a.X, 0, slab, ctx->stream));
+    if (a.R2) CK(cudaMemsetAsync(a.R2, 0, slab, ctx->stream));
     if (a.XC) CK(cudaMemsetAsync(a.XC, 0, (size_t)S * n * 4, ctx->stream));
     // ---- the query queue on the device ----
-    std::vector<int32_t> qs(nq), qsc(nq);
-    std::vector<double> qt(nq), qr0(nq);
+    std::vector<int32_t> qs(nq), qsc(nq), qk(nq), qnl(kinds ? nq : 0), qpo(kinds ? nq : 0);
+    std::vector<double> qt(nq), qr0(nq), qal(nq);
     std::vector<long long> qarr(arrival_ms ? nq : 0);
+    std::vector<double> psi_all;
+    std::map<int64_t, int32_t> psi_at;
     for (int64_t q = 0; q < nq; q++) {
+        const int k = kinds ? kinds[q] : kind;
+        const double al = alphas ? alphas[q] : p->alpha;
+        qk[q] = k;
+        qal[q] = al;
         qsc[q] = seeds[q];
         qs[q] = G->node_in(seeds[q]);
-        qt[q] = (kind == KIND_PPR) ? eps[q] * p->alpha : eps[q];  // eps*alpha*degree / eps*degree
-        qr0[q] = (kind == KIND_PPR) ? p->alpha : 1.0;
+        if (k == KIND_PPR) qt[q] = eps[q] * al;              // eps * alpha * degree
+        else if (k == KIND_KATZ) qt[q] = eps[q];             // eps * degree
+        else qt[q] = std::exp(p->tau) * eps[q];              // e^tau * eps * degree / N / psi
+        qr0[q] = (k == KIND_PPR) ? al : 1.0;
+        if (k == KIND_HK) {
+            const int64_t N = estimate_n(p->tau, .5 * eps[q]);  // hk_solver.py:216-218
+            if (!psi_at.count(N)) {
+                psi_at[N] = (int32_t)psi_all.size();
+                std::vector<double> ps = psi_table(p->tau, N);
+                psi_all.insert(psi_all.end(), ps.begin(), ps.end());
+            }
+            qnl[q] = (int32_t)N;
+            qpo[q] = psi_at[N];
+        }
         if (arrival_ms) qarr[q] = (long long)(arrival_ms[q] * 1e6);
     }
     auto dev = [&](const char* name, size_t bytes) { return wsget(ctx, name, std::max<size_t>(bytes, 8)); };
@@ -459,6 +499,25 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     if (d_arr) CK(cudaMemcpyAsync(d_arr, qarr.data(), nq * 8, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemsetAsync(d_start, 0, nq * 8, ctx->stream));
     CK(cudaMemsetAsync(d_finish, 0, nq * 8, ctx->stream));
+    int32_t* d_kind = nullptr;
+    double* d_alpha = nullptr;
+    int32_t* d_nlev = nullptr;
+    int32_t* d_poff = nullptr;
+    double* d_psi = nullptr;
+    if (kinds) {
+        d_kind = (int32_t*)dev("q_kind", nq * 4);
+        d_alpha = (double*)dev("q_alpha", nq * 8);
+        d_nlev = (int32_t*)dev("q_nlev", nq * 4);
+        d_poff = (int32_t*)dev("q_psioff", nq * 4);
+        d_psi = (double*)dev("q_psi", std::max<size_t>(psi_all.size(), 1) * 8);
+        if (!d_kind || !d_alpha || !d_nlev || !d_poff || !d_psi) return fail(ctx, GDE_ENOMEM, "query queue");
+        CK(cudaMemcpyAsync(d_kind, qk.data(), nq * 4, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(d_alpha, qal.data(), nq * 8, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(d_nlev, qnl.data(), nq * 4, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(d_poff, qpo.data(), nq * 4, cudaMemcpyHostToDevice, ctx->stream));
+        if (!psi_all.empty())
+            CK(cudaMemcpyAsync(d_psi, psi_all.data(), psi_all.size() * 8, cudaMemcpyHostToDevice, ctx->stream));
+    }
     // the leading queries that have arrived at launch start go straight into
     // slots; the other slots start idle and admit queries as they arrive
     int first = S;
@@ -482,11 +541,17 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     for (int t = 0; t < S; t++) {
         TileParams& P = tp[t];
         memset(&P, 0, sizeof(P));
-        P.kind = kind;
-        P.method = M_LOCAL_GD;
+        const int k = (t < first) ? qk[t] : kind;
+        P.kind = k;
+        P.method = (k == KIND_HK) ? M_HK_LOCAL : M_LOCAL_GD;
         P.ncols = 1;
-        P.alpha = p->alpha;
+        P.alpha = (t < first) ? qal[t] : p->alpha;
+        P.tau = p->tau;
         P.x_gain = 1.0;
+        if (k == KIND_HK) {
+            P.n_levels = qnl[t];
+            P.psi_tab = d_psi + qpo[t];
+        }
         TileState& T = ts[t];
         memset(&T, 0, sizeof(T));
         T.t0 = 0;
@@ -535,6 +600,13 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     Q.out64 = out64;
     Q.seed_caller = d_sc;
     Q.seed_add = (kind == KIND_KATZ) ? -1.0 : 0.0;  // xt[s_node] -= 1. (katz_solver.py:243)
+    Q.kind = d_kind;
+    Q.alpha = d_alpha;
+    Q.n_levels = d_nlev;
+    Q.psi_off = d_poff;
+    Q.psi = d_psi;
+    Q.tau = p->tau;
+    Q.hk_scale = std::exp(p->tau);
     Q.oper = d_oper;
     Q.rounds = d_rounds;
     Q.start_ns = d_start;
@@ -715,6 +787,41 @@ int gde_serve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
     if (nq == 0) return GDE_OK;
     return solve_served(ctx, G, p, nq, seeds, eps, arrival_ms, x_out, r_out, out64, out_mem, ld_out, oper_out,
                         rounds_out, lat_ms_out, stats);
+}
+
+int gde_serve_mixed(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const int32_t* kinds,
+                    const int32_t* seeds, const double* eps, const double* alphas, const double* arrival_ms,
+                    double hbm_budget_bytes, void* x_out, int out64, int out_mem, int64_t ld_out, double* oper_out,
+                    int32_t* rounds_out, float* lat_ms_out, gde_stats* stats) {
+    if (!ctx || !G || !p || nq < 0 || (nq > 0 && (!seeds || !eps || !kinds)))
+        return fail(ctx, GDE_EINVAL, "bad serve arguments");
+    CK(cudaSetDevice(ctx->device));
+    const int64_t n = G->g.n;
+    if (ld_out < n && x_out) return fail(ctx, GDE_EINVAL, "ld_out < n");
+    bool any_hk = false;
+    for (int64_t q = 0; q < nq; q++) {
+        const int k = kinds[q];
+        if (k != KIND_PPR && k != KIND_KATZ && k != KIND_HK)
+            return fail(ctx, GDE_EINVAL, "query kinds are GDE_PPR, GDE_KATZ or GDE_HK");
+        any_hk |= (k == KIND_HK);
+        if (seeds[q] < 0 || seeds[q] >= n) return fail(ctx, GDE_EINVAL, "seed out of range");
+        if (!(eps[q] > 0.0)) return fail(ctx, GDE_EINVAL, "eps must be > 0");
+        if (arrival_ms && !(arrival_ms[q] >= 0.0)) return fail(ctx, GDE_EINVAL, "arrival times must be >= 0");
+        if (arrival_ms && q > 0 && arrival_ms[q] < arrival_ms[q - 1])
+            return fail(ctx, GDE_EINVAL, "arrival times must be non-decreasing (queries are admitted in order)");
+        const double al = alphas ? alphas[q] : p->alpha;
+        if (k != KIND_HK && !(al > 0.0)) return fail(ctx, GDE_EINVAL, "alpha must be > 0");
+        if (k == KIND_PPR && !(eps[q] * G->h_deg[G->node_in(seeds[q])] <= 1.))
+            return fail(ctx, GDE_EINVAL, "eps * degree[s_node] > 1 (ppr_solver.py:213)");
+    }
+    if (any_hk && !(p->tau >= 1.0)) return fail(ctx, GDE_EINVAL, "tau must be >= 1 (hk_solver.py:35)");
+    if (stats) memset(stats, 0, sizeof(*stats));
+    if (nq == 0) return GDE_OK;
+    gde_params pp = *p;
+    pp.method = M_LOCAL_GD;
+    pp.kind = kinds[0] == KIND_HK ? KIND_PPR : kinds[0];
+    return solve_served(ctx, G, &pp, nq, seeds, eps, arrival_ms, x_out, nullptr, out64, out_mem, ld_out, oper_out,
+                        rounds_out, lat_ms_out, stats, kinds, alphas, hbm_budget_bytes);
 }
 
 int gde_ctx_sync(gde_ctx* ctx) {

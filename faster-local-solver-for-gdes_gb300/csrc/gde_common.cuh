@@ -136,7 +136,15 @@ struct ServeQueue {
     int64_t ld_out;
     int out64;
     const int32_t* seed_caller;   // caller seed id per query (Katz GD: x[s] -= 1)
-    double seed_add;
+    double seed_add;              // single-kind queues (kind == nullptr): added to x[seed]
+    // mixed queues (nullptr: every query is of the launch's tile kind)
+    const int32_t* kind;          // KIND_PPR / KIND_KATZ / KIND_HK per query
+    const double* alpha;          // PPR / Katz alpha per query
+    const int32_t* n_levels;      // HK: Taylor length N per query
+    const int32_t* psi_off;       // HK: offset of the query's psi table in psi
+    const double* psi;            // HK: psi tables, concatenated
+    double tau;                   // HK temperature
+    double hk_scale;              // HK: x is divided by e^tau
     double* oper;                 // [nq] operation counts
     int* rounds;                  // [nq]
     unsigned long long* start_ns; // [nq] admission time

@@ -1355,7 +1355,10 @@ __device__ void finish_round(const PushArgs& a, int t, int level, bool dense_nex
     {
         TileState& ts = a.ts[t];
         ts.dense_next[par ^ 1] = dense_next ? 1 : 0;
-        if (ts.front_cnt[par] == 0 || hk_end) {
+        // a served heat-kernel slot ends one (empty) round after its last
+        // level: that level pushes into x during SCATTER, so x is read out by
+        // the next round's retire
+        if (ts.front_cnt[par] == 0 || (hk_end && !a.serve)) {
             if (a.serve) {
                 // served slot: the query's result is extracted and the slot
                 // cleared by every block in this SCATTER; admit next round
@@ -1404,6 +1407,17 @@ __device__ void admit_query(const PushArgs& a, int t, int it) {
     ts.cand_cnt[0] = 1;
     ts.t0 = it + 1;
     ts.qid = qid;
+    if (q.kind) {
+        // mixed queue: the slot takes the query's kind and parameters
+        TileParams& tp = a.tp[t];
+        const int k = q.kind[qid];
+        tp.kind = k;
+        tp.method = (k == KIND_HK) ? M_HK_LOCAL : M_LOCAL_GD;
+        tp.alpha = (k == KIND_HK) ? 0.0 : q.alpha[qid];
+        tp.tau = q.tau;
+        tp.n_levels = (k == KIND_HK) ? q.n_levels[qid] : 0;
+        tp.psi_tab = (k == KIND_HK) ? q.psi + q.psi_off[qid] : nullptr;
+    }
     ColState& cs = a.cs[(int64_t)t * W];
     cs.theta = q.theta[qid];
     cs.oper = 0.0;
@@ -1428,14 +1442,20 @@ __device__ void retire_range(const PushArgs& a, int t, long long beg, long long 
     const int qid = a.ts[t].qid;
     T* X = slab_ptr<T>(a.X, a, t);
     T* R = slab_ptr<T>(a.R, a, t);
+    T* R2 = a.R2 ? slab_ptr<T>(a.R2, a, t) : nullptr;
     float* XC = a.kahan ? slab_ptr<float>(a.XC, a, t) : nullptr;
     const int32_t* perm = a.g.perm;
     const int sc = q.seed_caller[qid];
+    const int kind = q.kind ? q.kind[qid] : a.tp[t].kind;
+    // Katz GD: xt[s_node] -= 1 (katz_solver.py:243); HK: xt / e^tau (hk_solver.py:295)
+    const double seed_add = q.kind ? (kind == KIND_KATZ ? -1.0 : 0.0) : q.seed_add;
+    const double xdiv = (kind == KIND_HK) ? q.hk_scale : 1.0;
     for (long long u = beg + threadIdx.x; u < end; u += kThreads) {
         const int64_t v = (perm ? (int64_t)perm[u] : u) * a.ld;
         double x = (double)X[v];
         if (XC) x -= (double)XC[v];  // Kahan: the sum is X - XC
-        if (u == sc) x = x + q.seed_add;
+        if (u == sc) x = x + seed_add;
+        if (xdiv != 1.0) x = x / xdiv;
         if (q.x_out) {
             if (q.out64) reinterpret_cast<double*>(q.x_out)[(int64_t)qid * q.ld_out + u] = x;
             else reinterpret_cast<float*>(q.x_out)[(int64_t)qid * q.ld_out + u] = (float)x;
@@ -1446,6 +1466,7 @@ __device__ void retire_range(const PushArgs& a, int t, long long beg, long long 
         }
         X[v] = T(0);
         R[v] = T(0);
+        if (R2) R2[v] = T(0);
         if (XC) XC[v] = 0.f;
     }
 }

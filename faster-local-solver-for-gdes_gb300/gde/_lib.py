@@ -63,6 +63,8 @@ SIGNATURES = {
     "gde_feature_update": (_int, [_p, _p, _p, _p, _p, _p, _i64, _int, ctypes.POINTER(Params), _i64, _p, _p, _p,
                                   _i64, _dbl, _p, ctypes.POINTER(Stats)]),
     "gde_plain_ppr_local": (_int, [_p, _p, _i32, _dbl, _dbl, _p, _p, _p, _p]),
+    "gde_serve_mixed": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _p, _p, _p, _dbl, _p, _int, _int, _i64,
+                               _p, _p, _p, ctypes.POINTER(Stats)]),
     "gde_ctx_trace": (_int, [_p, _int]),
     "gde_ctx_trace_read": (_int, [_p, _p, _i64, _p, _p, _p]),
     "gde_solve_noalloc": (_int, [_p, _p, ctypes.POINTER(Params), _i32, _dbl, _p, _p, _int, _p, _p]),

@@ -182,6 +182,43 @@ def serve(graph: Graph, kind: int, seeds, eps, *, arrival_ms=None, prec: str = "
             "latency_ms": lat, "stats": st.as_dict()}
 
 
+def serve_mixed(graph: Graph, kinds, seeds, eps, *, alphas=None, tau: float = 0.0, arrival_ms=None,
+                hbm_budget_bytes: float = 0.0, prec: str = "fp32", out64: bool | None = None, want_x: bool = True,
+                x_out=None, device_out: bool = False, slots: int = 0, max_rounds: int = 0,
+                tuning: dict | None = None) -> dict:
+    """Served mix of PPR / Katz / heat-kernel queries (continuous batching, one persistent launch).
+
+    ``kinds[q]`` in (L.PPR, L.KATZ, L.HK); ``alphas[q]`` for PPR / Katz; heat
+    kernel uses ``tau``.  Returns dict(x, oper, rounds, latency_ms, stats).
+    """
+    lib = L.load()
+    kinds = np.ascontiguousarray(np.atleast_1d(kinds), dtype=np.int32)
+    seeds = np.ascontiguousarray(np.atleast_1d(seeds), dtype=np.int32)
+    nq = seeds.shape[0]
+    eps = np.ascontiguousarray(np.broadcast_to(np.asarray(eps, dtype=np.float64), (nq,)))
+    al = None if alphas is None else np.ascontiguousarray(np.broadcast_to(np.asarray(alphas, np.float64), (nq,)))
+    arr = None if arrival_ms is None else np.ascontiguousarray(arrival_ms, dtype=np.float64)
+    if out64 is None:
+        out64 = prec == "fp64"
+    n = graph.n
+    if want_x and x_out is None:
+        x_out = _alloc((nq, n), out64, device_out, graph)
+    oper = np.zeros(nq, dtype=np.float64)
+    rounds = np.zeros(nq, dtype=np.int32)
+    lat = np.zeros(nq, dtype=np.float32)
+    t = dict(tuning or {})
+    if slots:
+        t["slots"] = slots
+    p = make_params(L.PPR, L.LOCAL_GD, prec, 1, 0.0, tau, max_rounds=max_rounds, tuning=t)
+    st = L.Stats()
+    status = lib.gde_serve_mixed(graph.ctx.ptr, graph.ptr, ctypes.byref(p), nq, _ptr(kinds), _ptr(seeds), _ptr(eps),
+                                 _ptr(al), _ptr(arr), float(hbm_budget_bytes), _ptr(x_out) if want_x else None,
+                                 int(out64), L.MEM_DEVICE if device_out else L.MEM_HOST, n, _ptr(oper), _ptr(rounds),
+                                 _ptr(lat), ctypes.byref(st))
+    L.check(graph.ctx.ptr, status, "gde_serve_mixed")
+    return {"x": x_out if want_x else None, "oper": oper, "rounds": rounds, "latency_ms": lat, "stats": st.as_dict()}
+
+
 def _alloc(shape, out64: bool, device: bool, graph: Graph):
     if device:
         import torch

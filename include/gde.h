@@ -167,6 +167,22 @@ int gde_serve(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t nq, const
               const double *arrival_ms, void *x_out, void *r_out, int out64, int out_mem, int64_t ld_out,
               double *oper_out, int32_t *rounds_out, float *lat_ms_out, gde_stats *stats);
 
+/* ---- served mixed queries (continuous batching of PPR, Katz and heat kernel) ----
+ * kinds[q] in {GDE_PPR, GDE_KATZ, GDE_HK}; alphas[q] the PPR / Katz alpha
+ * (host, may be NULL: p->alpha); heat-kernel queries use p->tau and the
+ * level push with N = estimate_n(tau, eps/2) (hk_sor_queue, omega = 1,
+ * hk_solver.py:206-295).  Each slot takes the kind of the query it admits.
+ * hbm_budget_bytes > 0 admits only as many concurrent slots as their
+ * vectors fit in that many bytes (GDE_ENOMEM if not even one).  x_out rows
+ * are the solutions as the reference returns them (Katz x[s] - 1, heat
+ * kernel x / e^tau); arrival_ms and latency as in gde_serve.  Replaces a
+ * request loop over ppr_gd_local_gpu / katz_gd_local_gpu / hk_sor_queue
+ * calls (ppr_solver.py:82-146, katz_solver.py:81-146, hk_solver.py:206-295). */
+int gde_serve_mixed(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t nq, const int32_t *kinds,
+                    const int32_t *seeds, const double *eps, const double *alphas, const double *arrival_ms,
+                    double hbm_budget_bytes, void *x_out, int out64, int out_mem, int64_t ld_out, double *oper_out,
+                    int32_t *rounds_out, float *lat_ms_out, gde_stats *stats);
+
 /* heat-kernel Taylor length, hk_solver.py:28-48 (estimate_n) */
 int64_t gde_hk_estimate_n(double tau, double eps);
 

@@ -74,3 +74,42 @@ def test_served_queries_wait_for_their_arrival(cl):
     # the launch lasts at least until the last arrival; latency is counted from arrival
     assert served["stats"]["kernel_ms"] >= 10.0
     assert (served["latency_ms"] < 10.0).all()
+
+
+def test_served_mixed_kinds_same_alone(cl):
+    """PPR, Katz and heat-kernel queries in one served launch, arriving over time."""
+    g, Gd = cl
+    rng = np.random.default_rng(4)
+    nq = 18
+    kinds = np.array([L.PPR, L.KATZ, L.HK] * (nq // 3), dtype=np.int32)
+    rng.shuffle(kinds)
+    seeds = graphs.uniform_seeds(g, nq, seed=21)
+    eps = np.exp(rng.uniform(np.log(1e-6), np.log(1e-5), nq))
+    katz_alpha = 1.0 / (float(g.degree.max()) + 1.0)
+    alphas = np.where(kinds == L.KATZ, katz_alpha, 0.1)
+    tau = 5.0
+    arrival = np.cumsum(rng.exponential(0.03, nq))
+    served = api.serve_mixed(Gd, kinds, seeds, eps, alphas=alphas, tau=tau, arrival_ms=arrival, prec="fp64", slots=5)
+    for i in range(nq):
+        if kinds[i] == L.HK:
+            alone = api.solve(Gd, L.HK, L.HK_LOCAL, seeds[i:i + 1], eps[i:i + 1], prec="fp64", tau=tau, want_r=False)
+        else:
+            alone = api.solve(Gd, int(kinds[i]), L.LOCAL_GD, seeds[i:i + 1], eps[i:i + 1], prec="fp64",
+                              alpha=float(alphas[i]), tile_w=1, want_r=False)
+        assert served["oper"][i] == pytest.approx(alone["oper"][0], rel=1e-12), (i, int(kinds[i]))
+        assert rel_l1(served["x"][i], alone["x"][0]) < 1e-11, (i, int(kinds[i]))
+
+
+def test_served_mixed_hbm_budget_caps_slots(cl):
+    g, Gd = cl
+    seeds = graphs.uniform_seeds(g, 8, seed=4)
+    kinds = np.full(8, L.PPR, dtype=np.int32)
+    # about two slots' worth of vectors (FP32: ~45 B per node plus the chunk list)
+    two = 2.5 * (45 * g.n + 16 * (g.nnz // 64 + 64))
+    res = api.serve_mixed(Gd, kinds, seeds, 1e-6, alphas=0.1, hbm_budget_bytes=two, slots=8)
+    assert res["stats"]["tiles"] == 2
+    ref = api.serve(Gd, L.PPR, seeds, 1e-6, alpha=0.1, slots=8)
+    np.testing.assert_allclose(res["oper"], ref["oper"], rtol=1e-3)
+    with pytest.raises(L.GDEError) as ei:
+        api.serve_mixed(Gd, kinds, seeds, 1e-6, alphas=0.1, hbm_budget_bytes=1000.0)
+    assert ei.value.status == L.GDE_ENOMEM
