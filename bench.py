@@ -58,9 +58,12 @@ def parse():
     ap.add_argument("--cpu-queries", type=int, default=0, help="CPU-baseline sample (0 = 2 per host thread)")
     ap.add_argument("--no-baselines", action="store_true")
     ap.add_argument("--tuning", default="", help="k=v,... engine tuning overrides")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c5"],
+    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
                     help="c2: served PPR on the 2.36M graph (the headline); c3: 1,024 seeds per launch with "
-                         "per-seed eps on the 100k graph; c5: InstantGNN 128-column snapshot updates")
+                         "per-seed eps on the 100k graph; c4: served PPR/Katz/heat-kernel mix with Poisson "
+                         "arrivals on R-MAT scale 22; c5: InstantGNN 128-column snapshot updates")
+    ap.add_argument("--rates", default="250,500,1000,2000,0",
+                    help="c4: Poisson arrival rates in queries/s to sweep (0 = all queries at once)")
     return ap.parse_args()
 
 
@@ -427,6 +430,67 @@ def run_c3(args):
         print(json.dumps(out), flush=True)
 
 
+def run_c4(args):
+    """Served mixed queries on R-MAT scale 22: 60% PPR, 25% Katz, 15% heat kernel, Poisson arrivals."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from gde import _lib as L
+    from gde import api, graphs
+    t0 = time.perf_counter()
+    g = graphs.rmat_scale22()
+    gen_s = time.perf_counter() - t0
+    ctx = api.Context.get(local)
+    G = api.Graph(g.indptr, g.indices, ctx=ctx)
+    dmax = float(g.degree.max())
+    Q = args.batch
+    tau, budget = 5.0, 120e9
+    x_dev = torch.empty((Q, g.n), dtype=torch.float32, device=f"cuda:{local}")
+    stream = torch.cuda.ExternalStream(api.ctx_stream(ctx), device=f"cuda:{local}")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+
+    def queries(k, rate):
+        rng = np.random.default_rng(7 + 1000 * rank + k)
+        kinds = rng.choice(np.array([L.PPR, L.KATZ, L.HK], np.int32), size=Q, p=[0.60, 0.25, 0.15])
+        seeds = graphs.uniform_seeds(g, Q, seed=7 + 1000 * rank + k)
+        eps = np.exp(rng.uniform(np.log(1e-8), np.log(1e-5), Q))
+        # ppr_gd's precondition eps * degree[s] <= 1 (ppr_solver.py:213) for hub seeds
+        eps = np.where(kinds == L.PPR, np.minimum(eps, 1.0 / g.degree[seeds]), eps)
+        alphas = np.where(kinds == L.KATZ, 0.5 / dmax, ALPHA)
+        arr = None if rate <= 0 else np.cumsum(rng.exponential(1e3 / rate, Q))
+        return kinds, seeds, eps, alphas, arr
+
+    def step(k, rate):
+        kinds, seeds, eps, alphas, arr = queries(k, rate)
+        return api.serve_mixed(G, kinds, seeds, eps, alphas=alphas, tau=tau, arrival_ms=arr, hbm_budget_bytes=budget,
+                               prec="fp32", x_out=x_dev, device_out=True, slots=args.slots)
+
+    for w in range(args.warmup):
+        step(10 + w, 0)
+    rows = []
+    with ClockSampler(local) as clk:
+        for rate in [float(r) for r in args.rates.split(",")]:
+            times, outs = _timed_steps(stream, flush, args.steps, lambda k: step(100 + k, rate))
+            lat = np.concatenate([o["latency_ms"] for o in outs])
+            rows.append({"rate_qps": rate if rate > 0 else None, "queries_per_s": Q * len(times) / (sum(times) / 1e3),
+                         "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+                         "slots": int(outs[0]["stats"]["tiles"]), "ms_per_step": sum(times) / len(times)})
+    best = max(rows, key=lambda r: r["queries_per_s"])
+    out = {
+        "metric": "served mixed queries/s + p50/p99 ms (60% PPR, 25% Katz, 15% heat kernel), R-MAT scale 22",
+        "value": best["queries_per_s"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": best["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "served_mix_ppr_katz_hk_fp32_rmat22", "n": g.n, "nnz": g.nnz, "queries_per_step": Q,
+                   "ppr_alpha": ALPHA, "katz_alpha": "0.5 / d_max", "hk_tau": tau, "eps": "log-uniform [1e-8, 1e-5]",
+                   "hbm_budget_bytes": budget, "requested_slots": args.slots, "graph_generation_s": gen_s,
+                   "l2": "512 MB buffer written between timed steps"},
+        "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "rate_sweep": rows,
+        "gpu_launches": args.steps * len(rows), "clocks": clk.summary(),
+    }
+    print(json.dumps(out), flush=True)
+
+
 def run_c5(args):
     """InstantGNN dynamic propagation: 128 FP32 feature columns, 16 snapshots of 59,375 inserted edges."""
     import torch
@@ -491,6 +555,8 @@ def main():
         run_reference(args)
     elif args.workload == "c3":
         run_c3(args)
+    elif args.workload == "c4":
+        run_c4(args)
     elif args.workload == "c5":
         run_c5(args)
     else:

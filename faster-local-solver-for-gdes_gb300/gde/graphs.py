@@ -109,10 +109,15 @@ def chung_lu(n: int, exponent: float, mean_degree: float, max_degree: float, see
 
 def rmat(scale: int, edge_factor: int, a: float, b: float, c: float, seed: int,
          drop_isolated: bool = True, name: str = "", chunk: int = 1 << 23) -> CSRGraph:
-    """R-MAT graph on ``2**scale`` nodes with ``edge_factor * 2**scale`` sampled edges."""
+    """R-MAT graph on ``2**scale`` nodes with ``edge_factor * 2**scale`` CSR entries (before dedup).
+
+    ``edge_factor * 2**scale / 2`` undirected edges are sampled; symmetrising
+    gives ``edge_factor`` CSR entries per node before duplicates and
+    self-loops are dropped (scale 22, factor 16: ~67M entries).
+    """
     rng = np.random.default_rng(seed)
     n = 1 << scale
-    m = edge_factor * n
+    m = edge_factor * n // 2
     srcs = []
     dsts = []
     ab = a + b
