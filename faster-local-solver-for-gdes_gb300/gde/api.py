@@ -219,6 +219,16 @@ def serve_mixed(graph: Graph, kinds, seeds, eps, *, alphas=None, tau: float = 0.
     return {"x": x_out if want_x else None, "oper": oper, "rounds": rounds, "latency_ms": lat, "stats": st.as_dict()}
 
 
+def katz_spectral_bounds(graph: Graph, alpha: float, max_iter: int = 400, tol: float = 1e-10) -> dict:
+    """lambda_max / lambda_min of the adjacency (GPU Lanczos) and the Katz Chebyshev bounds l_max, mu_min."""
+    lib = L.load()
+    out = [ctypes.c_double() for _ in range(4)]
+    st = lib.gde_katz_spectral_bounds(graph.ctx.ptr, graph.ptr, float(alpha), int(max_iter), float(tol),
+                                      *[ctypes.byref(o) for o in out])
+    L.check(graph.ctx.ptr, st, "gde_katz_spectral_bounds")
+    return {"lam_max": out[0].value, "lam_min": out[1].value, "l_max": out[2].value, "mu_min": out[3].value}
+
+
 def _alloc(shape, out64: bool, device: bool, graph: Graph):
     if device:
         import torch

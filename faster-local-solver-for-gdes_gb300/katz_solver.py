@@ -15,7 +15,7 @@ from gde import api
 from gde.dropin import Timer, graph_for, oper_like
 
 __all__ = ["katz_gd", "katz_gd_local_gpu", "katz_gd_standard_gpu", "katz_cheby", "solve_a_graph_gpu",
-           "solve_a_graph_cheby"]
+           "solve_a_graph_cheby", "katz_spectral_bounds"]
 
 
 def _solve1(n, indptr, indices, degree, s_node, alpha, eps, method, prec, l_max=0.0, mu_min=0.0):
@@ -80,3 +80,17 @@ def solve_a_graph_cheby(n, indptr, indices, degree, alpha, l_max, mu_min, eps, g
         _, _, go[ii], gt[ii] = katz_cheby(n, indptr, indices, degree, int(s_nodes[ii]), alpha, l_max, mu_min, eps,
                                           False)
     return s_nodes, lo, lt, go, gt
+
+
+def katz_spectral_bounds(n, indptr, indices, degree, alpha):
+    """(l_max, mu_min, lambda_max, lambda_min) for katz_cheby on the GPU.
+
+    The reference computes lambda_max(A) and lambda_min(A) with
+    scipy.sparse.linalg.eigsh in its experiment scripts (katz_exp_dmax.py:20,
+    katz_exp_dmin.py:20); here a Lanczos iteration runs on the device.  The
+    spectrum of Q = I - alpha A then lies in [mu_min, l_max].
+    """
+    g = graph_for(indptr, indices, degree)
+    assert g.n == n, "n must equal len(indptr) - 1"
+    b = api.katz_spectral_bounds(g, alpha)
+    return b["l_max"], b["mu_min"], b["lam_max"], b["lam_min"]

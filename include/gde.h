@@ -183,6 +183,18 @@ int gde_serve_mixed(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t nq,
                     double hbm_budget_bytes, void *x_out, int out64, int out_mem, int64_t ld_out, double *oper_out,
                     int32_t *rounds_out, float *lat_ms_out, gde_stats *stats);
 
+/* ---- Katz Chebyshev spectral bounds ----
+ * lambda_max(A) and lambda_min(A) of the graph's adjacency by a Lanczos
+ * iteration on the GPU (FP64), the quantities katz_exp_dmax.py:20 and
+ * katz_exp_dmin.py:20 obtain with scipy.sparse.linalg.eigsh; l_max =
+ * 1 - alpha lambda_min and mu_min = 1 - alpha lambda_max bound the spectrum
+ * of Q = I - alpha A for katz_cheby (katz_solver.py:340-368).  Stops when
+ * both extreme Ritz values change by less than tol (relative) over 5 steps;
+ * GDE_EITERCAP (with the last estimates written) after max_iter steps.
+ * Outputs are host pointers (may be NULL). */
+int gde_katz_spectral_bounds(gde_ctx *ctx, gde_graph *g, double alpha, int max_iter, double tol, double *lam_max,
+                             double *lam_min, double *l_max, double *mu_min);
+
 /* heat-kernel Taylor length, hk_solver.py:28-48 (estimate_n) */
 int64_t gde_hk_estimate_n(double tau, double eps);
 

@@ -1,0 +1,55 @@
+"""Katz Chebyshev spectral bounds by GPU Lanczos against scipy's eigsh.
+
+The reference's experiment scripts take lambda_max(A) (eigsh which='LM')
+and lambda_min(A) (which='SA') of the adjacency (katz_exp_dmax.py:20,
+katz_exp_dmin.py:20); the GPU Lanczos must agree, and the bounds it gives
+must make katz_cheby converge to the Katz solution.
+"""
+import numpy as np
+import pytest
+import scipy.sparse as sp
+import scipy.sparse.linalg as sla
+
+from gde import _lib as L
+from gde import api, graphs
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.mark.parametrize("which", ["cl", "rmat"])
+def test_lanczos_extremes_match_eigsh(which):
+    if which == "cl":
+        g = graphs.chung_lu(3000, 2.1, 8.0, 300.0, seed=3)
+    else:
+        g = graphs.rmat(12, 16, 0.57, 0.19, 0.19, seed=1)
+    A = sp.csr_matrix((np.ones(g.nnz), g.indices, g.indptr), shape=(g.n, g.n))
+    lmax = sla.eigsh(A, 1, which="LA", tol=1e-12)[0][0]
+    lmin = sla.eigsh(A, 1, which="SA", tol=1e-12)[0][0]
+    Gd = api.Graph(g.indptr, g.indices)
+    alpha = 0.5 / lmax
+    b = api.katz_spectral_bounds(Gd, alpha, tol=1e-11)
+    assert b["lam_max"] == pytest.approx(lmax, rel=1e-8)
+    assert b["lam_min"] == pytest.approx(lmin, rel=1e-7, abs=1e-7 * lmax)
+    assert b["l_max"] == pytest.approx(1 - alpha * lmin, rel=1e-8)
+    assert b["mu_min"] == pytest.approx(1 - alpha * lmax, rel=1e-8)
+
+
+def test_bounds_drive_katz_cheby():
+    g = graphs.chung_lu(3000, 2.1, 8.0, 300.0, seed=3)
+    Gd = api.Graph(g.indptr, g.indices)
+    b = api.katz_spectral_bounds(Gd, 1.0)  # lambdas only
+    alpha = 0.5 / b["lam_max"]
+    l_max, mu_min = 1 - alpha * b["lam_min"], 1 - alpha * b["lam_max"]
+    s = int(graphs.uniform_seeds(g, 1, seed=5)[0])
+    res = api.solve(Gd, L.KATZ, L.GLOBAL_CHEBY, [s], [1e-9], prec="fp64", alpha=alpha, l_max=l_max, mu_min=mu_min)
+    # FP64 truth: (I - alpha A) x = e_s
+    A = sp.csr_matrix((np.ones(g.nnz), g.indices, g.indptr), shape=(g.n, g.n))
+    e = np.zeros(g.n)
+    e[s] = 1.0
+    truth = sla.spsolve((sp.identity(g.n) - alpha * A).tocsc(), e)
+    assert np.abs(res["x"][0] - truth).sum() / np.abs(truth).sum() < 1e-6
+    # and the same bounds as the oracle's Chebyshev takes them
+    xo, _, _ = O.cheby(g.n, g.indptr, g.indices, g.degree.astype(np.float64), s, alpha, 1e-9, False, katz=True,
+                       l_max=l_max, mu_min=mu_min, sync=True)
+    assert np.abs(res["x"][0] - xo).sum() / np.abs(xo).sum() < 1e-10
