@@ -62,6 +62,9 @@ def parse():
                     help="c2: served PPR on the 2.36M graph (the headline); c3: 1,024 seeds per launch with "
                          "per-seed eps on the 100k graph; c4: served PPR/Katz/heat-kernel mix with Poisson "
                          "arrivals on R-MAT scale 22; c5: InstantGNN 128-column snapshot updates")
+    ap.add_argument("--mlp", action="store_true",
+                    help="c5: train the MLP classifier on the device-resident features after the initial push and "
+                         "after the last snapshot (outside the timed region)")
     ap.add_argument("--rates", default="250,500,1000,2000,0",
                     help="c4: Poisson arrival rates in queries/s to sweep (0 = all queries at once)")
     return ap.parse_args()
@@ -516,6 +519,14 @@ def run_c5(args):
     api.feature_push(G, L.IGN, Pd, Rd, eps, alpha=ALPHA, beta=beta, prec="fp32")
     torch.cuda.synchronize()
     init_s = time.perf_counter() - t0
+    mlp = {}
+    if args.mlp:
+        # 40 classes from a random linear map of the features (argmax), random 60/20/20 split;
+        # the propagated matrix goes to torch on the device
+        from gde import consumer
+        labels = torch.from_numpy((X @ rng.standard_normal((F, 40))).argmax(1)).to(dev)
+        split = consumer.random_split(n, dev, seed=4)
+        mlp["initial"] = consumer.train_eval(Pd, labels, split)
     times, outs = [], []
     with ClockSampler(local) as clk:
         for s in range(snaps):
@@ -546,6 +557,9 @@ def run_c5(args):
                      "peak_kind": peak_kind, "traffic": None},
         "gpu_launches": int(sum(1 for _ in outs)), "clocks": clk.summary(),
     }
+    if args.mlp:
+        mlp["final"] = consumer.train_eval(Pd, labels, split)
+        out["mlp"] = mlp
     print(json.dumps(out), flush=True)
 
 
