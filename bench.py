@@ -552,6 +552,7 @@ def run_c5(args):
                    "snapshots": snaps, "edges_per_snapshot": int(dyn.Us.shape[1]), "alpha": ALPHA, "beta": beta,
                    "eps": eps, "initial_push_s": init_s},
         "column_updates_per_s": snaps * F / (total_ms / 1e3),
+        "push_kernel_ms_per_step": agg["kernel_ms"] / snaps,
         "mean_oper_per_column": float(np.mean([o["oper"].mean() for o in outs])),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": None},

@@ -22,66 +22,9 @@
 
 using namespace gde;
 
-namespace {
+#include "gde_internal.h"
 
-struct DevBuf {
-    void* p = nullptr;
-    size_t bytes = 0;
-};
 
-constexpr int kDefaultMaxRounds = 100000;
-
-}  // namespace
-
-struct gde_ctx {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    int sms = 0;
-    std::string err;
-    GridBarrier* bar = nullptr;
-    int* derr = nullptr;
-    LaunchStats* dstats = nullptr;
-    LaunchStats* hstats = nullptr;  // pinned
-    TileState* hts = nullptr;       // pinned scratch
-    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
-    std::map<std::string, DevBuf> ws;
-    std::vector<int> stamp;         // per-tile stamp bases (valid while "mark" is allocated)
-    PlainWork plain{};
-    int64_t plain_n = -1;
-    // opt-in push-kernel phase trace (gde_ctx_trace)
-    unsigned long long* trace = nullptr;
-    int trace_iters = 0;
-    int trace_grid = 0;
-};
-
-struct gde_graph {
-    gde_ctx* ctx = nullptr;
-    DevGraph g{};
-    int64_t* row_ptr = nullptr;
-    int32_t* col = nullptr;
-    int32_t* row_len = nullptr;
-    float* degf = nullptr;
-    double* degd = nullptr;
-    double* nfac = nullptr;
-    double* npush = nullptr;
-    double* tfac = nullptr;
-    float* tfac_f = nullptr;
-    double ign_beta = NAN;
-    std::vector<int64_t> h_indptr;
-    std::vector<int64_t> h_len;
-    std::vector<double> h_deg;
-    bool deg_is_len = true;
-    // Static graphs are stored relabelled by descending degree: push targets
-    // are hit in proportion to their degree, so the hot part of every
-    // residual vector is a short prefix that stays in L2.  h_perm maps a
-    // caller id to the internal id; every API id stays the caller's.
-    bool relabeled = false;
-    std::vector<int32_t> h_perm;
-    int32_t* perm_d = nullptr;
-    uint32_t* col_deg = nullptr;
-    NodeRec* rec = nullptr;
-    int32_t node_in(int64_t u) const { return relabeled ? h_perm[u] : (int32_t)u; }
-};
 
 namespace {
 
@@ -944,6 +887,7 @@ int gde_graph_free(gde_graph* G) {
     cudaFree(G->row_ptr); cudaFree(G->col); cudaFree(G->row_len); cudaFree(G->degf); cudaFree(G->degd);
     cudaFree(G->nfac); cudaFree(G->tfac); cudaFree(G->tfac_f); cudaFree(G->perm_d);
     cudaFree(G->col_deg); cudaFree(G->rec);
+    cudaFree(G->pw1); cudaFree(G->pwb);
     delete G;
     return GDE_OK;
 }
@@ -1474,3 +1418,7 @@ const DevGraph* gde_internal_devgraph(gde_graph* G) { return &G->g; }
 int32_t gde_internal_node_in(gde_graph* G, int64_t u) { return G->node_in(u); }
 double gde_internal_host_degree(gde_graph* G, int32_t u) { return G->h_deg[u]; }
 void gde_internal_fill_tuning(const gde_params* p, PushArgs* a) { fill_tuning(p, *a); }
+int gde_internal_ign_tables(gde_ctx* ctx, gde_graph* G, double beta) {
+    if (G->nfac && G->ign_beta == beta) return GDE_OK;
+    return upload_ign_tables(ctx, G, beta);
+}

@@ -7,9 +7,13 @@
 // GPU (InstantGNN.py:303-318 for InstantGNN, ppr_solver.py:776-792 for the
 // beta = 0 PPR update); (3) push from the repaired nodes with the engine.
 //
-// The edit itself is a short sequential pass on the host (O(sum of scanned
-// row lengths)); its effect on the device graph is uploaded as a list of
-// (position, value) entries plus the new degree tables.
+// Insert-only batches without self-loops are applied on the device
+// (device_insert below): which edges are inserted and where every new entry
+// lands are decided in parallel with exactly the sequential semantics, and
+// the caller's host arrays receive the same values afterwards.  Deletions
+// keep a short sequential pass on the host (O(sum of scanned row lengths)),
+// whose effect on the device graph is uploaded as (position, value) entries
+// plus the new degree tables.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -21,6 +25,7 @@
 
 #include "gde_common.cuh"
 #include "gde_engine.h"
+#include "gde_internal.h"
 
 using namespace gde;
 
@@ -37,6 +42,7 @@ cudaStream_t gde_internal_stream(gde_ctx* ctx);
 const double* gde_internal_npush(gde_graph* G);
 const double* gde_internal_degd(gde_graph* G);
 bool gde_internal_relabeled(gde_graph* G);
+int gde_internal_ign_tables(gde_ctx* ctx, gde_graph* G, double beta);
 
 namespace {
 
@@ -131,6 +137,382 @@ __global__ void repair_pass2(const RepairKey* keys, int nkeys, const int32_t* nb
     R[o] = (T)r;
 }
 
+// ---------------------------------------------------------------------------
+// Device-side insertion (updetaGraph with onlyinsert = True, no self-loops)
+// ---------------------------------------------------------------------------
+// Edge e = (u, v) of the batch is inserted iff v is not in u's row when the
+// sequential pass reaches it, i.e. iff the pair {u, v} is absent from the
+// graph at batch start and e is the first occurrence of {u, v} in the batch.
+// A row receives its new neighbours in batch order: the j-th inserted edge
+// incident to w (by batch index) lands at indptr[w] + degree[w] + j.
+
+constexpr int kEdT = 256;
+constexpr unsigned long long kEmptyKey = ~0ull;
+
+__global__ void ins_exists_kernel(DevGraph g, const int32_t* us, const int32_t* vs, int64_t k, uint8_t* state) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t e = w0; e < k; e += nw) {
+        const int u = us[e], v = vs[e];
+        const int64_t rp = g.row_ptr[u];
+        const int len = g.row_len[u];
+        bool hit = false;
+        for (int j = lane; j < len && !hit; j += 32) hit = (g.col[rp + j] == v);
+        hit = __any_sync(0xffffffffu, hit);
+        if (lane == 0) state[e] = hit ? 1 : 0;  // 1: present, skipped
+    }
+}
+
+__device__ __forceinline__ unsigned long long pair_key(int u, int v) {
+    const unsigned a = (unsigned)min(u, v), b = (unsigned)max(u, v);
+    return ((unsigned long long)a << 32) | b;
+}
+
+__device__ __forceinline__ unsigned hash_slot(unsigned long long key, unsigned mask) {
+    unsigned long long z = key * 0x9E3779B97F4A7C15ull;
+    return (unsigned)(z >> 32) & mask;
+}
+
+// first occurrence of each absent pair: open addressing on the pair key,
+// atomicMin of the batch index (probes bounded by the table size)
+__global__ void ins_hash_kernel(const int32_t* us, const int32_t* vs, int64_t k, const uint8_t* state,
+                                unsigned long long* keys, int* first, int* slot, unsigned mask, int* err) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < k; e += (int64_t)gridDim.x * blockDim.x) {
+        if (state[e]) continue;
+        const unsigned long long key = pair_key(us[e], vs[e]);
+        unsigned h = hash_slot(key, mask);
+        bool placed = false;
+        for (unsigned probe = 0; probe <= mask; ++probe) {
+            const unsigned long long old = atomicCAS(&keys[h], kEmptyKey, key);
+            if (old == kEmptyKey || old == key) {
+                atomicMin(&first[h], (int)e);
+                slot[e] = (int)h;
+                placed = true;
+                break;
+            }
+            h = (h + 1) & mask;
+        }
+        if (!placed) atomicExch(err, 2);
+    }
+}
+
+__global__ void ins_count_kernel(const int32_t* us, const int32_t* vs, int64_t k, uint8_t* state, const int* first,
+                                 const int* slot, int* cnt) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < k; e += (int64_t)gridDim.x * blockDim.x) {
+        if (state[e]) continue;
+        if (first[slot[e]] != (int)e) {
+            state[e] = 1;  // a repeat of an earlier inserted pair
+            continue;
+        }
+        state[e] = 2;  // inserted
+        atomicAdd(&cnt[us[e]], 1);
+        atomicAdd(&cnt[vs[e]], 1);
+    }
+}
+
+// exclusive scan of n ints: per-block scan, scan of block sums, add
+__global__ void scan_block_kernel(const int* in, int* out, int64_t n, int* sums) {
+    __shared__ int ws[kEdT / 32];
+    const int64_t i = (int64_t)blockIdx.x * kEdT + threadIdx.x;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int x = (i < n) ? in[i] : 0;
+    int inc = x;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const int y = __shfl_up_sync(0xffffffffu, inc, o);
+        if (lane >= o) inc += y;
+    }
+    if (lane == 31) ws[warp] = inc;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int acc = 0;
+        for (int w = 0; w < kEdT / 32; ++w) {
+            const int t = ws[w];
+            ws[w] = acc;
+            acc += t;
+        }
+        sums[blockIdx.x] = acc;
+    }
+    __syncthreads();
+    if (i < n) out[i] = ws[warp] + inc - x;
+}
+
+__global__ void scan_sums_kernel(int* sums, int nb, int* total) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    int acc = 0;
+    for (int b = 0; b < nb; ++b) {
+        const int t = sums[b];
+        sums[b] = acc;
+        acc += t;
+    }
+    *total = acc;
+}
+
+__global__ void scan_add_kernel(int* out, int64_t n, const int* sums, const int* total) {
+    const int64_t i = (int64_t)blockIdx.x * kEdT + threadIdx.x;
+    if (i < n) out[i] += sums[blockIdx.x];
+    if (i == n) out[n] = *total;
+}
+
+__global__ void ins_capacity_kernel(DevGraph g, const int* cnt, int64_t n, int* err) {
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (int64_t)gridDim.x * blockDim.x)
+        if (cnt[w] && g.row_ptr[w] + g.row_len[w] + cnt[w] > g.row_ptr[w + 1]) atomicExch(err, 1);
+}
+
+__global__ void ins_fill_kernel(const int32_t* us, const int32_t* vs, int64_t k, const uint8_t* state,
+                                const int* off, int* fill, int* be, int* bo) {
+    for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < k; e += (int64_t)gridDim.x * blockDim.x) {
+        if (state[e] != 2) continue;
+        const int u = us[e], v = vs[e];
+        const int su = off[u] + atomicAdd(&fill[u], 1);
+        be[su] = (int)e;
+        bo[su] = v;
+        const int sv = off[v] + atomicAdd(&fill[v], 1);
+        be[sv] = (int)e;
+        bo[sv] = u;
+    }
+}
+
+// One warp per node with insertions: rank the node's new neighbours by batch
+// index, write them after the old entries, update the degree tables.
+__global__ void ins_write_kernel(DevGraph g, int32_t* col, int32_t* row_len, float* degf, double* degd,
+                                 double* nfac, double* tfac, float* tfac_f, const double* pw1, const double* pwb,
+                                 int64_t n, const int* cnt, const int* off, const int* be, const int* bo,
+                                 int32_t* nbr_sorted, int64_t* pos_out) {
+    const int lane = threadIdx.x & 31;
+    const int64_t w0 = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t w = w0; w < n; w += nw) {
+        const int c = cnt[w];
+        if (c == 0) continue;
+        const int base = off[w];
+        const int old_len = row_len[w];
+        const int64_t start = g.row_ptr[w] + old_len;
+        for (int i = lane; i < c; i += 32) {
+            const int ei = be[base + i];
+            int rank = 0;
+            for (int j = 0; j < c; ++j) rank += (be[base + j] < ei) ? 1 : 0;
+            col[start + rank] = bo[base + i];
+            nbr_sorted[base + rank] = bo[base + i];
+            pos_out[base + rank] = start + rank;
+        }
+        __syncwarp();
+        if (lane == 0) {
+            const int d = old_len + c;
+            row_len[w] = d;
+            degf[w] = (float)d;
+            degd[w] = (double)d;
+            if (nfac && pw1) {
+                nfac[w] = pw1[d];
+                tfac[w] = pwb[d];
+                tfac_f[w] = (float)pwb[d];
+            }
+        }
+    }
+}
+
+__global__ void ins_flags_kernel(const int* cnt, int* flag, int64_t n) {
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (int64_t)gridDim.x * blockDim.x)
+        flag[w] = cnt[w] > 0 ? 1 : 0;
+}
+
+__global__ void ins_keys_kernel(const int* cnt, const int* kidx, int64_t n, int32_t* keys) {
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (int64_t)gridDim.x * blockDim.x)
+        if (cnt[w] > 0) keys[kidx[w]] = (int32_t)w;
+}
+
+// Repair factors of each touched node (InstantGNN.py:304-307 / ppr_solver.py:777-788).
+__global__ void ins_repair_keys_kernel(const int32_t* keys, int nkeys, const int* cnt, const int* off,
+                                       const int32_t* row_len, int kind, double beta, const double* pw1,
+                                       const double* pwb, RepairKey* out) {
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nkeys; i += gridDim.x * blockDim.x) {
+        const int u = keys[i];
+        const int d = row_len[u];
+        const int od = d - cnt[u];
+        RepairKey K;
+        K.u = u;
+        K.ins_beg = off[u];
+        K.ins_end = off[u] + cnt[u];
+        K.del_beg = K.del_end = K.ins_end;
+        if (kind == KIND_IGN) {
+            K.a1 = pow((double)d / (double)od, 1.0 - beta);
+            K.a2 = pw1[od];
+            K.a3 = pw1[d];
+            K.b1 = pwb[od];
+            K.b2 = pwb[d];
+        } else {
+            K.a1 = (double)d;
+            K.a2 = (double)od;
+            K.a3 = 0.0;
+            K.b1 = K.b2 = 0.0;
+        }
+        out[i] = K;
+    }
+}
+
+int exclusive_scan(gde_ctx* ctx, const int* in, int* out, int64_t n, cudaStream_t st) {
+    const int nb = (int)((n + kEdT) / kEdT);  // covers index n for the total
+    int* sums = (int*)gde_internal_wsget(ctx, "ins_scan_sums", (size_t)nb * 4 + 8);
+    if (!sums) return gde_internal_fail(ctx, GDE_ENOMEM, "scan scratch");
+    int* total = sums + nb;
+    scan_block_kernel<<<nb, kEdT, 0, st>>>(in, out, n, sums);
+    scan_sums_kernel<<<1, 32, 0, st>>>(sums, nb, total);
+    scan_add_kernel<<<nb, kEdT, 0, st>>>(out, n, sums, total);
+    return GDE_OK;
+}
+
+// Degree-power tables d^(1-beta), d^beta for d = 0..max row capacity, with
+// the host C library's pow (the same values upload_ign_tables computes).
+int ensure_power_tables(gde_ctx* ctx, gde_graph* G, double beta) {
+    int64_t dmax = 0;
+    for (int64_t u = 0; u < G->g.n; u++) dmax = std::max(dmax, G->h_indptr[u + 1] - G->h_indptr[u]);
+    if (G->pw1 && G->pw_beta == beta && G->pw_max >= dmax) return GDE_OK;
+    std::vector<double> a(dmax + 1), b(dmax + 1);
+    for (int64_t d = 0; d <= dmax; d++) {
+        a[d] = std::pow((double)d, 1 - beta);
+        b[d] = std::pow((double)d, beta);
+    }
+    cudaFree(G->pw1);
+    cudaFree(G->pwb);
+    G->pw1 = G->pwb = nullptr;
+    if (cudaMalloc(&G->pw1, (dmax + 1) * 8) != cudaSuccess || cudaMalloc(&G->pwb, (dmax + 1) * 8) != cudaSuccess) {
+        cudaGetLastError();
+        return gde_internal_fail(ctx, GDE_ENOMEM, "degree power tables");
+    }
+    cudaStream_t st = gde_internal_stream(ctx);
+    cudaMemcpyAsync(G->pw1, a.data(), (dmax + 1) * 8, cudaMemcpyHostToDevice, st);
+    cudaMemcpyAsync(G->pwb, b.data(), (dmax + 1) * 8, cudaMemcpyHostToDevice, st);
+    if (cudaStreamSynchronize(st) != cudaSuccess) return gde_internal_fail(ctx, GDE_ECUDA, "power tables upload");
+    G->pw_max = dmax;
+    G->pw_beta = beta;
+    return GDE_OK;
+}
+
+struct DeviceInsert {
+    int status = GDE_OK;
+    bool fallback = false;       // capacity exceeded: the host pass reproduces the partial edit
+    const int32_t* keys = nullptr;
+    int nkeys = 0;
+    RepairKey* rkeys = nullptr;
+    const int32_t* nbr = nullptr;
+    int64_t inserted = 0;
+};
+
+DeviceInsert device_insert(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree, const int32_t* us,
+                           const int32_t* vs, int64_t k, int kind, double beta) {
+    DeviceInsert R;
+    const int64_t n = G->g.n;
+    cudaStream_t st = gde_internal_stream(ctx);
+    auto ws = [&](const char* name, size_t bytes) { return gde_internal_wsget(ctx, name, std::max<size_t>(bytes, 8)); };
+    unsigned H = 1;
+    while (H < 2 * (uint64_t)std::max<int64_t>(k, 1)) H <<= 1;
+    int32_t* d_us = (int32_t*)ws("ins_us", k * 4);
+    int32_t* d_vs = (int32_t*)ws("ins_vs", k * 4);
+    uint8_t* d_state = (uint8_t*)ws("ins_state", k);
+    int* d_slot = (int*)ws("ins_slot", k * 4);
+    unsigned long long* d_hk = (unsigned long long*)ws("ins_hkeys", (size_t)H * 8);
+    int* d_hf = (int*)ws("ins_hfirst", (size_t)H * 4);
+    int* d_cnt = (int*)ws("ins_cnt", n * 4);
+    int* d_fill = (int*)ws("ins_fill", n * 4);
+    int* d_off = (int*)ws("ins_off", (n + 1) * 4);
+    int* d_err = (int*)ws("ins_err", 4);
+    if (!d_us || !d_vs || !d_state || !d_slot || !d_hk || !d_hf || !d_cnt || !d_fill || !d_off || !d_err) {
+        R.status = gde_internal_fail(ctx, GDE_ENOMEM, "insertion scratch");
+        return R;
+    }
+#define DI_CK(call)                                                                    \
+    do {                                                                               \
+        cudaError_t e__ = (call);                                                      \
+        if (e__ != cudaSuccess) {                                                      \
+            R.status = gde_internal_fail(ctx, GDE_ECUDA, cudaGetErrorString(e__));     \
+            return R;                                                                  \
+        }                                                                              \
+    } while (0)
+    DI_CK(cudaMemcpyAsync(d_us, us, k * 4, cudaMemcpyHostToDevice, st));
+    DI_CK(cudaMemcpyAsync(d_vs, vs, k * 4, cudaMemcpyHostToDevice, st));
+    DI_CK(cudaMemsetAsync(d_hk, 0xff, (size_t)H * 8, st));
+    DI_CK(cudaMemsetAsync(d_hf, 0x7f, (size_t)H * 4, st));
+    DI_CK(cudaMemsetAsync(d_cnt, 0, n * 4, st));
+    DI_CK(cudaMemsetAsync(d_fill, 0, n * 4, st));
+    DI_CK(cudaMemsetAsync(d_err, 0, 4, st));
+    const int eb = (int)std::min<int64_t>(4096, (k * 32 + kEdT - 1) / kEdT + 1);
+    const int tb = (int)std::min<int64_t>(4096, (k + kEdT - 1) / kEdT + 1);
+    const int nbk = (int)std::min<int64_t>(4096, (n + kEdT - 1) / kEdT + 1);
+    const int nwb = (int)std::min<int64_t>(4096, (n * 32 + kEdT - 1) / kEdT + 1);
+    ins_exists_kernel<<<eb, kEdT, 0, st>>>(G->g, d_us, d_vs, k, d_state);
+    ins_hash_kernel<<<tb, kEdT, 0, st>>>(d_us, d_vs, k, d_state, d_hk, d_hf, d_slot, H - 1, d_err);
+    ins_count_kernel<<<tb, kEdT, 0, st>>>(d_us, d_vs, k, d_state, d_hf, d_slot, d_cnt);
+    ins_capacity_kernel<<<nbk, kEdT, 0, st>>>(G->g, d_cnt, n, d_err);
+    int herr = 0;
+    DI_CK(cudaMemcpyAsync(&herr, d_err, 4, cudaMemcpyDeviceToHost, st));
+    DI_CK(cudaStreamSynchronize(st));
+    if (herr != 0) {
+        // no slack for some insertion (or an overfull hash table): nothing was
+        // written yet; the host pass applies the sequential partial edit
+        R.fallback = true;
+        return R;
+    }
+    if (exclusive_scan(ctx, d_cnt, d_off, n, st) != GDE_OK) { R.status = GDE_ENOMEM; return R; }
+    int total = 0;
+    DI_CK(cudaMemcpyAsync(&total, d_off + n, 4, cudaMemcpyDeviceToHost, st));
+    DI_CK(cudaStreamSynchronize(st));
+    int* d_be = (int*)ws("ins_be", (size_t)total * 4);
+    int* d_bo = (int*)ws("ins_bo", (size_t)total * 4);
+    int32_t* d_nbr = (int32_t*)ws("ins_nbr", (size_t)total * 4);
+    int64_t* d_pos = (int64_t*)ws("ins_pos", (size_t)total * 8);
+    int* d_flag = (int*)ws("ins_flag", n * 4);
+    int* d_kidx = (int*)ws("ins_kidx", (n + 1) * 4);
+    if (!d_be || !d_bo || !d_nbr || !d_pos || !d_flag || !d_kidx) {
+        R.status = gde_internal_fail(ctx, GDE_ENOMEM, "insertion scratch");
+        return R;
+    }
+    ins_fill_kernel<<<tb, kEdT, 0, st>>>(d_us, d_vs, k, d_state, d_off, d_fill, d_be, d_bo);
+    const bool ign = (kind == KIND_IGN);
+    ins_write_kernel<<<nwb, kEdT, 0, st>>>(G->g, G->col, G->row_len, G->degf, G->degd, ign ? G->nfac : nullptr,
+                                           G->tfac, G->tfac_f, ign ? G->pw1 : nullptr, G->pwb, n, d_cnt, d_off, d_be,
+                                           d_bo, d_nbr, d_pos);
+    ins_flags_kernel<<<nbk, kEdT, 0, st>>>(d_cnt, d_flag, n);
+    if (exclusive_scan(ctx, d_flag, d_kidx, n, st) != GDE_OK) { R.status = GDE_ENOMEM; return R; }
+    int nkeys = 0;
+    DI_CK(cudaMemcpyAsync(&nkeys, d_kidx + n, 4, cudaMemcpyDeviceToHost, st));
+    DI_CK(cudaStreamSynchronize(st));
+    int32_t* d_keys = (int32_t*)ws("ins_keys", (size_t)nkeys * 4);
+    RepairKey* d_rk = (RepairKey*)ws("ins_rkeys", (size_t)nkeys * sizeof(RepairKey));
+    if (!d_keys || !d_rk) {
+        R.status = gde_internal_fail(ctx, GDE_ENOMEM, "repair keys");
+        return R;
+    }
+    ins_keys_kernel<<<nbk, kEdT, 0, st>>>(d_cnt, d_kidx, n, d_keys);
+    if (nkeys > 0)
+        ins_repair_keys_kernel<<<(nkeys + kEdT - 1) / kEdT, kEdT, 0, st>>>(d_keys, nkeys, d_cnt, d_off, G->row_len,
+                                                                          kind, beta, G->pw1, G->pwb, d_rk);
+    DI_CK(cudaGetLastError());
+    // ---- the same edit on the caller's host arrays and the host mirror ----
+    std::vector<int64_t> hpos(total);
+    std::vector<int32_t> hval(total);
+    std::vector<int> hcnt(n);
+    DI_CK(cudaMemcpyAsync(hpos.data(), d_pos, (size_t)total * 8, cudaMemcpyDeviceToHost, st));
+    DI_CK(cudaMemcpyAsync(hval.data(), d_nbr, (size_t)total * 4, cudaMemcpyDeviceToHost, st));
+    DI_CK(cudaMemcpyAsync(hcnt.data(), d_cnt, n * 4, cudaMemcpyDeviceToHost, st));
+    DI_CK(cudaStreamSynchronize(st));
+#undef DI_CK
+    for (int i = 0; i < total; i++) h_indices[hpos[i]] = hval[i];
+    for (int64_t w = 0; w < n; w++) {
+        if (!hcnt[w]) continue;
+        h_degree[w] += hcnt[w];
+        G->h_len[w] = h_degree[w];
+        G->h_deg[w] = (double)h_degree[w];
+    }
+    G->g.vol += (double)total;
+    R.keys = d_keys;
+    R.nkeys = nkeys;
+    R.rkeys = d_rk;
+    R.nbr = d_nbr;
+    R.inserted = total / 2;
+    return R;
+}
+
 }  // namespace
 
 extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree,
@@ -151,6 +533,56 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
     for (int64_t u = 0; u < n; u++)
         if (h_degree[u] != hlen[u])
             return gde_internal_fail(ctx, GDE_EINVAL, "host degree array differs from the resident graph");
+    // ---- insert-only batches: the edit, the repair keys and the push all on the device ----
+    bool dev_ok = only_insert && k > 0 && G->deg_is_len;
+    for (int64_t e = 0; dev_ok && e < k; e++)
+        dev_ok = us[e] >= 0 && us[e] < n && vs[e] >= 0 && vs[e] < n && us[e] != vs[e];
+    if (dev_ok) {
+        if (kind == KIND_IGN) {
+            int rc0 = gde_internal_ign_tables(ctx, G, p->beta);
+            if (rc0 == GDE_OK) rc0 = ensure_power_tables(ctx, G, p->beta);
+            if (rc0 != GDE_OK) return rc0;
+        }
+        DeviceInsert D = device_insert(ctx, G, h_indices, h_degree, us, vs, k, kind, p->beta);
+        if (D.status != GDE_OK) return D.status;
+        if (!D.fallback) {
+            cudaStream_t st = gde_internal_stream(ctx);
+            const int prec64 = (p->prec == GDE_FP64);
+            if (D.nkeys > 0) {
+                const int64_t total = (int64_t)D.nkeys * F;
+                const int blocks = (int)((total + 255) / 256);
+                if (prec64) {
+                    repair_pass1<double><<<blocks, 256, 0, st>>>(D.rkeys, D.nkeys, (double*)Pm, (double*)Rm, ld, F,
+                                                                  kind, p->alpha);
+                    repair_pass2<double><<<blocks, 256, 0, st>>>(D.rkeys, D.nkeys, D.nbr, (const double*)Pm,
+                                                                  (double*)Rm, (const double*)Xm, ld, F, kind,
+                                                                  p->alpha, gde_internal_npush(G),
+                                                                  gde_internal_degd(G));
+                } else {
+                    repair_pass1<float><<<blocks, 256, 0, st>>>(D.rkeys, D.nkeys, (float*)Pm, (float*)Rm, ld, F,
+                                                                 kind, p->alpha);
+                    repair_pass2<float><<<blocks, 256, 0, st>>>(D.rkeys, D.nkeys, D.nbr, (const float*)Pm,
+                                                                 (float*)Rm, (const float*)Xm, ld, F, kind, p->alpha,
+                                                                 gde_internal_npush(G), gde_internal_degd(G));
+                }
+                cudaError_t e = cudaGetLastError();
+                if (e != cudaSuccess) return gde_internal_fail(ctx, GDE_ECUDA, cudaGetErrorString(e));
+            }
+            std::vector<double> opers(F, 0.0);
+            if (D.nkeys > 0) {
+                int rc = gde_internal_feature_push(ctx, G, p, F, Pm, Rm, ld, eps, D.keys, D.nkeys, opers.data(),
+                                                   stats);
+                if (rc != GDE_OK) return rc;
+            } else if (stats) {
+                memset(stats, 0, sizeof(*stats));
+            }
+            // the beta = 0 PPR update counts the repair work (ppr_solver.py:776-792)
+            const double oper_repair = 2.0 * (double)D.nkeys + 2.0 * (double)D.inserted;
+            if (oper_out)
+                for (int64_t c = 0; c < F; c++) oper_out[c] = opers[c] + (kind == KIND_UPPR ? oper_repair : 0.0);
+            return GDE_OK;
+        }
+    }
     std::vector<int64_t> old_degree(h_degree, h_degree + n);
     // ---- (1) sequential edit, InstantGNN.py:147-179 ----
     KeyMap ins, del;
