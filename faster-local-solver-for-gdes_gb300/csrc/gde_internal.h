@@ -59,6 +59,9 @@ struct gde_graph {
     double* pwb = nullptr;
     int64_t pw_max = -1;
     double pw_beta = NAN;
+    // greedy proper colouring (internal ids), built on first use by the LocalSOR engine
+    std::vector<int32_t> h_color;
+    int ncolors = 0;
     std::vector<int64_t> h_indptr;
     std::vector<int64_t> h_len;
     std::vector<double> h_deg;

@@ -42,44 +42,6 @@ namespace {
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
 constexpr unsigned kFull = 0xffffffffu;
-constexpr unsigned long long kSpinLimit = 1ull << 26;  // ~ seconds of polling
-
-// ---------------------------------------------------------------------------
-// Bounded grid barrier (sense by generation counter).  Co-residency of all
-// blocks is guaranteed by the cooperative launch; the spin limit only guards
-// against a bug turning into a hang: on expiry the block records GDE_EHANG
-// and every block leaves its loop at the next barrier.
-// ---------------------------------------------------------------------------
-__device__ __forceinline__ unsigned ld_volatile(const unsigned* p) { return *(volatile const unsigned*)p; }
-__device__ __forceinline__ int ld_volatile_i(const int* p) { return *(volatile const int*)p; }
-
-__device__ bool grid_barrier(GridBarrier* bar, int* err) {
-    __shared__ int s_ok;
-    __syncthreads();
-    if (threadIdx.x == 0) {
-        int ok = 1;
-        unsigned gen = ld_volatile(&bar->gen);
-        __threadfence();
-        unsigned arrived = atomicAdd(&bar->count, 1u);
-        if (arrived == gridDim.x - 1) {
-            atomicExch(&bar->count, 0u);
-            __threadfence();
-            atomicAdd(&bar->gen, 1u);
-        } else {
-            unsigned long long spins = 0;
-            while (ld_volatile(&bar->gen) == gen) {
-                if (ld_volatile_i(err) != 0) { ok = 0; break; }
-                if (++spins > kSpinLimit) { atomicCAS(err, 0, GDE_EHANG); ok = 0; break; }
-                __nanosleep(100);
-            }
-        }
-        __threadfence();
-        if (ld_volatile_i(err) != 0) ok = 0;
-        s_ok = ok;
-    }
-    __syncthreads();
-    return s_ok != 0;
-}
 
 // ---------------------------------------------------------------------------
 // Threshold test r >= theta * d without FP64 arithmetic in the common case.

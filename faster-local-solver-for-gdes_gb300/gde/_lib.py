@@ -65,6 +65,9 @@ SIGNATURES = {
     "gde_plain_ppr_local": (_int, [_p, _p, _i32, _dbl, _dbl, _p, _p, _p, _p]),
     "gde_serve_mixed": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _p, _p, _p, _dbl, _p, _int, _int, _i64,
                                _p, _p, _p, ctypes.POINTER(Stats)]),
+    "gde_sor": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _int, _p, _p, _int, _int, _i64, _p, _p,
+                       ctypes.POINTER(Stats)]),
+    "gde_graph_colors": (_int, [_p, _p, _p]),
     "gde_katz_spectral_bounds": (_int, [_p, _p, _dbl, _int, _dbl, _p, _p, _p, _p]),
     "gde_ctx_trace": (_int, [_p, _int]),
     "gde_ctx_trace_read": (_int, [_p, _p, _i64, _p, _p, _p]),

@@ -219,6 +219,39 @@ def serve_mixed(graph: Graph, kinds, seeds, eps, *, alphas=None, tau: float = 0.
     return {"x": x_out if want_x else None, "oper": oper, "rounds": rounds, "latency_ms": lat, "stats": st.as_dict()}
 
 
+def sor(graph: Graph, kind: int, seeds, eps, *, omega: float, local: bool = True, alpha: float = 0.0,
+        prec: str = "fp64", out64: bool | None = None, want_x: bool = True, want_r: bool = True,
+        device_out: bool = False, max_sweeps: int = 0) -> dict:
+    """Multicolour LocalSOR / global SOR (ppr_sor / katz_sor order on the GPU); dict(x, r, oper, sweeps, stats)."""
+    lib = L.load()
+    seeds = np.ascontiguousarray(np.atleast_1d(seeds), dtype=np.int32)
+    nq = seeds.shape[0]
+    eps = np.ascontiguousarray(np.broadcast_to(np.asarray(eps, dtype=np.float64), (nq,)))
+    if out64 is None:
+        out64 = prec == "fp64"
+    n = graph.n
+    x_out = _alloc((nq, n), out64, device_out, graph) if want_x else None
+    r_out = _alloc((nq, n), out64, device_out, graph) if want_r else None
+    oper = np.zeros(nq, dtype=np.float64)
+    sweeps = np.zeros(nq, dtype=np.int32)
+    p = make_params(kind, L.LOCAL_GD, prec, 1, alpha, omega=omega, max_rounds=max_sweeps)
+    st = L.Stats()
+    status = lib.gde_sor(graph.ctx.ptr, graph.ptr, ctypes.byref(p), nq, _ptr(seeds), _ptr(eps), int(local),
+                         _ptr(x_out), _ptr(r_out), int(out64), L.MEM_DEVICE if device_out else L.MEM_HOST, n,
+                         _ptr(oper), _ptr(sweeps), ctypes.byref(st))
+    L.check(graph.ctx.ptr, status, "gde_sor")
+    return {"x": x_out, "r": r_out, "oper": oper, "sweeps": sweeps, "stats": st.as_dict()}
+
+
+def graph_colors(graph: Graph) -> np.ndarray:
+    """The proper colouring gde_sor uses, per caller node id."""
+    lib = L.load()
+    out = np.zeros(graph.n, dtype=np.int32)
+    nc = ctypes.c_int32()
+    L.check(graph.ctx.ptr, lib.gde_graph_colors(graph.ptr, _ptr(out), ctypes.byref(nc)), "gde_graph_colors")
+    return out
+
+
 def katz_spectral_bounds(graph: Graph, alpha: float, max_iter: int = 400, tol: float = 1e-10) -> dict:
     """lambda_max / lambda_min of the adjacency (GPU Lanczos) and the Katz Chebyshev bounds l_max, mu_min."""
     lib = L.load()

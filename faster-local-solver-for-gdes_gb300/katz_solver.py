@@ -15,7 +15,7 @@ from gde import api
 from gde.dropin import Timer, graph_for, oper_like
 
 __all__ = ["katz_gd", "katz_gd_local_gpu", "katz_gd_standard_gpu", "katz_cheby", "solve_a_graph_gpu",
-           "solve_a_graph_cheby", "katz_spectral_bounds"]
+           "solve_a_graph_cheby", "katz_sor", "katz_spectral_bounds"]
 
 
 def _solve1(n, indptr, indices, degree, s_node, alpha, eps, method, prec, l_max=0.0, mu_min=0.0):
@@ -94,3 +94,16 @@ def katz_spectral_bounds(n, indptr, indices, degree, alpha):
     assert g.n == n, "n must equal len(indptr) - 1"
     b = api.katz_spectral_bounds(g, alpha)
     return b["l_max"], b["mu_min"], b["lam_max"], b["lam_min"]
+
+
+def katz_sor(n, indptr, indices, degree, s_node, alpha, eps, omega, local):
+    """LocalSOR / global SOR for Katz (katz_solver.py:251-337) -> (xt, rt, oper, algo_time).
+
+    Multicolour Gauss-Seidel order on the GPU (see ``ppr_solver.ppr_sor``);
+    the returned xt has xt[s_node] -= 1 like the reference's.
+    """
+    g = graph_for(indptr, indices, degree)
+    assert g.n == n, "n must equal len(indptr) - 1"
+    with Timer() as t:
+        r = api.sor(g, L.KATZ, [s_node], [eps], omega=omega, local=local, alpha=alpha, prec="fp64")
+    return r["x"][0], r["r"][0], oper_like(degree, r["oper"][0]), t.dt

@@ -16,8 +16,8 @@ from gde import _lib as L
 from gde import api
 from gde.dropin import Timer, graph_for, oper_like
 
-__all__ = ["ppr_gd", "ppr_gd_local_gpu", "ppr_gd_standard_gpu", "ppr_cheby", "ppr_gd_torch", "solve_a_graph_gpu",
-           "solve_a_graph_cheby", "solve_a_graph_torch", "update_ppr_parallel", "optimal_omega"]
+__all__ = ["ppr_gd", "ppr_gd_local_gpu", "ppr_gd_standard_gpu", "ppr_cheby", "ppr_sor", "ppr_gd_torch",
+           "solve_a_graph_gpu", "solve_a_graph_cheby", "solve_a_graph_torch", "update_ppr_parallel", "optimal_omega"]
 
 
 def _solve1(n, indptr, indices, degree, s_node, alpha, eps, method, prec):
@@ -60,6 +60,21 @@ def ppr_cheby(n, indptr, indices, degree, s_node, alpha, eps, local):
         x, r, oper = _solve1(n, indptr, indices, degree, s_node, alpha, eps,
                              L.LOCAL_CHEBY if local else L.GLOBAL_CHEBY, "fp64")
     return x, r, oper_like(degree, oper), t.dt
+
+
+def ppr_sor(n, indptr, indices, degree, s_node, alpha, eps, omega, local, opt_x=None, debug=False):
+    """LocalSOR / global SOR (ppr_solver.py:331-461) -> (xt, rt, oper, algo_time).
+
+    Same relaxation and stopping rule as the reference; the GPU relaxes in
+    multicolour Gauss-Seidel order (all pending nodes of one colour at once)
+    instead of the reference's FIFO queue, so ``oper`` is that order's count.
+    """
+    assert eps * degree[s_node] <= 1.
+    g = graph_for(indptr, indices, degree)
+    assert g.n == n, "n must equal len(indptr) - 1"
+    with Timer() as t:
+        r = api.sor(g, L.PPR, [s_node], [eps], omega=omega, local=local, alpha=alpha, prec="fp64")
+    return r["x"][0], r["r"][0], oper_like(degree, r["oper"][0]), t.dt
 
 
 def ppr_gd_torch(adj_mat, n, degree, deg_mat, alpha, eps, s_node, device):

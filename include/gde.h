@@ -183,6 +183,26 @@ int gde_serve_mixed(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t nq,
                     double hbm_budget_bytes, void *x_out, int out64, int out_mem, int64_t ld_out, double *oper_out,
                     int32_t *rounds_out, float *lat_ms_out, gde_stats *stats);
 
+/* ---- LocalSOR / APPR (ppr_sor, katz_sor) in multicolour order ----
+ * Relaxation res = omega r_u, x_u += res, r_u -= res, push (1-alpha) res / d_u
+ * (Katz: alpha res) as in ppr_sor (ppr_solver.py:331-461) / katz_sor
+ * (katz_solver.py:251-337), in a Gauss-Seidel order the GPU can run in
+ * parallel: sweeps over the colours of a greedy proper colouring (internal
+ * degree-descending order), all pending nodes of one colour relaxing together.
+ * A node is pending when an addition or its own update leaves |r_v| >=
+ * eps_vec[v]; local = 1 stops after a sweep that leaves nothing pending,
+ * local = 0 relaxes every node each sweep and stops when no node is at or
+ * above threshold (oper += n + m per sweep).  The order differs from the
+ * reference's FIFO queue, so operation counts differ from its (both meet the
+ * same stopping rule).  p->kind GDE_PPR / GDE_KATZ, p->omega in (0, 2),
+ * p->max_rounds caps the sweeps.  Outputs dense [nq][n] (ld_out = n). */
+int gde_sor(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t nq, const int32_t *seeds, const double *eps,
+            int local, void *x_out, void *r_out, int out64, int out_mem, int64_t ld_out, double *oper_out,
+            int32_t *sweeps_out, gde_stats *stats);
+/* The colouring gde_sor uses, per caller node id (host colors_out[n], may be
+ * NULL), and the number of colours. */
+int gde_graph_colors(gde_graph *g, int32_t *colors_out, int32_t *ncolors);
+
 /* ---- Katz Chebyshev spectral bounds ----
  * lambda_max(A) and lambda_min(A) of the graph's adjacency by a Lanczos
  * iteration on the GPU (FP64), the quantities katz_exp_dmax.py:20 and

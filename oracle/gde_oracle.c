@@ -404,6 +404,119 @@ double orc_sor(i64 n, const i64 *indptr, const i32 *indices, const double *degre
 }
 
 /* ------------------------------------------------------------------------ */
+/* Multicolour local / global SOR: the parallel order of the GPU LocalSOR.   */
+/* The update of a node is ppr_sor's (ppr_solver.py:390-402; katz_sor,       */
+/* katz_solver.py:296-310): res = omega r_u, x_u += res, r_u -= res, push    */
+/* (1-alpha) res / d_u (Katz: alpha res) to every neighbour.  The order is   */
+/* a sweep over colours c = 0..C-1 of a proper colouring; in colour c's      */
+/* phase every pending node of colour c with |r_u| >= eps_vec[u] relaxes.   */
+/* Same-coloured nodes are not adjacent, so a phase equals a sequential     */
+/* Gauss-Seidel pass over them in any order.  A node becomes pending when   */
+/* an addition leaves |r_v| >= eps_vec[v] (the reference's enqueue test,    */
+/* :398-401), or when its own update leaves it there (:402-405); it is      */
+/* processed at the next phase of its colour.  Local stops after a sweep    */
+/* that leaves nothing pending; global relaxes every node of each colour    */
+/* and stops after a sweep with no node at or above threshold (:452-457).   */
+/* ------------------------------------------------------------------------ */
+double orc_sor_color(i64 n, const i64 *indptr, const i32 *indices, const double *degree, i64 s, double alpha,
+                     double eps, double omega, int local, int katz, const i32 *color, i64 ncolors, double *xt,
+                     double *rt, i64 *sweeps_out) {
+    double *eps_vec = (double *)malloc((size_t)n * sizeof(double));
+    double m = 0.0, oper = 0.;
+    for (i64 i = 0; i < n; i++) m += degree[i];
+    memset(xt, 0, (size_t)n * sizeof(double));
+    memset(rt, 0, (size_t)n * sizeof(double));
+    rt[s] = katz ? 1.0 : alpha;
+    for (i64 i = 0; i < n; i++) eps_vec[i] = katz ? eps * degree[i] : eps * alpha * degree[i];
+    /* nodes of each colour, in node order */
+    i64 *cstart = (i64 *)calloc((size_t)ncolors + 1, sizeof(i64));
+    i64 *corder = (i64 *)malloc((size_t)(n > 0 ? n : 1) * sizeof(i64));
+    for (i64 i = 0; i < n; i++) cstart[color[i] + 1]++;
+    for (i64 c = 0; c < ncolors; c++) cstart[c + 1] += cstart[c];
+    {
+        i64 *fill = (i64 *)calloc((size_t)ncolors, sizeof(i64));
+        for (i64 i = 0; i < n; i++) corder[cstart[color[i]] + fill[color[i]]++] = i;
+        free(fill);
+    }
+    i64 sweeps = 0;
+    if (local) {
+        /* pending lists per colour (capacity: the colour's node count) */
+        i64 *plist = (i64 *)malloc((size_t)(n > 0 ? n : 1) * sizeof(i64));
+        i64 *pcnt = (i64 *)calloc((size_t)ncolors, sizeof(i64));
+        i64 *cur = (i64 *)malloc((size_t)(n > 0 ? n : 1) * sizeof(i64));
+        unsigned char *mark = (unsigned char *)calloc((size_t)(n > 0 ? n : 1), 1);
+        plist[cstart[color[s]]] = s;
+        pcnt[color[s]] = 1;
+        mark[s] = 1;
+        for (;;) {
+            i64 pend = 0;
+            for (i64 c = 0; c < ncolors; c++) pend += pcnt[c];
+            if (pend == 0) break;
+            sweeps++;
+            for (i64 c = 0; c < ncolors; c++) {
+                i64 k = pcnt[c];
+                if (k == 0) continue;
+                memcpy(cur, plist + cstart[c], (size_t)k * sizeof(i64));
+                pcnt[c] = 0;
+                for (i64 i = 0; i < k; i++) mark[cur[i]] = 0;
+                for (i64 i = 0; i < k; i++) {
+                    i64 u = cur[i];
+                    if (eps_vec[u] > fabs(rt[u])) continue;
+                    oper += degree[u];
+                    double res = omega * rt[u];
+                    xt[u] += res;
+                    rt[u] -= res;
+                    double push_res = katz ? alpha * res : (1. - alpha) * res / degree[u];
+                    i64 end = katz ? indptr[u + 1] : indptr[u] + (i64)degree[u];
+                    for (i64 j = indptr[u]; j < end; j++) {
+                        i64 v = indices[j];
+                        rt[v] += push_res;
+                        if (!mark[v] && eps_vec[v] <= fabs(rt[v])) {
+                            mark[v] = 1;
+                            plist[cstart[color[v]] + pcnt[color[v]]++] = v;
+                        }
+                    }
+                    if (!mark[u] && eps_vec[u] <= fabs(rt[u])) {
+                        mark[u] = 1;
+                        plist[cstart[c] + pcnt[c]++] = u;
+                    }
+                }
+            }
+        }
+        free(plist);
+        free(pcnt);
+        free(cur);
+        free(mark);
+    } else {
+        for (;;) {
+            sweeps++;
+            for (i64 c = 0; c < ncolors; c++) {
+                for (i64 i = cstart[c]; i < cstart[c + 1]; i++) {
+                    i64 u = corder[i];
+                    double res = omega * rt[u];
+                    if (res == 0.0) continue;
+                    xt[u] += res;
+                    rt[u] -= res;
+                    double push_res = katz ? alpha * res : (1. - alpha) * res / degree[u];
+                    i64 end = katz ? indptr[u + 1] : indptr[u] + (i64)degree[u];
+                    for (i64 j = indptr[u]; j < end; j++) rt[indices[j]] += push_res;
+                }
+            }
+            oper += (double)n + m;
+            i64 cnt = 0;
+            for (i64 i = 0; i < n; i++) cnt += (eps_vec[i] <= fabs(rt[i]));
+            if (cnt <= 0) break;
+        }
+    }
+    if (katz) xt[s] -= 1.;
+    if (sweeps_out) *sweeps_out = sweeps;
+    free(eps_vec);
+    free(cstart);
+    free(corder);
+    return oper;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Heat kernel (hk_solver.py:15-80, :206-295)                                */
 /* ------------------------------------------------------------------------ */
 static double est_coef(double t, i64 k) { /* estimate_coefficient, :15-25 */

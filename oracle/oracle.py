@@ -52,6 +52,8 @@ def lib():
         L.orc_katz_gd.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _int, _p, _p]
         L.orc_sor.restype = _dbl
         L.orc_sor.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _dbl, _int, _int, _p, _p]
+        L.orc_sor_color.restype = _dbl
+        L.orc_sor_color.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _dbl, _int, _int, _p, _i64, _p, _p, _p]
         L.orc_hk_estimate_n.restype = _i64
         L.orc_hk_estimate_n.argtypes = [_dbl, _dbl]
         L.orc_hk_sor_queue.restype = _dbl
@@ -126,6 +128,32 @@ def sor(n, indptr, indices, degree, s, alpha, eps, omega, local, katz=False):
     oper = lib().orc_sor(n, _ptr(indptr), _ptr(indices), _ptr(degree), int(s), alpha, eps, omega, int(local),
                          int(katz), _ptr(x), _ptr(r))
     return x, r, float(oper)
+
+
+def sor_color(n, indptr, indices, degree, s, alpha, eps, omega, local, colors, katz=False):
+    """Multicolour local/global SOR (the GPU LocalSOR order) -> (x, r, oper, sweeps)."""
+    indptr, indices, degree = _graph(indptr, indices, degree)
+    colors = np.ascontiguousarray(colors, dtype=np.int32)
+    x = np.zeros(n)
+    r = np.zeros(n)
+    sw = ctypes.c_int64()
+    oper = lib().orc_sor_color(n, _ptr(indptr), _ptr(indices), _ptr(degree), int(s), alpha, eps, omega, int(local),
+                               int(katz), _ptr(colors), int(colors.max()) + 1 if colors.size else 0, _ptr(x), _ptr(r),
+                               ctypes.byref(sw))
+    return x, r, float(oper), int(sw.value)
+
+
+def greedy_colors(indptr, indices, order):
+    """Greedy proper colouring visiting nodes in ``order`` (smallest colour not used by a coloured neighbour)."""
+    n = len(indptr) - 1
+    col = np.full(n, -1, dtype=np.int32)
+    for u in order:
+        used = {int(col[v]) for v in indices[indptr[u]:indptr[u + 1]] if col[v] >= 0}
+        c = 0
+        while c in used:
+            c += 1
+        col[u] = c
+    return col
 
 
 def hk_estimate_n(t, eps):

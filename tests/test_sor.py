@@ -1,0 +1,109 @@
+"""GPU LocalSOR / global SOR (multicolour order) against the oracle's restatement.
+
+``oracle.sor_color`` runs the same multicolour Gauss-Seidel order
+sequentially on the CPU in FP64, given the colouring the GPU uses; the GPU
+must reproduce its operation counts and sweeps exactly and its solution to
+1e-12 (only the order of additions at a target differs).  The colouring is
+a proper colouring and equals greedy colouring in degree-descending order.
+"""
+import numpy as np
+import pytest
+
+from gde import _lib as L
+from gde import api, graphs
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+FP64_L1 = 1e-12
+
+
+@pytest.fixture(scope="module")
+def cl():
+    g = graphs.chung_lu(3000, 2.1, 8.0, 300.0, seed=3)
+    return g, api.Graph(g.indptr, g.indices)
+
+
+def rel_l1(a, b):
+    return np.abs(np.asarray(a, np.float64) - b).sum() / max(np.abs(b).sum(), 1e-300)
+
+
+def test_colouring_is_proper_and_greedy(cl):
+    g, Gd = cl
+    col = api.graph_colors(Gd)
+    src = np.repeat(np.arange(g.n), np.diff(g.indptr))
+    assert (col[src] != col[g.indices]).all()
+    order = np.argsort(-np.diff(g.indptr), kind="stable")
+    np.testing.assert_array_equal(col, O.greedy_colors(g.indptr, g.indices, order))
+
+
+@pytest.mark.parametrize("omega", [1.0, 1.3, 1.7])
+@pytest.mark.parametrize("local", [True, False])
+def test_ppr_sor_fp64_matches_oracle(cl, omega, local):
+    g, Gd = cl
+    deg = g.degree.astype(np.float64)
+    col = api.graph_colors(Gd)
+    seeds = graphs.uniform_seeds(g, 4, seed=12)
+    eps = 1e-6 if local else 1e-5
+    res = api.sor(Gd, L.PPR, seeds, eps, omega=omega, local=local, alpha=0.1)
+    for i, s in enumerate(seeds):
+        xo, ro, oo, so = O.sor_color(g.n, g.indptr, g.indices, deg, int(s), 0.1, eps, omega, local, col)
+        assert res["oper"][i] == pytest.approx(oo, rel=1e-12), (i, res["oper"][i], oo)
+        assert res["sweeps"][i] == so
+        assert rel_l1(res["x"][i], xo) < FP64_L1
+        assert np.abs(res["r"][i] - ro).sum() < 1e-12
+
+
+def test_katz_sor_fp64_matches_oracle(cl):
+    g, Gd = cl
+    deg = g.degree.astype(np.float64)
+    col = api.graph_colors(Gd)
+    alpha = 1.0 / (float(g.degree.max()) + 1.0)
+    seeds = graphs.uniform_seeds(g, 3, seed=13)
+    res = api.sor(Gd, L.KATZ, seeds, 1e-6, omega=1.2, local=True, alpha=alpha)
+    for i, s in enumerate(seeds):
+        xo, _, oo, so = O.sor_color(g.n, g.indptr, g.indices, deg, int(s), alpha, 1e-6, 1.2, True, col, katz=True)
+        assert res["oper"][i] == pytest.approx(oo, rel=1e-12)
+        assert rel_l1(res["x"][i], xo) < FP64_L1
+
+
+def test_sor_converges_like_the_reference_order(cl):
+    """Multicolour order vs the reference's FIFO order: same stopping rule, similar work and error."""
+    g, Gd = cl
+    deg = g.degree.astype(np.float64)
+    s = int(graphs.uniform_seeds(g, 1, seed=14)[0])
+    truth = O.global_solve_ppr(g.indptr, g.indices, deg, s, 0.1)
+    res = api.sor(Gd, L.PPR, [s], 1e-6, omega=1.3, local=True, alpha=0.1)
+    xf, _, of = O.sor(g.n, g.indptr, g.indices, deg, s, 0.1, 1e-6, 1.3, True)
+    err_gpu = np.abs(res["x"][0] - truth).sum()
+    err_fifo = np.abs(xf - truth).sum()
+    assert err_gpu < 2 * err_fifo + 1e-9
+    assert 0.5 * of < res["oper"][0] < 2 * of
+    # every residual is below its threshold at the end
+    assert (np.abs(res["r"][0]) < 1e-6 * 0.1 * deg).all()
+
+
+def test_sor_batched_equals_single(cl):
+    g, Gd = cl
+    seeds = graphs.uniform_seeds(g, 6, seed=15)
+    eps = np.array([1e-5, 1e-6, 3e-6, 1e-5, 2e-6, 1e-6])
+    both = api.sor(Gd, L.PPR, seeds, eps, omega=1.4, local=True, alpha=0.1)
+    for i in (0, 3, 5):
+        one = api.sor(Gd, L.PPR, seeds[i:i + 1], eps[i:i + 1], omega=1.4, local=True, alpha=0.1)
+        assert one["oper"][0] == pytest.approx(both["oper"][i], rel=1e-12)
+        assert rel_l1(both["x"][i], one["x"][0]) < FP64_L1
+
+
+def test_sor_fp32(cl):
+    g, Gd = cl
+    deg = g.degree.astype(np.float64)
+    col = api.graph_colors(Gd)
+    seeds = graphs.uniform_seeds(g, 6, seed=16)
+    res = api.sor(Gd, L.PPR, seeds, 1e-6, omega=1.3, local=True, alpha=0.1, prec="fp32")
+    errs = []
+    for i, s in enumerate(seeds):
+        xo, _, oo, _ = O.sor_color(g.n, g.indptr, g.indices, deg, int(s), 0.1, 1e-6, 1.3, True, col)
+        errs.append(rel_l1(res["x"][i], xo))
+        assert errs[-1] < 2e-6 + 6 * 1e-7 * float(g.degree.max())
+        assert abs(res["oper"][i] - oo) <= 1e-2 * oo
+    assert np.mean(errs) < 1e-5
