@@ -293,6 +293,8 @@ int upload_degrees(gde_ctx* ctx, gde_graph* G) {
     return GDE_OK;
 }
 
+constexpr int64_t kHubLen = 64;  // rows longer than this are hubs (warp-combined atomics)
+
 // Static graphs: node records {row start, length, degree} and, when every
 // degree is an exact integer, column words carrying the target's degree in
 // the bits above the node id.  A graph that is edited later never gets them.
@@ -864,7 +866,7 @@ int gde_graph_upload(gde_ctx* ctx, int64_t n, int64_t cap, const int64_t* indptr
     // pushes into them are combined per warp before the atomic
     G->g.hub_cut = 0;
     if (G->relabeled)
-        while (G->g.hub_cut < n && G->h_len[G->g.hub_cut] > 64) G->g.hub_cut++;
+        while (G->g.hub_cut < n && G->h_len[G->g.hub_cut] > kHubLen) G->g.hub_cut++;
     G->g.row_ptr = G->row_ptr;
     G->g.col = G->col;
     G->g.row_len = G->row_len;

@@ -297,19 +297,25 @@ __global__ void sor_seed_kernel(SorArgs a, const int32_t* seeds, int prec64) {
     }
 }
 
-// Greedy proper colouring in internal node order (degree-descending for
-// static graphs): each node takes the smallest colour no earlier neighbour has.
+// Greedy proper colouring visiting nodes by descending degree (ties by
+// caller id): each node takes the smallest colour no earlier neighbour has.
 int build_colors(gde_graph* G) {
     const int64_t n = G->g.n;
     std::vector<int32_t> col(n, -1);
     std::vector<int64_t> seen;  // colour -> last node that saw it among its neighbours
     int C = 0;
+    std::vector<int32_t> order(n);  // caller ids by descending degree (stable)
+    for (int64_t u = 0; u < n; u++) order[u] = (int32_t)u;
+    std::stable_sort(order.begin(), order.end(), [&](int32_t a, int32_t b) {
+        return G->h_len[G->node_in(a)] > G->h_len[G->node_in(b)];
+    });
     // the adjacency in internal ids, from the resident graph
     std::vector<int32_t> h_col_idx(std::max<int64_t>(G->g.cap, 1));
     if (G->g.cap > 0 &&
         cudaMemcpy(h_col_idx.data(), G->col, G->g.cap * sizeof(int32_t), cudaMemcpyDeviceToHost) != cudaSuccess)
         return -1;
-    for (int64_t u = 0; u < n; u++) {
+    for (int64_t k = 0; k < n; k++) {
+        const int64_t u = G->node_in(order[k]);
         const int64_t rp = G->h_indptr[u];
         const int64_t len = G->h_len[u];
         for (int64_t j = rp; j < rp + len; j++) {
