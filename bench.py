@@ -170,6 +170,25 @@ def cpu_baseline(g, n_queries: int, eps: float):
     return n_queries / dt, threads, n_queries, dt
 
 
+def accuracy_vs_oracle(G, g, tuning, n_queries: int = 8):
+    """FP32 served results against the FP64 oracle on a few of the workload's queries (outside any timing)."""
+    from gde import _lib as L
+    from gde import api, graphs
+    from oracle import oracle as O
+    seeds = graphs.uniform_seeds(g, n_queries, seed=515151)
+    deg = g.degree.astype(np.float64)
+    oper_o, x_o = O.ppr_gd_many(g.n, g.indptr, g.indices, deg, seeds, ALPHA, EPS, local=True, keep_x=True)
+    res = api.solve(G, L.PPR, L.LOCAL_GD, seeds, EPS, prec="fp32", alpha=ALPHA, tile_w=1, want_r=False,
+                    tuning=tuning)
+    rel = [float(np.abs(res["x"][i] - x_o[i]).sum() / np.abs(x_o[i]).sum()) for i in range(n_queries)]
+    absl1 = [float(np.abs(res["x"][i] - x_o[i]).sum()) for i in range(n_queries)]
+    od = [abs(float(res["oper"][i]) - float(oper_o[i])) / float(oper_o[i]) for i in range(n_queries)]
+    return {"vs": "FP64 oracle (C port of ppr_gd local)", "queries": n_queries, "eps": EPS,
+            "l1_mean": float(np.mean(absl1)), "l1_max": float(np.max(absl1)),
+            "rel_l1_mean": float(np.mean(rel)), "rel_l1_max": float(np.max(rel)),
+            "oper_rel_diff_max": float(np.max(od))}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -339,6 +358,7 @@ def run_ours(args):
         qps, threads, nq, dt = cpu_baseline(g, args.cpu_queries, EPS)
         out["cpu_baseline"] = {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
                                "sample": f"{nq} queries (ppr_gd local FP64, one per OpenMP thread), {dt:.1f} s"}
+        out["accuracy"] = accuracy_vs_oracle(G, g, tuning)
     print(json.dumps(out), flush=True)
     if world > 1:
         torch.distributed.barrier()

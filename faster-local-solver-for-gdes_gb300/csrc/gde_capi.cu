@@ -24,6 +24,11 @@ using namespace gde;
 
 #include "gde_internal.h"
 
+// sor_engine.cu: the InstantGNN push with relaxation omega != 1
+int gde_internal_sor_feature_push(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t F, void* Pm, void* Rm,
+                                  int64_t ld, double eps, const int32_t* d_cand, int64_t ncand, double* oper_out,
+                                  gde_stats* stats);
+
 
 
 namespace {
@@ -1186,6 +1191,19 @@ static int feature_push_impl(gde_ctx* ctx, gde_graph* G, const gde_params* p, in
     if (kind == KIND_IGN && (std::isnan(G->ign_beta) || G->ign_beta != p->beta)) {
         int rc = upload_ign_tables(ctx, G, p->beta);
         if (rc != GDE_OK) return rc;
+    }
+    if (kind == KIND_IGN && p->omega != 0.0 && p->omega != 1.0) {
+        // relaxation omega != 1: instantGNNSorPush order on the GPU (multicolour SOR)
+        if (G->relabeled) return fail(ctx, GDE_EINVAL, "the SOR feature push runs on padded (row_len) graphs");
+        const int32_t* dc = cand;
+        if (cand && !cand_on_device) {
+            int32_t* d = (int32_t*)wsget(ctx, "sor_cand", std::max<int64_t>(ncand, 1) * 4);
+            if (!d) return fail(ctx, GDE_ENOMEM, "candidate list");
+            CK(cudaMemcpyAsync(d, cand, ncand * 4, cudaMemcpyHostToDevice, ctx->stream));
+            dc = d;
+        }
+        G->g.nfac = G->nfac;
+        return gde_internal_sor_feature_push(ctx, G, p, F, Pm, Rm, ld, eps, dc, ncand, oper_out, stats);
     }
     int W = p->tile_w;
     if (W <= 0) W = prec64 ? 8 : 16;

@@ -49,6 +49,7 @@ struct SorArgs {
     int ncolors;
     int local;
     int katz;
+    int ign;                 // InstantGNN columns: thresholds eps d^(1-beta), target scale d^-beta
     double alpha, omega;
     const int32_t* color;    // [n] internal ids
     const int32_t* corder;   // [n] nodes sorted by colour
@@ -116,8 +117,30 @@ __device__ void relax_phase(const SorArgs& a, int q, int c, int p, int it) {
             if (a.local) mark[u] = 0;
             const T r = R[u];
             const double d = a.g.degd[u];
-            act = a.local ? at_or_above(r, theta, d) : (r != T(0));
-            if (act) {
+            const double tf = a.ign ? a.g.nfac[u] : d;  // threshold factor: d, or d^(1-beta)
+            act = a.local ? at_or_above(r, theta, tf) : (r != T(0));
+            if (act && a.ign) {
+                const int64_t rp = a.g.row_ptr[u];
+                const int len = a.g.row_len[u];
+                if (len == 0 || (len == 1 && a.g.col[rp] == u)) {
+                    // absorbing node: p = r, r = 0 (InstantGNN.py:81-84)
+                    X[u] = (double)r;
+                    R[u] = T(0);
+                    act = false;
+                } else {
+                    // InstantGNN.py:85-88
+                    const double res = a.omega * (double)r;
+                    X[u] += a.alpha * res;
+                    const T rn = (T)((1 - a.omega) * (double)r);
+                    R[u] = rn;
+                    push = (T)(((1. - a.alpha) * res) / a.g.npush[u]);
+                    my_oper += d;
+                    if (at_or_above(rn, theta, tf)) {  // :94-97
+                        mark[u] = 1;
+                        push_pending(a, q, p ^ 1, u, c);
+                    }
+                }
+            } else if (act) {
                 // ppr_solver.py:390-395 / katz_solver.py:296-301
                 const double res = a.omega * (double)r;
                 X[u] += res;
@@ -164,10 +187,13 @@ __device__ void push_phase(const SorArgs& a, int q, int c, int p, int it) {
         const int len = a.katz ? (int)(a.g.row_ptr[u + 1] - rp) : a.g.row_len[u];
         for (int j = lane; j < len; j += 32) {
             const int v = a.g.col[rp + j];
-            const T old = atomicAdd(R + v, val);
+            // InstantGNN divides by d_v^beta at the target (InstantGNN.py:90)
+            const T add = a.ign ? (T)((double)val / a.g.tfac[v]) : val;
+            const T old = atomicAdd(R + v, add);
             if (a.local) {
-                const T now = old + val;
-                if (at_or_above(now, theta, a.g.degd[v]) && mark[v] == 0 && atomicExch(&mark[v], 1) == 0) {
+                const T now = old + add;
+                const double tf = a.ign ? a.g.nfac[v] : a.g.degd[v];
+                if (at_or_above(now, theta, tf) && mark[v] == 0 && atomicExch(&mark[v], 1) == 0) {
                     const int cv = a.color[v];
                     push_pending(a, q, (cv > c) ? p : (p ^ 1), v, cv);
                 }
@@ -297,6 +323,37 @@ __global__ void sor_seed_kernel(SorArgs a, const int32_t* seeds, int prec64) {
     }
 }
 
+// Feature columns: every candidate at or above its threshold starts pending.
+template <typename T>
+__global__ void sor_seed_cand_kernel(SorArgs a, const int32_t* cand, int64_t ncand) {
+    const int64_t n = a.g.n;
+    const int64_t total = (int64_t)a.nq * ncand;
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += (int64_t)gridDim.x * blockDim.x) {
+        const int q = (int)(i / ncand);
+        const int64_t k = i % ncand;
+        const int u = cand ? cand[k] : (int)k;
+        const T r = reinterpret_cast<const T*>(a.R)[(int64_t)q * n + u];
+        if (!at_or_above(r, a.theta[q], a.g.nfac[u])) continue;
+        if (atomicExch(&a.mark[(int64_t)q * n + u], 1) == 0) push_pending(a, q, 0, u, a.color[u]);
+    }
+}
+
+// node-major caller matrix [n][ld] <-> per-column slabs [F][n]
+template <typename T, typename S>
+__global__ void sor_gather_kernel(const T* M, int64_t ld, int64_t F, int64_t n, S* slab) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * F; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = i / F, q = i % F;
+        slab[q * n + u] = (S)M[u * ld + q];
+    }
+}
+template <typename T, typename S>
+__global__ void sor_scatter_kernel(const S* slab, int64_t ld, int64_t F, int64_t n, T* M) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * F; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t u = i / F, q = i % F;
+        M[u * ld + q] = (T)slab[q * n + u];
+    }
+}
+
 // Greedy proper colouring visiting nodes by descending degree (ties by
 // caller id): each node takes the smallest colour no earlier neighbour has.
 int build_colors(gde_graph* G) {
@@ -337,6 +394,110 @@ int build_colors(gde_graph* G) {
 
 }  // namespace
 
+#define SO_CK(call)                                                                       \
+    do {                                                                                  \
+        cudaError_t e__ = (call);                                                         \
+        if (e__ != cudaSuccess) {                                                         \
+            std::string m__ = std::string(#call) + ": " + cudaGetErrorString(e__);       \
+            return gde_internal_fail(ctx, GDE_ECUDA, m__.c_str());                        \
+        }                                                                                 \
+    } while (0)
+
+namespace {
+
+// Workspace, colouring and per-query state of a SOR launch over nq vectors.
+int sor_prepare(gde_ctx* ctx, gde_graph* G, int64_t nq, int prec64, const std::vector<double>& theta, SorArgs& a) {
+    const int64_t n = G->g.n;
+    cudaStream_t st = ctx->stream;
+    if (G->ncolors <= 0 && build_colors(G) < 0) return gde_internal_fail(ctx, GDE_ECUDA, "reading the graph for colouring");
+    const int C = G->ncolors;
+    std::vector<int32_t> cstart(C + 1, 0), corder(n);
+    for (int64_t u = 0; u < n; u++) cstart[G->h_color[u] + 1]++;
+    for (int c = 0; c < C; c++) cstart[c + 1] += cstart[c];
+    {
+        std::vector<int32_t> fill(C, 0);
+        for (int64_t u = 0; u < n; u++) corder[cstart[G->h_color[u]] + fill[G->h_color[u]]++] = (int32_t)u;
+    }
+    const size_t es = prec64 ? 8 : 4;
+    auto ws = [&](const char* name, size_t bytes) { return gde_internal_wsget(ctx, name, std::max<size_t>(bytes, 8)); };
+    a.g = G->g;
+    a.nq = (int)nq;
+    a.ncolors = C;
+    int32_t* d_color = (int32_t*)ws("sor_color", n * 4);
+    int32_t* d_corder = (int32_t*)ws("sor_corder", n * 4);
+    int32_t* d_cstart = (int32_t*)ws("sor_cstart", (C + 1) * 4);
+    a.R = ws("sor_R", (size_t)nq * n * es);
+    a.X = (double*)ws("sor_X", (size_t)nq * n * 8);
+    a.plist = (int32_t*)ws("sor_plist", (size_t)nq * 2 * n * 4);
+    a.pcnt = (int*)ws("sor_pcnt", (size_t)nq * 2 * C * 4);
+    a.mark = (int32_t*)ws("sor_mark", (size_t)nq * n * 4);
+    a.front = (int32_t*)ws("sor_front", (size_t)nq * n * 4);
+    a.pv = ws("sor_pv", (size_t)nq * n * es);
+    a.fcnt = (int*)ws("sor_fcnt", (size_t)nq * 2 * 4);
+    a.gcnt = (unsigned long long*)ws("sor_gcnt", (size_t)nq * 2 * 8);
+    double* d_theta = (double*)ws("sor_theta", (size_t)nq * 8);
+    a.oper = (double*)ws("sor_oper", (size_t)nq * 8);
+    a.sweeps = (int*)ws("sor_sweeps", (size_t)nq * 4);
+    a.done = (int*)ws("sor_done", (size_t)nq * 4);
+    if (!d_color || !d_corder || !d_cstart || !a.R || !a.X || !a.plist || !a.pcnt || !a.mark || !a.front || !a.pv ||
+        !a.fcnt || !a.gcnt || !d_theta || !a.oper || !a.sweeps || !a.done)
+        return gde_internal_fail(ctx, GDE_ENOMEM, "device memory exhausted (SOR workspace)");
+    a.color = d_color;
+    a.corder = d_corder;
+    a.cstart = d_cstart;
+    a.theta = d_theta;
+    a.bar = ctx->bar;
+    a.err = ctx->derr;
+    SO_CK(cudaMemcpyAsync(d_color, G->h_color.data(), n * 4, cudaMemcpyHostToDevice, st));
+    SO_CK(cudaMemcpyAsync(d_corder, corder.data(), n * 4, cudaMemcpyHostToDevice, st));
+    SO_CK(cudaMemcpyAsync(d_cstart, cstart.data(), (C + 1) * 4, cudaMemcpyHostToDevice, st));
+    SO_CK(cudaMemcpyAsync(d_theta, theta.data(), nq * 8, cudaMemcpyHostToDevice, st));
+    SO_CK(cudaMemsetAsync(a.pcnt, 0, (size_t)nq * 2 * C * 4, st));
+    SO_CK(cudaMemsetAsync(a.mark, 0, (size_t)nq * n * 4, st));
+    SO_CK(cudaMemsetAsync(a.fcnt, 0, (size_t)nq * 2 * 4, st));
+    SO_CK(cudaMemsetAsync(a.gcnt, 0, (size_t)nq * 2 * 8, st));
+    SO_CK(cudaMemsetAsync(a.oper, 0, (size_t)nq * 8, st));
+    SO_CK(cudaMemsetAsync(a.done, 0, (size_t)nq * 4, st));
+    SO_CK(cudaMemsetAsync(a.sweeps, 0, (size_t)nq * 4, st));
+    return GDE_OK;
+}
+
+// Cooperative launch of the sweeps; per-query operation counts, sweeps and
+// whether any query hit max_sweeps come back to the host.
+int sor_run(gde_ctx* ctx, SorArgs& a, int prec64, std::vector<double>& hop, std::vector<int>& hsw, bool* capped,
+            float* ms) {
+    cudaStream_t st = ctx->stream;
+    SO_CK(cudaMemsetAsync(ctx->bar, 0, sizeof(GridBarrier), st));
+    SO_CK(cudaMemsetAsync(ctx->derr, 0, sizeof(int), st));
+    int per_sm = 0;
+    if (prec64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sor_kernel<double>, kSorThreads, 0);
+    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sor_kernel<float>, kSorThreads, 0);
+    const int grid = std::max(1, std::min(per_sm, 4)) * ctx->sms;
+    void* args[] = {&a};
+    SO_CK(cudaEventRecord(ctx->ev[0], st));
+    if (prec64) SO_CK(cudaLaunchCooperativeKernel((void*)sor_kernel<double>, grid, kSorThreads, args, 0, st));
+    else SO_CK(cudaLaunchCooperativeKernel((void*)sor_kernel<float>, grid, kSorThreads, args, 0, st));
+    SO_CK(cudaEventRecord(ctx->ev[1], st));
+    const int64_t nq = a.nq;
+    hop.assign(nq, 0.0);
+    hsw.assign(nq, 0);
+    std::vector<int> hdone(nq);
+    int herr = 0;
+    SO_CK(cudaMemcpyAsync(hop.data(), a.oper, nq * 8, cudaMemcpyDeviceToHost, st));
+    SO_CK(cudaMemcpyAsync(hsw.data(), a.sweeps, nq * 4, cudaMemcpyDeviceToHost, st));
+    SO_CK(cudaMemcpyAsync(hdone.data(), a.done, nq * 4, cudaMemcpyDeviceToHost, st));
+    SO_CK(cudaMemcpyAsync(&herr, ctx->derr, 4, cudaMemcpyDeviceToHost, st));
+    SO_CK(cudaStreamSynchronize(st));
+    if (herr != 0) return gde_internal_fail(ctx, herr, "a device-side wait ran out of iterations (grid barrier)");
+    *capped = false;
+    for (int64_t q = 0; q < nq; q++) *capped |= hdone[q] == 2;
+    *ms = 0.f;
+    cudaEventElapsedTime(ms, ctx->ev[0], ctx->ev[1]);
+    return GDE_OK;
+}
+
+}  // namespace
+
 extern "C" int gde_sor(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const int32_t* seeds,
                        const double* eps, int local, void* x_out, void* r_out, int out64, int out_mem, int64_t ld_out,
                        double* oper_out, int32_t* sweeps_out, gde_stats* stats) {
@@ -355,95 +516,37 @@ extern "C" int gde_sor(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t 
     if (nq == 0) return GDE_OK;
     if (cudaSetDevice(ctx->device) != cudaSuccess) return gde_internal_fail(ctx, GDE_ECUDA, "cudaSetDevice");
     cudaStream_t st = ctx->stream;
-    // ---- colouring (once per graph) ----
-    if (G->ncolors <= 0 && build_colors(G) < 0) return gde_internal_fail(ctx, GDE_ECUDA, "reading the graph for colouring");
-    const int C = G->ncolors;
-    std::vector<int32_t> cstart(C + 1, 0), corder(n);
-    for (int64_t u = 0; u < n; u++) cstart[G->h_color[u] + 1]++;
-    for (int c = 0; c < C; c++) cstart[c + 1] += cstart[c];
-    {
-        std::vector<int32_t> fill(C, 0);
-        for (int64_t u = 0; u < n; u++) corder[cstart[G->h_color[u]] + fill[G->h_color[u]]++] = (int32_t)u;
-    }
     const int prec64 = (p->prec == GDE_FP64);
     const size_t es = prec64 ? 8 : 4;
     auto ws = [&](const char* name, size_t bytes) { return gde_internal_wsget(ctx, name, std::max<size_t>(bytes, 8)); };
-    SorArgs a{};
-    a.g = G->g;
-    a.nq = (int)nq;
-    a.ncolors = C;
-    a.local = local ? 1 : 0;
-    a.katz = p->kind == KIND_KATZ;
-    a.alpha = p->alpha;
-    a.omega = p->omega;
-    a.max_sweeps = p->max_rounds > 0 ? p->max_rounds : kDefaultMaxRounds;
-    int32_t* d_color = (int32_t*)ws("sor_color", n * 4);
-    int32_t* d_corder = (int32_t*)ws("sor_corder", n * 4);
-    int32_t* d_cstart = (int32_t*)ws("sor_cstart", (C + 1) * 4);
-    a.R = ws("sor_R", (size_t)nq * n * es);
-    a.X = (double*)ws("sor_X", (size_t)nq * n * 8);
-    a.plist = (int32_t*)ws("sor_plist", (size_t)nq * 2 * n * 4);
-    a.pcnt = (int*)ws("sor_pcnt", (size_t)nq * 2 * C * 4);
-    a.mark = (int32_t*)ws("sor_mark", (size_t)nq * n * 4);
-    a.front = (int32_t*)ws("sor_front", (size_t)nq * n * 4);
-    a.pv = ws("sor_pv", (size_t)nq * n * es);
-    a.fcnt = (int*)ws("sor_fcnt", (size_t)nq * 2 * 4);
-    a.gcnt = (unsigned long long*)ws("sor_gcnt", (size_t)nq * 2 * 8);
-    double* d_theta = (double*)ws("sor_theta", (size_t)nq * 8);
-    a.oper = (double*)ws("sor_oper", (size_t)nq * 8);
-    a.sweeps = (int*)ws("sor_sweeps", (size_t)nq * 4);
-    a.done = (int*)ws("sor_done", (size_t)nq * 4);
-    int32_t* d_seeds = (int32_t*)ws("sor_seeds", (size_t)nq * 4);
-    if (!d_color || !d_corder || !d_cstart || !a.R || !a.X || !a.plist || !a.pcnt || !a.mark || !a.front || !a.pv ||
-        !a.fcnt || !a.gcnt || !d_theta || !a.oper || !a.sweeps || !a.done || !d_seeds)
-        return gde_internal_fail(ctx, GDE_ENOMEM, "device memory exhausted (SOR workspace)");
-    a.color = d_color;
-    a.corder = d_corder;
-    a.cstart = d_cstart;
-    a.theta = d_theta;
-    a.bar = ctx->bar;
-    a.err = ctx->derr;
     std::vector<double> th(nq);
     std::vector<int32_t> sd(nq);
     for (int64_t q = 0; q < nq; q++) {
         th[q] = (p->kind == KIND_PPR) ? eps[q] * p->alpha : eps[q];
         sd[q] = G->node_in(seeds[q]);
     }
-#define SO_CK(call)                                                                       \
-    do {                                                                                  \
-        cudaError_t e__ = (call);                                                         \
-        if (e__ != cudaSuccess) {                                                         \
-            std::string m__ = std::string(#call) + ": " + cudaGetErrorString(e__);       \
-            return gde_internal_fail(ctx, GDE_ECUDA, m__.c_str());                        \
-        }                                                                                 \
-    } while (0)
-    SO_CK(cudaMemcpyAsync(d_color, G->h_color.data(), n * 4, cudaMemcpyHostToDevice, st));
-    SO_CK(cudaMemcpyAsync(d_corder, corder.data(), n * 4, cudaMemcpyHostToDevice, st));
-    SO_CK(cudaMemcpyAsync(d_cstart, cstart.data(), (C + 1) * 4, cudaMemcpyHostToDevice, st));
-    SO_CK(cudaMemcpyAsync(d_theta, th.data(), nq * 8, cudaMemcpyHostToDevice, st));
+    SorArgs a{};
+    int rc = sor_prepare(ctx, G, nq, prec64, th, a);
+    if (rc != GDE_OK) return rc;
+    a.local = local ? 1 : 0;
+    a.katz = p->kind == KIND_KATZ;
+    a.ign = 0;
+    a.alpha = p->alpha;
+    a.omega = p->omega;
+    a.max_sweeps = p->max_rounds > 0 ? p->max_rounds : kDefaultMaxRounds;
+    int32_t* d_seeds = (int32_t*)ws("sor_seeds", (size_t)nq * 4);
+    if (!d_seeds) return gde_internal_fail(ctx, GDE_ENOMEM, "seed list");
     SO_CK(cudaMemcpyAsync(d_seeds, sd.data(), nq * 4, cudaMemcpyHostToDevice, st));
     SO_CK(cudaMemsetAsync(a.R, 0, (size_t)nq * n * es, st));
     SO_CK(cudaMemsetAsync(a.X, 0, (size_t)nq * n * 8, st));
-    SO_CK(cudaMemsetAsync(a.pcnt, 0, (size_t)nq * 2 * C * 4, st));
-    SO_CK(cudaMemsetAsync(a.mark, 0, (size_t)nq * n * 4, st));
-    SO_CK(cudaMemsetAsync(a.fcnt, 0, (size_t)nq * 2 * 4, st));
-    SO_CK(cudaMemsetAsync(a.gcnt, 0, (size_t)nq * 2 * 8, st));
-    SO_CK(cudaMemsetAsync(a.oper, 0, (size_t)nq * 8, st));
-    SO_CK(cudaMemsetAsync(a.done, 0, (size_t)nq * 4, st));
-    SO_CK(cudaMemsetAsync(a.sweeps, 0, (size_t)nq * 4, st));
-    SO_CK(cudaMemsetAsync(ctx->bar, 0, sizeof(GridBarrier), st));
-    SO_CK(cudaMemsetAsync(ctx->derr, 0, sizeof(int), st));
     sor_seed_kernel<<<(int)((nq + 127) / 128), 128, 0, st>>>(a, d_seeds, prec64);
     SO_CK(cudaGetLastError());
-    int per_sm = 0;
-    if (prec64) cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sor_kernel<double>, kSorThreads, 0);
-    else cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, sor_kernel<float>, kSorThreads, 0);
-    const int grid = std::max(1, std::min(per_sm, 4)) * ctx->sms;
-    void* args[] = {&a};
-    SO_CK(cudaEventRecord(ctx->ev[0], st));
-    if (prec64) SO_CK(cudaLaunchCooperativeKernel((void*)sor_kernel<double>, grid, kSorThreads, args, 0, st));
-    else SO_CK(cudaLaunchCooperativeKernel((void*)sor_kernel<float>, grid, kSorThreads, args, 0, st));
-    SO_CK(cudaEventRecord(ctx->ev[1], st));
+    std::vector<double> hop;
+    std::vector<int> hsw;
+    bool capped = false;
+    float ms = 0.f;
+    rc = sor_run(ctx, a, prec64, hop, hsw, &capped, &ms);
+    if (rc != GDE_OK) return rc;
     // ---- results ----
     const size_t oes = out64 ? 8 : 4;
     void* dx = nullptr;
@@ -461,29 +564,81 @@ extern "C" int gde_sor(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t 
         if (x_out) SO_CK(cudaMemcpyAsync(x_out, dx, (size_t)nq * n * oes, cudaMemcpyDeviceToHost, st));
         if (r_out) SO_CK(cudaMemcpyAsync(r_out, dr, (size_t)nq * n * oes, cudaMemcpyDeviceToHost, st));
     }
-    std::vector<double> hop(nq);
-    std::vector<int> hsw(nq), hdone(nq);
-    int herr = 0;
-    SO_CK(cudaMemcpyAsync(hop.data(), a.oper, nq * 8, cudaMemcpyDeviceToHost, st));
-    SO_CK(cudaMemcpyAsync(hsw.data(), a.sweeps, nq * 4, cudaMemcpyDeviceToHost, st));
-    SO_CK(cudaMemcpyAsync(hdone.data(), a.done, nq * 4, cudaMemcpyDeviceToHost, st));
-    SO_CK(cudaMemcpyAsync(&herr, ctx->derr, 4, cudaMemcpyDeviceToHost, st));
     SO_CK(cudaStreamSynchronize(st));
-#undef SO_CK
-    if (herr != 0) return gde_internal_fail(ctx, herr, "a device-side wait ran out of iterations (grid barrier)");
-    bool capped = false;
     for (int64_t q = 0; q < nq; q++) {
         // global: every sweep touches every node and edge (ppr_solver.py:451)
         if (oper_out) oper_out[q] = local ? hop[q] : (double)hsw[q] * ((double)n + G->g.vol);
         if (sweeps_out) sweeps_out[q] = hsw[q];
-        capped |= hdone[q] == 2;
     }
     if (stats) {
-        float ms = 0.f;
-        cudaEventElapsedTime(&ms, ctx->ev[0], ctx->ev[1]);
         stats->kernel_ms = ms;
         stats->total_ms = ms;
         stats->tiles = (int)nq;
+        stats->tile_w = 1;
+    }
+    if (capped) return gde_internal_fail(ctx, GDE_EITERCAP, "max sweeps reached before nothing was pending");
+    return GDE_OK;
+}
+
+// InstantGNN push with relaxation omega != 1 (instantGNNSorPush,
+// InstantGNN.py:74-105) in multicolour order, on the caller's node-major
+// device matrices P, R ([n][ld], F columns), in place.  Candidates: d_cand
+// (device, ncand entries) or every node.
+int gde_internal_sor_feature_push(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t F, void* Pm, void* Rm,
+                                  int64_t ld, double eps, const int32_t* d_cand, int64_t ncand, double* oper_out,
+                                  gde_stats* stats) {
+    const int64_t n = G->g.n;
+    if (!(p->omega > 0.0 && p->omega < 2.0)) return gde_internal_fail(ctx, GDE_EINVAL, "omega must be in (0, 2)");
+    if (!G->g.nfac) return gde_internal_fail(ctx, GDE_EINVAL, "InstantGNN tables missing");
+    if (stats) memset(stats, 0, sizeof(*stats));
+    if (F == 0) return GDE_OK;
+    cudaStream_t st = ctx->stream;
+    const int prec64 = (p->prec == GDE_FP64);
+    std::vector<double> th(F, eps);
+    SorArgs a{};
+    int rc = sor_prepare(ctx, G, F, prec64, th, a);
+    if (rc != GDE_OK) return rc;
+    a.g = G->g;  // current tables
+    a.local = 1;
+    a.katz = 0;
+    a.ign = 1;
+    a.alpha = p->alpha;
+    a.omega = p->omega;
+    a.max_sweeps = p->max_rounds > 0 ? p->max_rounds : kDefaultMaxRounds;
+    const int gb = (int)std::min<int64_t>(4096, (n * F + 255) / 256);
+    if (prec64) {
+        sor_gather_kernel<double, double><<<gb, 256, 0, st>>>((const double*)Rm, ld, F, n, (double*)a.R);
+        sor_gather_kernel<double, double><<<gb, 256, 0, st>>>((const double*)Pm, ld, F, n, a.X);
+    } else {
+        sor_gather_kernel<float, float><<<gb, 256, 0, st>>>((const float*)Rm, ld, F, n, (float*)a.R);
+        sor_gather_kernel<float, double><<<gb, 256, 0, st>>>((const float*)Pm, ld, F, n, a.X);
+    }
+    const int64_t nc = d_cand ? ncand : n;
+    const int sb = (int)std::min<int64_t>(4096, (nc * F + 255) / 256 + 1);
+    if (prec64) sor_seed_cand_kernel<double><<<sb, 256, 0, st>>>(a, d_cand, nc);
+    else sor_seed_cand_kernel<float><<<sb, 256, 0, st>>>(a, d_cand, nc);
+    SO_CK(cudaGetLastError());
+    std::vector<double> hop;
+    std::vector<int> hsw;
+    bool capped = false;
+    float ms = 0.f;
+    rc = sor_run(ctx, a, prec64, hop, hsw, &capped, &ms);
+    if (rc != GDE_OK) return rc;
+    if (prec64) {
+        sor_scatter_kernel<double, double><<<gb, 256, 0, st>>>((const double*)a.R, ld, F, n, (double*)Rm);
+        sor_scatter_kernel<double, double><<<gb, 256, 0, st>>>(a.X, ld, F, n, (double*)Pm);
+    } else {
+        sor_scatter_kernel<float, float><<<gb, 256, 0, st>>>((const float*)a.R, ld, F, n, (float*)Rm);
+        sor_scatter_kernel<float, double><<<gb, 256, 0, st>>>(a.X, ld, F, n, (float*)Pm);
+    }
+    SO_CK(cudaGetLastError());
+    SO_CK(cudaStreamSynchronize(st));
+    if (oper_out)
+        for (int64_t q = 0; q < F; q++) oper_out[q] = hop[q];
+    if (stats) {
+        stats->kernel_ms = ms;
+        stats->total_ms = ms;
+        stats->tiles = (int)F;
         stats->tile_w = 1;
     }
     if (capped) return gde_internal_fail(ctx, GDE_EITERCAP, "max sweeps reached before nothing was pending");

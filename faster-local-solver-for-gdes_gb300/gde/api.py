@@ -295,13 +295,18 @@ def trace_read(ctx: Context | None = None) -> np.ndarray:
 
 
 def feature_push(graph: Graph, kind: int, P, R, eps: float, *, alpha: float, beta: float = 0.0, prec: str = "fp64",
-                 cand=None, tile_w: int = 0, max_rounds: int = 0, tuning: dict | None = None) -> dict:
-    """Multi-column push on device matrices P, R ([n, F] torch tensors), in place."""
+                 cand=None, tile_w: int = 0, max_rounds: int = 0, tuning: dict | None = None,
+                 omega: float = 1.0) -> dict:
+    """Multi-column push on device matrices P, R ([n, F] torch tensors), in place.
+
+    ``omega != 1`` (GDE_IGN): relaxed push in multicolour SOR order (instantGNNSorPush).
+    """
     lib = L.load()
     F = int(P.shape[1])
     ld = int(P.stride(0))
     assert R.stride(0) == ld and P.is_cuda and R.is_cuda
-    p = make_params(kind, L.LOCAL_GD, prec, tile_w, alpha=alpha, beta=beta, max_rounds=max_rounds, tuning=tuning)
+    p = make_params(kind, L.LOCAL_GD, prec, tile_w, alpha=alpha, beta=beta, omega=omega, max_rounds=max_rounds,
+                    tuning=tuning)
     oper = np.zeros(F, dtype=np.float64)
     st = L.Stats()
     c = None if cand is None else np.ascontiguousarray(cand, dtype=np.int32)
@@ -313,7 +318,7 @@ def feature_push(graph: Graph, kind: int, P, R, eps: float, *, alpha: float, bet
 
 def feature_update(graph: Graph, kind: int, h_indices: np.ndarray, h_degree: np.ndarray, us, vs, only_insert: bool,
                    P, R, X, eps: float, *, alpha: float, beta: float = 0.0, prec: str = "fp64", tile_w: int = 0,
-                   max_rounds: int = 0) -> dict:
+                   max_rounds: int = 0, omega: float = 1.0) -> dict:
     """Edge batch + repair + push (device P, R, X; host graph arrays mutated in place)."""
     lib = L.load()
     assert h_indices.dtype == np.int32 and h_degree.dtype == np.int64
@@ -322,7 +327,7 @@ def feature_update(graph: Graph, kind: int, h_indices: np.ndarray, h_degree: np.
     vs = np.ascontiguousarray(vs, dtype=np.int32)
     F = int(P.shape[1])
     ld = int(P.stride(0))
-    p = make_params(kind, L.LOCAL_GD, prec, tile_w, alpha=alpha, beta=beta, max_rounds=max_rounds)
+    p = make_params(kind, L.LOCAL_GD, prec, tile_w, alpha=alpha, beta=beta, omega=omega, max_rounds=max_rounds)
     oper = np.zeros(F, dtype=np.float64)
     st = L.Stats()
     status = lib.gde_feature_update(graph.ctx.ptr, graph.ptr, _ptr(h_indices), _ptr(h_degree), _ptr(us), _ptr(vs),

@@ -516,6 +516,78 @@ double orc_sor_color(i64 n, const i64 *indptr, const i32 *indices, const double 
     return oper;
 }
 
+/* Multicolour SOR push of one InstantGNN column (the GPU order for          */
+/* instantGNNSorPush, InstantGNN.py:74-105): sweeps over colours; in colour  */
+/* c's phase every pending node of colour c with |r_u| >= eps_vec[u]         */
+/* relaxes -- absorbing nodes take p = r, r = 0; others res = omega r_u,     */
+/* p += alpha res, r_u = (1-omega) r_u, r_v += (1-alpha) res / d_u^(1-beta)  */
+/* / d_v^beta.  Pending: the candidates at or above threshold at the start, */
+/* then every node an addition or its own update leaves there.  p, r have   */
+/* stride cs.  Returns the sum of degrees of the relaxed non-absorbing      */
+/* nodes.                                                                   */
+i64 orc_ign_sor_color_column(i64 n, const i64 *indptr, const i32 *indices, const i64 *degree, double alpha,
+                             const double *eps_vec, double beta, double omega, double *p, double *r, i64 cs,
+                             const unsigned char *cand0, const i32 *color, i64 ncolors) {
+    i64 *cstart = (i64 *)calloc((size_t)ncolors + 1, sizeof(i64));
+    for (i64 i = 0; i < n; i++) cstart[color[i] + 1]++;
+    for (i64 c = 0; c < ncolors; c++) cstart[c + 1] += cstart[c];
+    i64 *plist = (i64 *)malloc((size_t)(n > 0 ? n : 1) * sizeof(i64));
+    i64 *pcnt = (i64 *)calloc((size_t)ncolors, sizeof(i64));
+    i64 *cur = (i64 *)malloc((size_t)(n > 0 ? n : 1) * sizeof(i64));
+    unsigned char *mark = (unsigned char *)calloc((size_t)(n > 0 ? n : 1), 1);
+    i64 oper = 0;
+    for (i64 u = 0; u < n; u++)
+        if (cand0[u] && fabs(r[u * cs]) >= eps_vec[u]) {
+            mark[u] = 1;
+            plist[cstart[color[u]] + pcnt[color[u]]++] = u;
+        }
+    for (;;) {
+        i64 pend = 0;
+        for (i64 c = 0; c < ncolors; c++) pend += pcnt[c];
+        if (pend == 0) break;
+        for (i64 c = 0; c < ncolors; c++) {
+            i64 k = pcnt[c];
+            if (k == 0) continue;
+            memcpy(cur, plist + cstart[c], (size_t)k * sizeof(i64));
+            pcnt[c] = 0;
+            for (i64 i = 0; i < k; i++) mark[cur[i]] = 0;
+            for (i64 i = 0; i < k; i++) {
+                i64 u = cur[i];
+                double ru = r[u * cs];
+                if (fabs(ru) < eps_vec[u]) continue;
+                if ((degree[u] == 1 && indices[indptr[u]] == u) || degree[u] == 0) {
+                    p[u * cs] = ru;
+                    r[u * cs] = 0;
+                    continue;
+                }
+                oper += degree[u];
+                double res_u = omega * ru;
+                p[u * cs] += alpha * res_u;
+                double push_u = (1. - alpha) * res_u / pow((double)degree[u], 1 - beta);
+                r[u * cs] = (1 - omega) * ru;
+                for (i64 e = indptr[u]; e < indptr[u] + degree[u]; e++) {
+                    i64 v = indices[e];
+                    r[v * cs] += push_u / pow((double)degree[v], beta);
+                    if (!mark[v] && fabs(r[v * cs]) >= eps_vec[v]) {
+                        mark[v] = 1;
+                        plist[cstart[color[v]] + pcnt[color[v]]++] = v;
+                    }
+                }
+                if (!mark[u] && fabs(r[u * cs]) >= eps_vec[u]) {
+                    mark[u] = 1;
+                    plist[cstart[c] + pcnt[c]++] = u;
+                }
+            }
+        }
+    }
+    free(cstart);
+    free(plist);
+    free(pcnt);
+    free(cur);
+    free(mark);
+    return oper;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Heat kernel (hk_solver.py:15-80, :206-295)                                */
 /* ------------------------------------------------------------------------ */

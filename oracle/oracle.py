@@ -52,6 +52,8 @@ def lib():
         L.orc_katz_gd.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _int, _p, _p]
         L.orc_sor.restype = _dbl
         L.orc_sor.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _dbl, _int, _int, _p, _p]
+        L.orc_ign_sor_color_column.restype = _i64
+        L.orc_ign_sor_color_column.argtypes = [_i64, _p, _p, _p, _dbl, _p, _dbl, _dbl, _p, _p, _i64, _p, _p, _i64]
         L.orc_sor_color.restype = _dbl
         L.orc_sor_color.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _dbl, _int, _int, _p, _i64, _p, _p, _p]
         L.orc_hk_estimate_n.restype = _i64
@@ -274,6 +276,24 @@ def ign_sync(n, indptr, indices, degree, alpha, eps, beta, P, R, cand0=None, max
         opers[f] = lib().orc_ign_sync_column(n, _ptr(indptr), _ptr(indices), _ptr(degree), alpha,
                                              alpha if x_gain is None else x_gain, _ptr(eps_vec), beta,
                                              P.ctypes.data + 8 * f, R.ctypes.data + 8 * f, F, _ptr(cand0), max_rounds)
+    return opers
+
+
+def ign_sor_color(n, indptr, indices, degree, alpha, eps, beta, omega, P, R, colors, cand0=None):
+    """Multicolour SOR InstantGNN push (the GPU order) on every column of P, R in place -> opers."""
+    indptr, indices, degree = _ign_graph(indptr, indices, degree)
+    eps_vec = np.power(degree.astype(np.float64), 1 - beta) * eps
+    F = R.shape[1]
+    if cand0 is None:
+        cand0 = np.ones(n, np.uint8)
+    cand0 = np.ascontiguousarray(cand0, dtype=np.uint8)
+    colors = np.ascontiguousarray(colors, dtype=np.int32)
+    opers = np.zeros(F, np.int64)
+    for f in range(F):
+        opers[f] = lib().orc_ign_sor_color_column(n, _ptr(indptr), _ptr(indices), _ptr(degree), alpha,
+                                                  _ptr(eps_vec), beta, omega, P.ctypes.data + 8 * f,
+                                                  R.ctypes.data + 8 * f, F, _ptr(cand0), _ptr(colors),
+                                                  int(colors.max()) + 1)
     return opers
 
 

@@ -107,3 +107,59 @@ def test_sor_fp32(cl):
         assert errs[-1] < 2e-6 + 6 * 1e-7 * float(g.degree.max())
         assert abs(res["oper"][i] - oo) <= 1e-2 * oo
     assert np.mean(errs) < 1e-5
+
+
+def _dyn():
+    import golden_cases as G
+    return G.dyn(), G
+
+
+def test_instantgnn_sor_static_matches_oracle():
+    import torch
+    dy, _ = _dyn()
+    n = len(dy["indptr"]) - 1
+    X = dy["X"]
+    alpha, eps, beta, omega = 0.1, 1e-4, 0.5, 1.3
+    ip = dy["indptr"].copy()
+    ix = dy["indices"].astype(np.int32).copy()
+    dg = dy["degree"].astype(np.int64).copy()
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    col = api.graph_colors(Gd)
+    Po = np.zeros_like(X)
+    Ro = X.copy()
+    oo = O.ign_sor_color(n, ip, ix, dg, alpha, eps, beta, omega, Po, Ro, col)
+    P = torch.zeros(X.shape, dtype=torch.float64, device="cuda")
+    R = torch.from_numpy(X.copy()).cuda()
+    res = api.feature_push(Gd, L.IGN, P, R, eps, alpha=alpha, beta=beta, prec="fp64", omega=omega)
+    np.testing.assert_allclose(res["oper"], oo, rtol=1e-12)
+    np.testing.assert_allclose(P.cpu().numpy(), Po, rtol=1e-9, atol=1e-13)
+    np.testing.assert_allclose(R.cpu().numpy(), Ro, rtol=1e-9, atol=1e-13)
+
+
+def test_instantgnn_sor_update_meets_stopping_rule():
+    import torch
+    dy, G = _dyn()
+    X = dy["X"]
+    alpha, eps, beta = 0.1, 1e-4, 0.5
+    out = {}
+    for omega in (1.0, 1.3):
+        ip = dy["indptr"].copy()
+        ix = dy["indices"].astype(np.int32).copy()
+        dg = dy["degree"].astype(np.int64).copy()
+        Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+        P = torch.zeros(X.shape, dtype=torch.float64, device="cuda")
+        R = torch.from_numpy(X.copy()).cuda()
+        Xd = torch.from_numpy(X.copy()).cuda()
+        api.feature_push(Gd, L.IGN, P, R, eps, alpha=alpha, beta=beta, prec="fp64", omega=omega)
+        ups = sorted([c for c in G.cases("instantgnn_update") if "insert" in str(c["p"]["algo"])],
+                     key=lambda c: int(c["p"]["snap"]))
+        for c in ups[:2]:
+            api.feature_update(Gd, L.IGN, ix, dg, c["o"]["us"], c["o"]["vs"], True, P, R, Xd, eps, alpha=alpha,
+                               beta=beta, prec="fp64", omega=omega)
+        thr = eps * np.power(dg.astype(np.float64), 1 - beta)
+        Rn = R.cpu().numpy()
+        absorbing = dg == 0
+        assert (np.abs(Rn[~absorbing]) < thr[~absorbing, None]).all()
+        out[omega] = P.cpu().numpy()
+    # both pushes approximate the same propagated features to within the eps-level residual
+    assert np.abs(out[1.3] - out[1.0]).max() < 50 * eps
