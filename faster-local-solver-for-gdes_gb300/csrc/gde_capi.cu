@@ -1192,8 +1192,9 @@ static int feature_push_impl(gde_ctx* ctx, gde_graph* G, const gde_params* p, in
         int rc = upload_ign_tables(ctx, G, p->beta);
         if (rc != GDE_OK) return rc;
     }
-    if (kind == KIND_IGN && p->omega != 0.0 && p->omega != 1.0) {
-        // relaxation omega != 1: instantGNNSorPush order on the GPU (multicolour SOR)
+    if (p->omega != 0.0 && p->omega != 1.0) {
+        // relaxation omega != 1: instantGNNSorPush / update_ppr's push in
+        // multicolour SOR order
         if (G->relabeled) return fail(ctx, GDE_EINVAL, "the SOR feature push runs on padded (row_len) graphs");
         const int32_t* dc = cand;
         if (cand && !cand_on_device) {

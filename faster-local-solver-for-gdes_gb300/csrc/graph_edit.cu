@@ -533,6 +533,7 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
     for (int64_t u = 0; u < n; u++)
         if (h_degree[u] != hlen[u])
             return gde_internal_fail(ctx, GDE_EINVAL, "host degree array differs from the resident graph");
+    if (k > 0) G->ncolors = 0;  // the edges change: the SOR colouring is rebuilt on its next use
     // ---- insert-only batches: the edit, the repair keys and the push all on the device ----
     bool dev_ok = only_insert && k > 0 && G->deg_is_len;
     for (int64_t e = 0; dev_ok && e < k; e++)

@@ -49,7 +49,8 @@ struct SorArgs {
     int ncolors;
     int local;
     int katz;
-    int ign;                 // InstantGNN columns: thresholds eps d^(1-beta), target scale d^-beta
+    int ign;                 // feature columns: 1 InstantGNN (thresholds eps d^(1-beta), target scale d^-beta),
+                             // 2 dynamic PPR (update_ppr: thresholds alpha eps d); both absorb lone nodes
     double alpha, omega;
     const int32_t* color;    // [n] internal ids
     const int32_t* corder;   // [n] nodes sorted by colour
@@ -117,31 +118,32 @@ __device__ void relax_phase(const SorArgs& a, int q, int c, int p, int it) {
             if (a.local) mark[u] = 0;
             const T r = R[u];
             const double d = a.g.degd[u];
-            const double tf = a.ign ? a.g.nfac[u] : d;  // threshold factor: d, or d^(1-beta)
+            const double tf = (a.ign == 1) ? a.g.nfac[u] : d;  // threshold factor: d, or d^(1-beta)
             act = a.local ? at_or_above(r, theta, tf) : (r != T(0));
             if (act && a.ign) {
                 const int64_t rp = a.g.row_ptr[u];
                 const int len = a.g.row_len[u];
                 if (len == 0 || (len == 1 && a.g.col[rp] == u)) {
-                    // absorbing node: p = r, r = 0 (InstantGNN.py:81-84)
+                    // absorbing node: p = r, r = 0 (InstantGNN.py:81-84, ppr_solver.py:802-805)
                     X[u] = (double)r;
                     R[u] = T(0);
                     act = false;
-                } else {
-                    // InstantGNN.py:85-88
-                    const double res = a.omega * (double)r;
-                    X[u] += a.alpha * res;
-                    const T rn = (T)((1 - a.omega) * (double)r);
-                    R[u] = rn;
-                    push = (T)(((1. - a.alpha) * res) / a.g.npush[u]);
-                    my_oper += d;
-                    if (at_or_above(rn, theta, tf)) {  // :94-97
-                        mark[u] = 1;
-                        push_pending(a, q, p ^ 1, u, c);
-                    }
+                }
+            }
+            if (act && a.ign == 1) {
+                // InstantGNN.py:85-88
+                const double res = a.omega * (double)r;
+                X[u] += a.alpha * res;
+                const T rn = (T)((1 - a.omega) * (double)r);
+                R[u] = rn;
+                push = (T)(((1. - a.alpha) * res) / a.g.npush[u]);
+                my_oper += d;
+                if (at_or_above(rn, theta, tf)) {  // :94-97
+                    mark[u] = 1;
+                    push_pending(a, q, p ^ 1, u, c);
                 }
             } else if (act) {
-                // ppr_solver.py:390-395 / katz_solver.py:296-301
+                // ppr_solver.py:390-395 / katz_solver.py:296-301; update_ppr: ppr_solver.py:806-813
                 const double res = a.omega * (double)r;
                 X[u] += res;
                 const T rn = (T)((double)r - res);
@@ -188,11 +190,11 @@ __device__ void push_phase(const SorArgs& a, int q, int c, int p, int it) {
         for (int j = lane; j < len; j += 32) {
             const int v = a.g.col[rp + j];
             // InstantGNN divides by d_v^beta at the target (InstantGNN.py:90)
-            const T add = a.ign ? (T)((double)val / a.g.tfac[v]) : val;
+            const T add = (a.ign == 1) ? (T)((double)val / a.g.tfac[v]) : val;
             const T old = atomicAdd(R + v, add);
             if (a.local) {
                 const T now = old + add;
-                const double tf = a.ign ? a.g.nfac[v] : a.g.degd[v];
+                const double tf = (a.ign == 1) ? a.g.nfac[v] : a.g.degd[v];
                 if (at_or_above(now, theta, tf) && mark[v] == 0 && atomicExch(&mark[v], 1) == 0) {
                     const int cv = a.color[v];
                     push_pending(a, q, (cv > c) ? p : (p ^ 1), v, cv);
@@ -333,7 +335,7 @@ __global__ void sor_seed_cand_kernel(SorArgs a, const int32_t* cand, int64_t nca
         const int64_t k = i % ncand;
         const int u = cand ? cand[k] : (int)k;
         const T r = reinterpret_cast<const T*>(a.R)[(int64_t)q * n + u];
-        if (!at_or_above(r, a.theta[q], a.g.nfac[u])) continue;
+        if (!at_or_above(r, a.theta[q], (a.ign == 1) ? a.g.nfac[u] : a.g.degd[u])) continue;
         if (atomicExch(&a.mark[(int64_t)q * n + u], 1) == 0) push_pending(a, q, 0, u, a.color[u]);
     }
 }
@@ -581,27 +583,29 @@ extern "C" int gde_sor(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t 
 }
 
 // InstantGNN push with relaxation omega != 1 (instantGNNSorPush,
-// InstantGNN.py:74-105) in multicolour order, on the caller's node-major
-// device matrices P, R ([n][ld], F columns), in place.  Candidates: d_cand
-// (device, ncand entries) or every node.
+// InstantGNN.py:74-105), or update_ppr's push (ppr_solver.py:798-819) for
+// GDE_UPPR, in multicolour order, on the caller's node-major device matrices
+// P, R ([n][ld], F columns), in place.  Candidates: d_cand (device, ncand
+// entries) or every node.
 int gde_internal_sor_feature_push(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t F, void* Pm, void* Rm,
                                   int64_t ld, double eps, const int32_t* d_cand, int64_t ncand, double* oper_out,
                                   gde_stats* stats) {
     const int64_t n = G->g.n;
     if (!(p->omega > 0.0 && p->omega < 2.0)) return gde_internal_fail(ctx, GDE_EINVAL, "omega must be in (0, 2)");
-    if (!G->g.nfac) return gde_internal_fail(ctx, GDE_EINVAL, "InstantGNN tables missing");
+    const bool uppr = (p->kind == KIND_UPPR);
+    if (!uppr && !G->g.nfac) return gde_internal_fail(ctx, GDE_EINVAL, "InstantGNN tables missing");
     if (stats) memset(stats, 0, sizeof(*stats));
     if (F == 0) return GDE_OK;
     cudaStream_t st = ctx->stream;
     const int prec64 = (p->prec == GDE_FP64);
-    std::vector<double> th(F, eps);
+    std::vector<double> th(F, uppr ? p->alpha * eps : eps);  // alpha eps d (ppr_solver.py:832) ; eps d^(1-beta)
     SorArgs a{};
     int rc = sor_prepare(ctx, G, F, prec64, th, a);
     if (rc != GDE_OK) return rc;
     a.g = G->g;  // current tables
     a.local = 1;
     a.katz = 0;
-    a.ign = 1;
+    a.ign = uppr ? 2 : 1;
     a.alpha = p->alpha;
     a.omega = p->omega;
     a.max_sweeps = p->max_rounds > 0 ? p->max_rounds : kDefaultMaxRounds;

@@ -299,7 +299,8 @@ def feature_push(graph: Graph, kind: int, P, R, eps: float, *, alpha: float, bet
                  omega: float = 1.0) -> dict:
     """Multi-column push on device matrices P, R ([n, F] torch tensors), in place.
 
-    ``omega != 1`` (GDE_IGN): relaxed push in multicolour SOR order (instantGNNSorPush).
+    ``omega != 1``: relaxed push in multicolour SOR order (instantGNNSorPush for GDE_IGN,
+    update_ppr's push for GDE_UPPR).
     """
     lib = L.load()
     F = int(P.shape[1])

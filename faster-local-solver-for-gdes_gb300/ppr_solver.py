@@ -127,7 +127,8 @@ def update_ppr_parallel(n, indptr, indices, degree, alpha, eps, omega, P, R, us,
     """Dynamic PPR update (ppr_solver.py:824-849): edits the padded CSR in place, repairs and pushes.
 
     P, R are F x n (one row per feature) and are updated in place; returns
-    (opers, runtimes, P, R).  The push is synchronous with omega = 1.
+    (opers, runtimes, P, R).  omega != 1 relaxes in multicolour SOR order;
+    omega = 1 pushes synchronously.
     """
     import torch
     g = graph_for(indptr, indices, degree, padded=True)
@@ -136,7 +137,7 @@ def update_ppr_parallel(n, indptr, indices, degree, alpha, eps, omega, P, R, us,
     Rd = torch.from_numpy(np.ascontiguousarray(R.T)).to(dev)
     with Timer() as t:
         res = api.feature_update(g, L.UPPR, indices, degree, us, vs, False, Pd, Rd, None, eps, alpha=alpha,
-                                 prec="fp64")
+                                 prec="fp64", omega=omega)
     P[:] = Pd.T.cpu().numpy()
     R[:] = Rd.T.cpu().numpy()
     F = P.shape[0]

@@ -68,7 +68,7 @@ typedef struct {
     double l_max;      /* Katz Chebyshev spectral bounds (katz_solver.py:341) */
     double mu_min;
     double beta;       /* InstantGNN exponent */
-    double omega;      /* accepted for SOR-style entry points; the synchronous push uses omega = 1 */
+    double omega;      /* relaxation of gde_sor and of the feature push / update (0 or 1 = synchronous push) */
     int max_rounds;    /* 0 = default (100000) */
     int small_max;     /* degree buckets: <= small_max lane group per row, 0 = default */
     int med_max;       /* <= med_max warp per row, else CTA chunks; 0 = default */
@@ -224,7 +224,10 @@ int64_t gde_hk_estimate_n(double tau, double eps);
  * (instantGNNParallel's initial scan, InstantGNN.py:59-63) when cand == NULL,
  * else the host list cand[0..ncand).  kind GDE_IGN: p += alpha r,
  * r_v += (1-alpha) r_u / d_u^(1-beta) / d_v^beta, threshold d^(1-beta) eps;
- * kind GDE_UPPR (beta = 0): p += r, threshold alpha eps d.
+ * kind GDE_UPPR (beta = 0): p += r, threshold alpha eps d.  p->omega 0 or 1:
+ * synchronous frontier push; otherwise res = omega r_u relaxes in
+ * multicolour SOR order (as gde_sor; instantGNNSorPush, InstantGNN.py:74-105,
+ * and update_ppr's push, ppr_solver.py:798-819), on padded graphs only.
  * Replaces instantGNNParallel / instantGNNSorParallel (InstantGNN.py:46-134);
  * oper_out (host, may be NULL) receives per-column operation counts. */
 int gde_feature_push(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t F, void *P, void *R, int64_t ld,
@@ -237,7 +240,8 @@ int gde_feature_push(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t F,
  * h_indices / h_degree in place and the device copy of the graph; repairs
  * P, R at the touched nodes from X (InstantGNN.py:303-318, kind GDE_IGN) or
  * with the beta = 0 rule (ppr_solver.py:776-792, kind GDE_UPPR); then
- * pushes from the repaired nodes.  Replaces instantGNNUpdateBatchParallel
+ * pushes from the repaired nodes (with p->omega as gde_feature_push; the
+ * colouring is rebuilt for the edited graph).  Replaces instantGNNUpdateBatchParallel
  * (InstantGNN.py:332-359) and update_ppr_parallel (ppr_solver.py:824-849).
  * X may be NULL for GDE_UPPR. */
 int gde_feature_update(gde_ctx *ctx, gde_graph *g, int32_t *h_indices, int64_t *h_degree, const int32_t *us,

@@ -524,10 +524,11 @@ double orc_sor_color(i64 n, const i64 *indptr, const i32 *indices, const double 
 /* / d_v^beta.  Pending: the candidates at or above threshold at the start, */
 /* then every node an addition or its own update leaves there.  p, r have   */
 /* stride cs.  Returns the sum of degrees of the relaxed non-absorbing      */
-/* nodes.                                                                   */
+/* nodes.  uppr=1 gives update_ppr's push instead (ppr_solver.py:806-813):  */
+/* p += res, r_u -= res, r_v += (1-alpha) res / d_u.                        */
 i64 orc_ign_sor_color_column(i64 n, const i64 *indptr, const i32 *indices, const i64 *degree, double alpha,
                              const double *eps_vec, double beta, double omega, double *p, double *r, i64 cs,
-                             const unsigned char *cand0, const i32 *color, i64 ncolors) {
+                             const unsigned char *cand0, const i32 *color, i64 ncolors, int uppr) {
     i64 *cstart = (i64 *)calloc((size_t)ncolors + 1, sizeof(i64));
     for (i64 i = 0; i < n; i++) cstart[color[i] + 1]++;
     for (i64 c = 0; c < ncolors; c++) cstart[c + 1] += cstart[c];
@@ -562,12 +563,19 @@ i64 orc_ign_sor_color_column(i64 n, const i64 *indptr, const i32 *indices, const
                 }
                 oper += degree[u];
                 double res_u = omega * ru;
-                p[u * cs] += alpha * res_u;
-                double push_u = (1. - alpha) * res_u / pow((double)degree[u], 1 - beta);
-                r[u * cs] = (1 - omega) * ru;
+                double push_u;
+                if (uppr) {  /* ppr_solver.py:806-809 */
+                    p[u * cs] += res_u;
+                    push_u = (1. - alpha) * res_u / (double)degree[u];
+                    r[u * cs] -= res_u;
+                } else {
+                    p[u * cs] += alpha * res_u;
+                    push_u = (1. - alpha) * res_u / pow((double)degree[u], 1 - beta);
+                    r[u * cs] = (1 - omega) * ru;
+                }
                 for (i64 e = indptr[u]; e < indptr[u] + degree[u]; e++) {
                     i64 v = indices[e];
-                    r[v * cs] += push_u / pow((double)degree[v], beta);
+                    r[v * cs] += uppr ? push_u : push_u / pow((double)degree[v], beta);
                     if (!mark[v] && fabs(r[v * cs]) >= eps_vec[v]) {
                         mark[v] = 1;
                         plist[cstart[color[v]] + pcnt[color[v]]++] = v;
@@ -909,12 +917,13 @@ i64 orc_ign_sync_column(i64 n, const i64 *indptr, const i32 *indices, const i64 
 /* instantGNNUpdateBatch for one column (InstantGNN.py:298-329).  p, r, x are
  * columns with stride cs; the maps are the outputs of orc_update_graph.
  * sync=1 keeps the reference's repair and replaces the FIFO push with the
- * synchronous push (candidates = the repaired nodes); returns its oper. */
+ * synchronous push (candidates = the repaired nodes); sync=2 replaces it with
+ * the multicolour SOR order given by color; both return the push's oper. */
 i64 orc_ign_update_column(i64 n, const i64 *indptr, const i32 *indices, const i64 *degree, const i64 *old_degree,
                           double *p, double *r, const double *x, i64 cs, double alpha, double eps, double omega,
                           int sor, int insert_only, double beta, const i64 *ins_keys, const i64 *ins_off,
                           const i64 *ins_nbr, i64 n_ins, const i64 *del_keys, const i64 *del_off,
-                          const i64 *del_nbr, i64 n_del, int sync) {
+                          const i64 *del_nbr, i64 n_del, int sync, const i32 *color, i64 ncolors) {
     i64 sync_oper = 0;
     double *eps_vec = (double *)malloc((size_t)n * sizeof(double));
     double *pc = (double *)malloc((size_t)n * sizeof(double));
@@ -958,8 +967,12 @@ i64 orc_ign_update_column(i64 n, const i64 *indptr, const i32 *indices, const i6
     if (sync) {
         unsigned char *cand0 = (unsigned char *)calloc((size_t)n, 1);
         for (i64 t = 0; t < n_ins; t++) cand0[ins_keys[t]] = 1;
-        sync_oper = orc_ign_sync_column(n, indptr, indices, degree, alpha, alpha, eps_vec, beta, pc, rc, 1, cand0,
-                                        (i64)1 << 40);
+        if (sync == 2)
+            sync_oper = orc_ign_sor_color_column(n, indptr, indices, degree, alpha, eps_vec, beta, omega, pc, rc, 1,
+                                                 cand0, color, ncolors, 0);
+        else
+            sync_oper = orc_ign_sync_column(n, indptr, indices, degree, alpha, alpha, eps_vec, beta, pc, rc, 1, cand0,
+                                            (i64)1 << 40);
         free(cand0);
     } else if (rear != front) {
         ign_push(n + 2, indptr, indices, degree, alpha, eps_vec, omega, sor, NULL, pc, rc, queue, front, rear,
@@ -975,11 +988,11 @@ i64 orc_ign_update_column(i64 n, const i64 *indptr, const i32 *indices, const i6
     return sync_oper;
 }
 
-/* update_ppr for one feature row (ppr_solver.py:769-821). */
+/* update_ppr for one feature row (ppr_solver.py:769-821); sync as in orc_ign_update_column. */
 i64 orc_update_ppr_row(i64 n, const i64 *indptr, const i32 *indices, const i64 *degree, const i64 *old_degree,
                        double *p, double *r, double alpha, double eps, double omega, const i64 *ins_keys,
                        const i64 *ins_off, const i64 *ins_nbr, i64 n_ins, const i64 *del_keys, const i64 *del_off,
-                       const i64 *del_nbr, i64 n_del, int sync) {
+                       const i64 *del_nbr, i64 n_del, int sync, const i32 *color, i64 ncolors) {
     double *eps_vec = (double *)malloc((size_t)n * sizeof(double));
     i64 *queue = (i64 *)calloc((size_t)n + 2, sizeof(i64));
     unsigned char *q_mark = (unsigned char *)calloc((size_t)n, 1);
@@ -1020,8 +1033,12 @@ i64 orc_update_ppr_row(i64 n, const i64 *indptr, const i32 *indices, const i64 *
     if (sync) {
         unsigned char *cand0 = (unsigned char *)calloc((size_t)n, 1);
         for (i64 t = 0; t < n_ins; t++) cand0[ins_keys[t]] = 1;
-        oper += orc_ign_sync_column(n, indptr, indices, degree, alpha, 1.0, eps_vec, 0.0, p, r, 1, cand0,
-                                    (i64)1 << 40);
+        if (sync == 2)
+            oper += orc_ign_sor_color_column(n, indptr, indices, degree, alpha, eps_vec, 0.0, omega, p, r, 1, cand0,
+                                             color, ncolors, 1);
+        else
+            oper += orc_ign_sync_column(n, indptr, indices, degree, alpha, 1.0, eps_vec, 0.0, p, r, 1, cand0,
+                                        (i64)1 << 40);
         free(cand0);
         rear = front;  /* skip the FIFO push */
     }

@@ -53,7 +53,8 @@ def lib():
         L.orc_sor.restype = _dbl
         L.orc_sor.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _dbl, _int, _int, _p, _p]
         L.orc_ign_sor_color_column.restype = _i64
-        L.orc_ign_sor_color_column.argtypes = [_i64, _p, _p, _p, _dbl, _p, _dbl, _dbl, _p, _p, _i64, _p, _p, _i64]
+        L.orc_ign_sor_color_column.argtypes = [_i64, _p, _p, _p, _dbl, _p, _dbl, _dbl, _p, _p, _i64, _p, _p, _i64,
+                                               _int]
         L.orc_sor_color.restype = _dbl
         L.orc_sor_color.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _dbl, _int, _int, _p, _i64, _p, _p, _p]
         L.orc_hk_estimate_n.restype = _i64
@@ -68,10 +69,10 @@ def lib():
         L.orc_update_graph.argtypes = [_i64, _p, _p, _p, _p, _p, _i64, _int, _p, _p, _p, _p, _p, _p, _p, _p]
         L.orc_ign_update_column.restype = _i64
         L.orc_ign_update_column.argtypes = [_i64, _p, _p, _p, _p, _p, _p, _p, _i64, _dbl, _dbl, _dbl, _int, _int,
-                                            _dbl, _p, _p, _p, _i64, _p, _p, _p, _i64, _int]
+                                            _dbl, _p, _p, _p, _i64, _p, _p, _p, _i64, _int, _p, _i64]
         L.orc_update_ppr_row.restype = _i64
         L.orc_update_ppr_row.argtypes = [_i64, _p, _p, _p, _p, _p, _p, _dbl, _dbl, _dbl, _p, _p, _p, _i64, _p, _p,
-                                         _p, _i64, _int]
+                                         _p, _i64, _int, _p, _i64]
         L.orc_ign_sync_column.restype = _i64
         L.orc_ign_sync_column.argtypes = [_i64, _p, _p, _p, _dbl, _dbl, _p, _dbl, _p, _p, _i64, _p, _i64]
         L.orc_threads.restype = _int
@@ -145,12 +146,16 @@ def sor_color(n, indptr, indices, degree, s, alpha, eps, omega, local, colors, k
     return x, r, float(oper), int(sw.value)
 
 
-def greedy_colors(indptr, indices, order):
-    """Greedy proper colouring visiting nodes in ``order`` (smallest colour not used by a coloured neighbour)."""
+def greedy_colors(indptr, indices, order, row_len=None):
+    """Greedy proper colouring visiting nodes in ``order`` (smallest colour not used by a coloured neighbour).
+
+    ``row_len`` gives the used length of each row of a padded CSR.
+    """
     n = len(indptr) - 1
+    ends = indptr[1:] if row_len is None else indptr[:-1] + row_len
     col = np.full(n, -1, dtype=np.int32)
     for u in order:
-        used = {int(col[v]) for v in indices[indptr[u]:indptr[u + 1]] if col[v] >= 0}
+        used = {int(col[v]) for v in indices[indptr[u]:ends[u]] if col[v] >= 0}
         c = 0
         while c in used:
             c += 1
@@ -220,14 +225,22 @@ def update_graph(n, indptr, indices, degree, us, vs, onlyinsert):
     return ik[:a], io[:a + 1], inb[:io[a]], dk[:b], do[:b + 1], dnb[:do[b]]
 
 
-def ign_update(n, indptr, indices, degree, alpha, eps, omega, P, R, X, us, vs, beta, algo, sync=False):
+def _padded_colors(indptr, indices, degree):
+    """The GPU's colouring of a padded graph: greedy in degree-descending order, ties by id."""
+    return greedy_colors(indptr, indices, np.argsort(-degree, kind="stable"), row_len=degree)
+
+
+def ign_update(n, indptr, indices, degree, alpha, eps, omega, P, R, X, us, vs, beta, algo, sync=False, color=False):
     """``instantGNNUpdateBatchParallel`` (InstantGNN.py:332-359); mutates graph, P, R in place.
 
     sync=True keeps the reference's repair and uses the synchronous push;
-    returns (maps, per-column push opers).
+    color=True keeps it and relaxes in multicolour SOR order (colouring of the
+    edited graph); returns (maps, per-column push opers).
     """
     old_degree = degree.copy()
     maps = update_graph(n, indptr, indices, degree, us, vs, "insert" in algo)
+    mode = 2 if color else (1 if sync else 0)
+    col = _padded_colors(indptr, indices, degree) if color else np.zeros(1, np.int32)
     ik, io, inb, dk, do, dnb = maps
     F = R.shape[1]
     X = np.ascontiguousarray(X, dtype=np.float64)
@@ -237,24 +250,28 @@ def ign_update(n, indptr, indices, degree, alpha, eps, omega, P, R, X, us, vs, b
                                                P.ctypes.data + 8 * f, R.ctypes.data + 8 * f, X.ctypes.data + 8 * f, F,
                                                alpha, eps, omega, int("sor" in algo), int("insert" in algo), beta,
                                                _ptr(ik), _ptr(io), _ptr(inb), len(ik), _ptr(dk), _ptr(do), _ptr(dnb),
-                                               len(dk), int(sync))
+                                               len(dk), mode, _ptr(col), int(col.max()) + 1)
     return maps, opers
 
 
-def update_ppr(n, indptr, indices, degree, alpha, eps, omega, P, R, us, vs, sync=False):
+def update_ppr(n, indptr, indices, degree, alpha, eps, omega, P, R, us, vs, sync=False, color=False):
     """``update_ppr_parallel`` (ppr_solver.py:824-849); P, R are F x n, updated in place -> opers.
 
-    sync=True keeps the reference's repair and uses the synchronous push.
+    sync=True keeps the reference's repair and uses the synchronous push;
+    color=True keeps it and relaxes in multicolour SOR order.
     """
     old_degree = degree.copy()
     ik, io, inb, dk, do, dnb = update_graph(n, indptr, indices, degree, us, vs, False)
+    mode = 2 if color else (1 if sync else 0)
+    col = _padded_colors(indptr, indices, degree) if color else np.zeros(1, np.int32)
     opers = np.zeros(P.shape[0], np.int64)
     for f in range(P.shape[0]):
         p = np.ascontiguousarray(P[f])
         r = np.ascontiguousarray(R[f])
         opers[f] = lib().orc_update_ppr_row(n, _ptr(indptr), _ptr(indices), _ptr(degree), _ptr(old_degree), _ptr(p),
                                             _ptr(r), alpha, eps, omega, _ptr(ik), _ptr(io), _ptr(inb), len(ik),
-                                            _ptr(dk), _ptr(do), _ptr(dnb), len(dk), int(sync))
+                                            _ptr(dk), _ptr(do), _ptr(dnb), len(dk), mode, _ptr(col),
+                                            int(col.max()) + 1)
         P[f] = p
         R[f] = r
     return opers
@@ -293,7 +310,7 @@ def ign_sor_color(n, indptr, indices, degree, alpha, eps, beta, omega, P, R, col
         opers[f] = lib().orc_ign_sor_color_column(n, _ptr(indptr), _ptr(indices), _ptr(degree), alpha,
                                                   _ptr(eps_vec), beta, omega, P.ctypes.data + 8 * f,
                                                   R.ctypes.data + 8 * f, F, _ptr(cand0), _ptr(colors),
-                                                  int(colors.max()) + 1)
+                                                  int(colors.max()) + 1, 0)
     return opers
 
 

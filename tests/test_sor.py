@@ -136,9 +136,74 @@ def test_instantgnn_sor_static_matches_oracle():
     np.testing.assert_allclose(R.cpu().numpy(), Ro, rtol=1e-9, atol=1e-13)
 
 
-def test_instantgnn_sor_update_meets_stopping_rule():
+def _padded(dy):
+    ip = dy["indptr"].copy()
+    ix = dy["indices"].astype(np.int32).copy()
+    dg = dy["degree"].astype(np.int64).copy()
+    return ip, ix, dg
+
+
+def test_instantgnn_sor_update_matches_oracle():
+    """Insert batches + repair + SOR push: exact against the oracle in the same colour order."""
     import torch
     dy, G = _dyn()
+    n = len(dy["indptr"]) - 1
+    X = dy["X"]
+    alpha, eps, beta, omega = 0.1, 1e-4, 0.5, 1.25
+    ip, ix, dg = _padded(dy)
+    ix_o, dg_o = ix.copy(), dg.copy()
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    Po = np.zeros_like(X)
+    Ro = X.copy()
+    O.ign_sor_color(n, ip, ix_o, dg_o, alpha, eps, beta, omega, Po, Ro, api.graph_colors(Gd))
+    P = torch.from_numpy(Po.copy()).cuda()
+    R = torch.from_numpy(Ro.copy()).cuda()
+    Xd = torch.from_numpy(X.copy()).cuda()
+    for snap in range(3):
+        us, vs = dy["Us"][snap], dy["Vs"][snap]
+        _, oo = O.ign_update(n, ip, ix_o, dg_o, alpha, eps, omega, Po, Ro, X, us, vs, beta, "insert_sor", color=True)
+        res = api.feature_update(Gd, L.IGN, ix, dg, us, vs, True, P, R, Xd, eps, alpha=alpha, beta=beta,
+                                 prec="fp64", omega=omega)
+        np.testing.assert_array_equal(ix, ix_o)
+        np.testing.assert_array_equal(dg, dg_o)
+        # the colouring follows the edited graph
+        np.testing.assert_array_equal(api.graph_colors(Gd), O._padded_colors(ip, ix_o, dg_o))
+        np.testing.assert_allclose(res["oper"], oo, rtol=1e-12)
+        np.testing.assert_allclose(P.cpu().numpy(), Po, rtol=1e-9, atol=1e-13)
+        np.testing.assert_allclose(R.cpu().numpy(), Ro, rtol=1e-9, atol=1e-13)
+
+
+@pytest.mark.parametrize("omega", [1.2, 1.5])
+def test_update_ppr_sor_matches_oracle(omega):
+    """update_ppr_parallel with omega != 1 (insertions and deletions): exact in multicolour order."""
+    import torch
+    dy, G = _dyn()
+    n = len(dy["indptr"]) - 1
+    seeds = G.load()["dynppr/seeds"]
+    alpha, eps = 0.1, 1e-5
+    ip, ix, dg = _padded(dy)
+    ix_o, dg_o = ix.copy(), dg.copy()
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    Po = np.zeros((len(seeds), n))
+    Ro = np.zeros((len(seeds), n))
+    for f, s in enumerate(seeds):
+        Ro[f, s] = alpha
+    P = torch.zeros((n, len(seeds)), dtype=torch.float64, device="cuda")
+    R = torch.from_numpy(np.ascontiguousarray(Ro.T)).cuda()
+    for snap in range(3):
+        oo = O.update_ppr(n, ip, ix_o, dg_o, alpha, eps, omega, Po, Ro, dy["Us"][snap], dy["Vs"][snap], color=True)
+        res = api.feature_update(Gd, L.UPPR, ix, dg, dy["Us"][snap], dy["Vs"][snap], False, P, R, None, eps,
+                                 alpha=alpha, prec="fp64", omega=omega)
+        np.testing.assert_array_equal(ix, ix_o)
+        np.testing.assert_array_equal(dg, dg_o)
+        np.testing.assert_allclose(res["oper"], oo, rtol=1e-12)
+        np.testing.assert_allclose(P.cpu().numpy().T, Po, rtol=1e-9, atol=1e-13)
+        np.testing.assert_allclose(R.cpu().numpy().T, Ro, rtol=1e-9, atol=1e-13)
+
+
+def test_instantgnn_sor_update_meets_stopping_rule():
+    import torch
+    dy, _ = _dyn()
     X = dy["X"]
     alpha, eps, beta = 0.1, 1e-4, 0.5
     out = {}
@@ -151,10 +216,8 @@ def test_instantgnn_sor_update_meets_stopping_rule():
         R = torch.from_numpy(X.copy()).cuda()
         Xd = torch.from_numpy(X.copy()).cuda()
         api.feature_push(Gd, L.IGN, P, R, eps, alpha=alpha, beta=beta, prec="fp64", omega=omega)
-        ups = sorted([c for c in G.cases("instantgnn_update") if "insert" in str(c["p"]["algo"])],
-                     key=lambda c: int(c["p"]["snap"]))
-        for c in ups[:2]:
-            api.feature_update(Gd, L.IGN, ix, dg, c["o"]["us"], c["o"]["vs"], True, P, R, Xd, eps, alpha=alpha,
+        for snap in range(2):
+            api.feature_update(Gd, L.IGN, ix, dg, dy["Us"][snap], dy["Vs"][snap], True, P, R, Xd, eps, alpha=alpha,
                                beta=beta, prec="fp64", omega=omega)
         thr = eps * np.power(dg.astype(np.float64), 1 - beta)
         Rn = R.cpu().numpy()
