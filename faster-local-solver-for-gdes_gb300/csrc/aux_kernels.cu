@@ -23,8 +23,9 @@ __global__ void init_columns_kernel(PushArgs a, const InitCol* cols, int ncols, 
     InitCol ic = cols[wid];
     const int64_t n = a.g.n;
     const int64_t base = (int64_t)ic.tile * a.tile_stride;
+    const int64_t xld = a.xld ? a.xld : a.ld;  // X may interleave {x, Kahan term}
     T* R = reinterpret_cast<T*>(a.R) + base;
-    T* X = reinterpret_cast<T*>(a.X) + base;
+    T* X = reinterpret_cast<T*>(a.X) + (int64_t)ic.tile * (a.xld ? a.xtile : a.tile_stride);
     T* DX = a.DX ? reinterpret_cast<T*>(a.DX) + base : nullptr;
     int32_t* mark = a.mark + (int64_t)ic.tile * n;
     int32_t* list = a.cand + ((int64_t)ic.tile * 2 + 0) * n;
@@ -33,7 +34,7 @@ __global__ void init_columns_kernel(PushArgs a, const InitCol* cols, int ncols, 
     const int64_t so = (int64_t)ic.seed * a.ld + ic.col;
     if (lane == 0) {
         R[so] = (T)ic.r0;
-        if (ic.x0 != 0.0) X[so] = (T)ic.x0;
+        if (ic.x0 != 0.0) X[(int64_t)ic.seed * xld + ic.col] = (T)ic.x0;
         if (DX && ic.dx0 != 0.0) DX[so] = (T)ic.dx0;
     }
     __syncwarp();
@@ -56,18 +57,21 @@ __global__ void extract_kernel(PushArgs a, const ExtractCol* cols, O* x_out, O* 
                                int clear) {
     const ExtractCol ec = cols[blockIdx.y];
     const int64_t base = (int64_t)ec.tile * a.tile_stride + ec.col;
-    T* X = reinterpret_cast<T*>(a.X) + base;
+    const int64_t xbase = (int64_t)ec.tile * (a.xld ? a.xtile : a.tile_stride) + ec.col;
+    const int64_t xld = a.xld ? a.xld : a.ld;  // X may interleave {x, Kahan term}
+    T* X = reinterpret_cast<T*>(a.X) + xbase;
     T* R = reinterpret_cast<T*>(a.R) + base;
     T* R2 = a.R2 ? reinterpret_cast<T*>(a.R2) + base : nullptr;
-    float* XC = a.XC ? a.XC + base : nullptr;  // Kahan compensation: the sum is X - XC
+    float* XC = a.XC ? a.XC + xbase : nullptr;  // Kahan compensation: the sum is X - XC
     const int rl = ec.r_levels;
     const int32_t* perm = a.g.perm;
     // u runs over caller ids; the slabs are in internal (relabelled) order
     for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t o = (perm ? (int64_t)perm[u] : u) * a.ld;
+        const int64_t v = perm ? (int64_t)perm[u] : u;
+        const int64_t o = v * a.ld, xo = v * xld;
         if (x_out) {
-            double x = (double)X[o];
-            if (XC) x -= (double)XC[o];
+            double x = (double)X[xo];
+            if (XC) x -= (double)XC[xo];
             if (u == ec.seed) x = x + ec.seed_add;
             if (ec.scale != 1.0) x = x / ec.scale;
             x_out[ec.out_row * ld_out + u] = (O)x;
@@ -77,10 +81,10 @@ __global__ void extract_kernel(PushArgs a, const ExtractCol* cols, O* x_out, O* 
             if (rl == 2) r_out[(ec.out_row * rl + 1) * ld_out + u] = R2 ? (O)R2[o] : (O)0;
         }
         if (clear) {
-            X[o] = T(0);
+            X[xo] = T(0);
             R[o] = T(0);
             if (R2) R2[o] = T(0);
-            if (XC) XC[o] = 0.f;
+            if (XC) XC[xo] = 0.f;
         }
     }
 }
@@ -94,6 +98,16 @@ __global__ void permute_rows_kernel(const T* src, int64_t sld, T* dst, int64_t d
         const int64_t p = perm[u];
         if (to_internal) dst[p * dld + c] = src[u * sld + c];
         else dst[u * dld + c] = src[p * sld + c];
+    }
+}
+
+// per row r: dst[r][u] (caller order) <- src[r][perm[u]] (internal order)
+template <typename T>
+__global__ void permute_entries_kernel(const T* src, int64_t sld, T* dst, int64_t dld, const int32_t* perm, int64_t n,
+                                       int64_t rows) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * rows; i += (int64_t)gridDim.x * blockDim.x) {
+        const int64_t r = i / n, u = i % n;
+        dst[r * dld + u] = src[r * sld + perm[u]];
     }
 }
 
@@ -139,6 +153,19 @@ cudaError_t permute_rows(const void* src, int64_t sld, void* dst, int64_t dld, c
     else
         permute_rows_kernel<float><<<blocks, 256, 0, st>>>((const float*)src, sld, (float*)dst, dld, perm, n, F,
                                                             to_internal);
+    return cudaGetLastError();
+}
+
+cudaError_t permute_entries(const void* src, int64_t sld, void* dst, int64_t dld, const int32_t* perm, int64_t n,
+                            int64_t rows, int elem, cudaStream_t st) {
+    if (n == 0 || rows == 0) return cudaSuccess;
+    const int64_t total = n * rows;
+    const int blocks = (int)std::min<int64_t>((total + 255) / 256, 8192);
+    if (elem == 8)
+        permute_entries_kernel<double><<<blocks, 256, 0, st>>>((const double*)src, sld, (double*)dst, dld, perm, n,
+                                                                rows);
+    else
+        permute_entries_kernel<float><<<blocks, 256, 0, st>>>((const float*)src, sld, (float*)dst, dld, perm, n, rows);
     return cudaGetLastError();
 }
 

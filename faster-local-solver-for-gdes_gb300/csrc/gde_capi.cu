@@ -126,11 +126,14 @@ int alloc_tiles(gde_ctx* ctx, gde_graph* G, int ntiles, int W, int prec64, bool 
     PushArgs& a = tw.a;
     a.g = G->g;
     a.ntiles = ntiles;
+    // one-column FP32 Kahan slabs interleave the solution and its Kahan term
+    // as {x, c} pairs, so a frontier node's update touches one sector
+    const bool inter = own_slabs && kahan && !prec64 && W == 1 && !need_r2;
     if (own_slabs) {
         a.ld = W;
         a.tile_stride = (int64_t)n * W;
         a.R = wsget(ctx, "R", slab);
-        a.X = wsget(ctx, "X", slab);
+        a.X = wsget(ctx, "X", inter ? 2 * slab : slab);
         if (!a.R || !a.X) return fail(ctx, GDE_ENOMEM, "device memory exhausted (residual/solution slabs)");
         a.R2 = need_r2 ? wsget(ctx, "R2", slab) : nullptr;
         a.DX = need_dx ? wsget(ctx, "DX", slab) : nullptr;
@@ -138,13 +141,18 @@ int alloc_tiles(gde_ctx* ctx, gde_graph* G, int ntiles, int W, int prec64, bool 
     }
     a.XC = nullptr;
     a.kahan = 0;
-    if (kahan && !prec64) {
-        size_t xcb = own_slabs ? (size_t)ntiles * n * W * 4 : 0;
-        if (xcb) {
-            a.XC = (float*)wsget(ctx, "XC", xcb);
+    a.xld = 0;
+    a.xtile = 0;
+    if (kahan && !prec64 && own_slabs) {
+        if (inter) {
+            a.XC = (float*)a.X + 1;
+            a.xld = 2;
+            a.xtile = 2 * n;
+        } else {
+            a.XC = (float*)wsget(ctx, "XC", (size_t)ntiles * n * W * 4);
             if (!a.XC) return fail(ctx, GDE_ENOMEM, "device memory exhausted (Kahan slab)");
-            a.kahan = 1;
         }
+        a.kahan = 1;
     }
     a.P = wsget(ctx, "P", slab);
     a.cand = (int32_t*)wsget(ctx, "cand", (size_t)ntiles * 2 * n * 4);
@@ -396,11 +404,11 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     const size_t slab = (size_t)S * n * es;
     CK(cudaEventRecord(ctx->ev[2], ctx->stream));
     CK(cudaMemsetAsync(a.R, 0, slab, ctx->stream));
-    CK(cudaMemsetAsync(a.X, 0, slab, ctx->stream));
+    CK(cudaMemsetAsync(a.X, 0, a.xld ? 2 * slab : slab, ctx->stream));  // interleaved: X and XC
     if (a.R2) CK(cudaMemsetAsync(a.R2, 0, slab, ctx->stream));
-    if (a.XC) CK(cudaMemsetAsync(a.XC, 0, (size_t)S * n * 4, ctx->stream));
+    if (a.XC && !a.xld) CK(cudaMemsetAsync(a.XC, 0, (size_t)S * n * 4, ctx->stream));
     // ---- the query queue on the device ----
-    std::vector<int32_t> qs(nq), qsc(nq), qk(nq), qnl(kinds ? nq : 0), qpo(kinds ? nq : 0);
+    std::vector<int32_t> qs(nq), qk(nq), qnl(kinds ? nq : 0), qpo(kinds ? nq : 0);
     std::vector<double> qt(nq), qr0(nq), qal(nq);
     std::vector<long long> qarr(arrival_ms ? nq : 0);
     std::vector<double> psi_all;
@@ -410,7 +418,6 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
         const double al = alphas ? alphas[q] : p->alpha;
         qk[q] = k;
         qal[q] = al;
-        qsc[q] = seeds[q];
         qs[q] = G->node_in(seeds[q]);
         if (k == KIND_PPR) qt[q] = eps[q] * al;              // eps * alpha * degree
         else if (k == KIND_KATZ) qt[q] = eps[q];             // eps * degree
@@ -430,7 +437,6 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     }
     auto dev = [&](const char* name, size_t bytes) { return wsget(ctx, name, std::max<size_t>(bytes, 8)); };
     int32_t* d_seed = (int32_t*)dev("q_seed", nq * 4);
-    int32_t* d_sc = (int32_t*)dev("q_seed_caller", nq * 4);
     double* d_theta = (double*)dev("q_theta", nq * 8);
     double* d_r0 = (double*)dev("q_r0", nq * 8);
     long long* d_arr = arrival_ms ? (long long*)dev("q_arrival", nq * 8) : nullptr;
@@ -439,11 +445,10 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     unsigned long long* d_start = (unsigned long long*)dev("q_start", nq * 8);
     unsigned long long* d_finish = (unsigned long long*)dev("q_finish", nq * 8);
     int* d_next = (int*)dev("q_next", 4);
-    if (!d_seed || !d_sc || !d_theta || !d_r0 || (arrival_ms && !d_arr) || !d_oper || !d_rounds || !d_start ||
+    if (!d_seed || !d_theta || !d_r0 || (arrival_ms && !d_arr) || !d_oper || !d_rounds || !d_start ||
         !d_finish || !d_next)
         return fail(ctx, GDE_ENOMEM, "query queue");
     CK(cudaMemcpyAsync(d_seed, qs.data(), nq * 4, cudaMemcpyHostToDevice, ctx->stream));
-    CK(cudaMemcpyAsync(d_sc, qsc.data(), nq * 4, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(d_theta, qt.data(), nq * 8, cudaMemcpyHostToDevice, ctx->stream));
     CK(cudaMemcpyAsync(d_r0, qr0.data(), nq * 8, cudaMemcpyHostToDevice, ctx->stream));
     if (d_arr) CK(cudaMemcpyAsync(d_arr, qarr.data(), nq * 8, cudaMemcpyHostToDevice, ctx->stream));
@@ -548,7 +553,6 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     Q.r_out = dr;
     Q.ld_out = ld_out;
     Q.out64 = out64;
-    Q.seed_caller = d_sc;
     Q.seed_add = (kind == KIND_KATZ) ? -1.0 : 0.0;  // xt[s_node] -= 1. (katz_solver.py:243)
     Q.kind = d_kind;
     Q.alpha = d_alpha;
@@ -565,6 +569,24 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     rc = run_engine(ctx, a, prec64, 1, stats, &kernel_ms);
     if (rc != GDE_OK) return rc;
     // ---- results ----
+    // retired rows are in internal node order: permute them to caller order
+    // through a wave buffer of a few rows (random reads stay in L2)
+    if (G->perm_d) {
+        const int64_t row_bytes = n * (int64_t)oes;
+        const int64_t wave = std::max<int64_t>(1, std::min<int64_t>(nq, (int64_t)(48 << 20) / row_bytes));
+        void* tmp = dev("out_wave", (size_t)(wave * row_bytes));
+        if (!tmp) return fail(ctx, GDE_ENOMEM, "output permutation buffer");
+        for (void* rows : {dx, dr}) {
+            if (!rows) continue;
+            for (int64_t q0 = 0; q0 < nq; q0 += wave) {
+                const int64_t w = std::min<int64_t>(wave, nq - q0);
+                char* at = (char*)rows + (size_t)q0 * ld_out * oes;
+                CK(cudaMemcpy2DAsync(tmp, row_bytes, at, ld_out * oes, row_bytes, w, cudaMemcpyDeviceToDevice,
+                                     ctx->stream));
+                CK(permute_entries(tmp, n, at, ld_out, G->perm_d, n, w, (int)oes, ctx->stream));
+            }
+        }
+    }
     if (out_mem != GDE_MEM_DEVICE) {
         if (x_out) CK(cudaMemcpyAsync(x_out, dx, (size_t)nq * ld_out * oes, cudaMemcpyDeviceToHost, ctx->stream));
         if (r_out) CK(cudaMemcpyAsync(r_out, dr, (size_t)nq * ld_out * oes, cudaMemcpyDeviceToHost, ctx->stream));
@@ -1020,10 +1042,10 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
         if (rc != GDE_OK) return rc;
         const size_t slab = (size_t)nt * n * W * es;
         CK(cudaMemsetAsync(a.R, 0, slab, ctx->stream));
-        CK(cudaMemsetAsync(a.X, 0, slab, ctx->stream));
+        CK(cudaMemsetAsync(a.X, 0, a.xld ? 2 * slab : slab, ctx->stream));  // interleaved: X and XC
         if (a.R2) CK(cudaMemsetAsync(a.R2, 0, slab, ctx->stream));
         if (a.DX) CK(cudaMemsetAsync(a.DX, 0, slab, ctx->stream));
-        if (a.XC) CK(cudaMemsetAsync(a.XC, 0, (size_t)nt * n * W * 4, ctx->stream));
+        if (a.XC && !a.xld) CK(cudaMemsetAsync(a.XC, 0, (size_t)nt * n * W * 4, ctx->stream));
         std::vector<TileParams> tp(nt);
         std::vector<TileState> ts(nt);
         std::vector<ColState> cs((size_t)nt * W);

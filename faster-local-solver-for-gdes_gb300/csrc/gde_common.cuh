@@ -135,7 +135,6 @@ struct ServeQueue {
     void* r_out;                  // [nq][ld_out] residual rows (may be null)
     int64_t ld_out;
     int out64;
-    const int32_t* seed_caller;   // caller seed id per query (Katz GD: x[s] -= 1)
     double seed_add;              // single-kind queues (kind == nullptr): added to x[seed]
     // mixed queues (nullptr: every query is of the launch's tile kind)
     const int32_t* kind;          // KIND_PPR / KIND_KATZ / KIND_HK per query
@@ -207,6 +206,9 @@ struct PushArgs {
     void* R2;                  // HK odd-level residual slab
     void* X;                   // solution slab
     float* XC;                 // Kahan compensation (FP32 solution), may be null
+    int xld;                   // X / XC row stride; 0: the slabs' ld.  2 = interleaved
+                               // {x, c} pairs (W = 1 Kahan slabs: XC = (float*)X + 1)
+    int64_t xtile;             // X / XC offset between tiles (with xld != 0)
     void* DX;                  // Chebyshev delta-x slab
     int32_t* cand;             // [ntiles][2][n] (list storage by parity)
     void* P;                   // [ntiles][n][W] push rows

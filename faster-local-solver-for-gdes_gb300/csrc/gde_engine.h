@@ -48,6 +48,11 @@ int plain_ppr_local(const DevGraph& g, PlainWork& w, int seed, double alpha, dou
 cudaError_t permute_rows(const void* src, int64_t sld, void* dst, int64_t dld, const int32_t* perm, int64_t n,
                          int64_t F, int elem, int to_internal, cudaStream_t st);
 
+// Entry permutation within rows (aux_kernels.cu): per row r < rows,
+// dst[r * dld + u] = src[r * sld + perm[u]] for u < n (internal -> caller order).
+cudaError_t permute_entries(const void* src, int64_t sld, void* dst, int64_t dld, const int32_t* perm, int64_t n,
+                            int64_t rows, int elem, cudaStream_t st);
+
 // Graph helpers (aux_kernels.cu).
 cudaError_t graph_apply_entries(int32_t* col, const int64_t* pos, const int32_t* val, int64_t k, cudaStream_t st);
 

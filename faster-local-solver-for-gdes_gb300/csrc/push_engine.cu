@@ -143,6 +143,14 @@ __device__ __forceinline__ T* slab_ptr(void* base, const PushArgs& a, int t) {
     return reinterpret_cast<T*>(base) + (int64_t)t * a.tile_stride;
 }
 
+// The solution and its Kahan term may be interleaved ({x, c} per node, one
+// sector per random access): their own row stride and tile offset.
+__device__ __forceinline__ int64_t x_ld(const PushArgs& a) { return a.xld ? a.xld : a.ld; }
+template <typename T>
+__device__ __forceinline__ T* xslab_ptr(void* base, const PushArgs& a, int t) {
+    return reinterpret_cast<T*>(base) + (int64_t)t * (a.xld ? a.xtile : a.tile_stride);
+}
+
 // Per-tile data staged in shared memory at the start of each tile's phase.
 struct TileSh {
     TileParams tp;
@@ -344,7 +352,6 @@ __device__ __forceinline__ int find_tile(const long long* off, int ntl, long lon
     return lo;
 }
 
-constexpr long long kRetireChunk = 4096;  // nodes per extraction work item
 
 // This block's share [lo, hi) of a flattened space of `total` items.
 __device__ __forceinline__ void block_share(long long total, long long& lo, long long& hi) {
@@ -440,8 +447,9 @@ __device__ void prep_w1_cross(const PushArgs& a, int t, const TileSh& sh, long l
     const int par = sh.parity;
     const int32_t* cand = a.cand + ((int64_t)t * 2 + par) * n;
     T* R = slab_ptr<T>(a.R, a, t);
-    T* X = slab_ptr<T>(a.X, a, t);
-    float* XC = a.kahan ? slab_ptr<float>(a.XC, a, t) : nullptr;
+    T* X = xslab_ptr<T>(a.X, a, t);
+    float* XC = a.kahan ? xslab_ptr<float>(a.XC, a, t) : nullptr;
+    const int64_t xld = x_ld(a);
     const double alpha = sh.tp.alpha;
     const bool katz = sh.tp.kind == KIND_KATZ;
     const double theta = sh.col_theta[0];
@@ -467,10 +475,10 @@ __device__ void prep_w1_cross(const PushArgs& a, int t, const TileSh& sh, long l
         for (int q = 0; q < kPrepILP; ++q) {
             r[q] = T(0); xv[q] = T(0); df[q] = 1.f; xc[q] = 0.f; len[q] = 0; rp[q] = 0;
             if (val[q]) {
-                const int64_t off = (int64_t)u[q] * ld;
+                const int64_t off = (int64_t)u[q] * ld, xoff = (int64_t)u[q] * xld;
                 r[q] = R[off];
-                xv[q] = X[off];
-                if (XC) xc[q] = XC[off];
+                xv[q] = X[xoff];
+                if (XC) xc[q] = XC[xoff];
                 if (g.rec) {
                     const NodeRec nr = g.rec[u[q]];
                     rp[q] = nr.rp;
@@ -501,16 +509,16 @@ __device__ void prep_w1_cross(const PushArgs& a, int t, const TileSh& sh, long l
                     if (act) push = (T)(katz ? alpha * rv : ((1. - alpha) * rv) / du);
                 }
                 if (act) {
-                    const int64_t off = (int64_t)u[q] * ld;
+                    const int64_t off = (int64_t)u[q] * ld, xoff = (int64_t)u[q] * xld;
                     R[off] = T(0);
                     if (XC) {
                         // Kahan-compensated FP32 accumulation of the solution
                         const float y = (float)r[q] - xc[q];
                         const float s = (float)xv[q] + y;
-                        XC[off] = (s - (float)xv[q]) - y;
-                        X[off] = (T)s;
+                        XC[xoff] = (s - (float)xv[q]) - y;
+                        X[xoff] = (T)s;
                     } else {
-                        X[off] = xv[q] + r[q];
+                        X[xoff] = xv[q] + r[q];
                     }
                     my_nodes += 1;
                     if (g.degf_exact) ideg += (long long)df[q];
@@ -550,8 +558,9 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
     PushItem* blarge = a.blarge + (int64_t)t * a.large_cap;
     TileState& ts = a.ts[t];
     T* R = slab_ptr<T>((hk && (sh.level & 1)) ? a.R2 : a.R, a, t);
-    T* X = slab_ptr<T>(a.X, a, t);
-    float* XC = a.kahan ? slab_ptr<float>(a.XC, a, t) : nullptr;
+    T* X = xslab_ptr<T>(a.X, a, t);
+    float* XC = a.kahan ? xslab_ptr<float>(a.XC, a, t) : nullptr;
+    const int64_t xld = x_ld(a);
     T* DX = cheby ? slab_ptr<T>(a.DX, a, t) : nullptr;
     const double alpha = sh.tp.alpha;
     int* next_cnt = &ts.cand_cnt[(sh.level + 1) % 3];
@@ -597,6 +606,7 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
             if (valid) {
                 u = sh.dense ? (int)i : cand[i];
                 const int64_t off = (int64_t)u * a.ld + c0;
+                const int64_t xoff = (int64_t)u * xld + c0;
                 vload<T, VEC>(R + off, r);
                 // fast test first: most scanned nodes are below every threshold
                 du = g.degf_exact ? (double)g.degf[u] : g.degd[u];
@@ -679,24 +689,24 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
                         vstore<T, VEC>(R + off, r);
                         if (cheby) vstore<T, VEC>(DX + off, dxv);
                         Vec<T, VEC> xv;
-                        vload<T, VEC>(X + off, xv);
+                        vload<T, VEC>(X + xoff, xv);
                         if (absorb) {
                             // p[u] = r[u]; r[u] = 0 for an absorbing node (InstantGNN.py:22-25)
     #pragma unroll
                             for (int k = 0; k < VEC; ++k)
                                 if (act[k]) {
                                     xv.v[k] = xadd.v[k];
-                                    if (XC) XC[off + k] = 0.f;
+                                    if (XC) XC[xoff + k] = 0.f;
                                 }
                         } else if (XC) {
                             // Kahan-compensated FP32 accumulation of the solution
     #pragma unroll
                             for (int k = 0; k < VEC; ++k)
                                 if (act[k]) {
-                                    float cc = XC[off + k];
+                                    float cc = XC[xoff + k];
                                     float y = (float)xadd.v[k] - cc;
                                     float s = (float)xv.v[k] + y;
-                                    XC[off + k] = (s - (float)xv.v[k]) - y;
+                                    XC[xoff + k] = (s - (float)xv.v[k]) - y;
                                     xv.v[k] = (T)s;
                                 }
                         } else {
@@ -704,7 +714,7 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
                             for (int k = 0; k < VEC; ++k)
                                 if (act[k]) xv.v[k] = xv.v[k] + xadd.v[k];
                         }
-                        vstore<T, VEC>(X + off, xv);
+                        vstore<T, VEC>(X + xoff, xv);
                     }
                     any = false;
     #pragma unroll
@@ -851,6 +861,7 @@ __device__ __forceinline__ ScatterCtx<T, W> scatter_ctx(const PushArgs& a, int t
     const int64_t n = a.g.n;
     const int par = level & 1;
     if (flags & SF_HK) {
+        // heat-kernel tiles never interleave X (xld == 0): rows stride a.ld
         if (flags & SF_FINAL) c.tgt = slab_ptr<T>(a.X, a, t);
         else c.tgt = slab_ptr<T>((level & 1) ? a.R : a.R2, a, t);
     } else {
@@ -1396,40 +1407,45 @@ __device__ void admit_query(const PushArgs& a, int t, int it) {
     ts.done = SLOT_LIVE;
 }
 
-// Served solves: write a retiring slot's solution row (caller node order)
-// and clear the slot's vectors, nodes [beg, end) in caller order.
+// Served solves: write a retiring slot's solution row and clear the slot's
+// vectors, internal nodes [beg, end).  The row is written in internal node
+// order (sequential reads, writes and clears); the host permutes finished
+// rows to caller order after the launch (permute_rows_to_caller).
 template <typename T, int W>
 __device__ void retire_range(const PushArgs& a, int t, long long beg, long long end) {
     const ServeQueue& q = a.queue;
     const int qid = a.ts[t].qid;
-    T* X = slab_ptr<T>(a.X, a, t);
+    T* X = xslab_ptr<T>(a.X, a, t);
     T* R = slab_ptr<T>(a.R, a, t);
     T* R2 = a.R2 ? slab_ptr<T>(a.R2, a, t) : nullptr;
-    float* XC = a.kahan ? slab_ptr<float>(a.XC, a, t) : nullptr;
-    const int32_t* perm = a.g.perm;
-    const int sc = q.seed_caller[qid];
+    float* XC = a.kahan ? xslab_ptr<float>(a.XC, a, t) : nullptr;
+    const int64_t xld = x_ld(a);
+    const int si = q.seed[qid];
     const int kind = q.kind ? q.kind[qid] : a.tp[t].kind;
     // Katz GD: xt[s_node] -= 1 (katz_solver.py:243); HK: xt / e^tau (hk_solver.py:295)
     const double seed_add = q.kind ? (kind == KIND_KATZ ? -1.0 : 0.0) : q.seed_add;
     const double xdiv = (kind == KIND_HK) ? q.hk_scale : 1.0;
-    for (long long u = beg + threadIdx.x; u < end; u += kThreads) {
-        const int64_t v = (perm ? (int64_t)perm[u] : u) * a.ld;
-        double x = (double)X[v];
-        if (XC) x -= (double)XC[v];  // Kahan: the sum is X - XC
-        if (u == sc) x = x + seed_add;
+    const int64_t orow = (int64_t)qid * q.ld_out;
+    float* xo32 = (q.x_out && !q.out64) ? reinterpret_cast<float*>(q.x_out) + orow : nullptr;
+    double* xo64 = (q.x_out && q.out64) ? reinterpret_cast<double*>(q.x_out) + orow : nullptr;
+    // streaming (evict-first) loads and output stores: a retiring row is
+    // read and written once and should not push the residual slabs out of L2
+    for (long long v = beg + threadIdx.x; v < end; v += kThreads) {
+        const int64_t o = v * a.ld, xo = v * xld;
+        double x = (double)__ldcs(X + xo);
+        if (XC) x -= (double)__ldcs(XC + xo);  // Kahan: the sum is X - XC
+        if (v == si) x = x + seed_add;
         if (xdiv != 1.0) x = x / xdiv;
-        if (q.x_out) {
-            if (q.out64) reinterpret_cast<double*>(q.x_out)[(int64_t)qid * q.ld_out + u] = x;
-            else reinterpret_cast<float*>(q.x_out)[(int64_t)qid * q.ld_out + u] = (float)x;
-        }
+        if (xo32) __stcs(xo32 + v, (float)x);
+        if (xo64) __stcs(xo64 + v, x);
         if (q.r_out) {
-            if (q.out64) reinterpret_cast<double*>(q.r_out)[(int64_t)qid * q.ld_out + u] = (double)R[v];
-            else reinterpret_cast<float*>(q.r_out)[(int64_t)qid * q.ld_out + u] = (float)R[v];
+            if (q.out64) reinterpret_cast<double*>(q.r_out)[orow + v] = (double)R[o];
+            else reinterpret_cast<float*>(q.r_out)[orow + v] = (float)R[o];
         }
-        X[v] = T(0);
-        R[v] = T(0);
-        if (R2) R2[v] = T(0);
-        if (XC) XC[v] = 0.f;
+        X[xo] = T(0);
+        R[o] = T(0);
+        if (R2) R2[o] = T(0);
+        if (XC) XC[xo] = 0.f;
     }
 }
 
@@ -1570,10 +1586,11 @@ __global__ void __launch_bounds__(kThreads, GDE_MIN_BLOCKS) push_kernel(PushArgs
         __syncthreads();
         block_exclusive_scan(s_vals, ntl, rs.off[2], rs.scan_tmp);
         if (a.serve) {
-            // slots whose query finished this round: extract + clear, chunked
+            // slots whose query finished this round: extract + clear, every
+            // block an equal share of the retiring slots' nodes
             for (int k = threadIdx.x; k < ntl; k += kThreads) {
                 const TileState& ts = a.ts[rs.tiles[k]];
-                s_vals[k] = (ts.front_cnt[rs.level[k] & 1] == 0) ? (n + kRetireChunk - 1) / kRetireChunk : 0;
+                s_vals[k] = (ts.front_cnt[rs.level[k] & 1] == 0) ? n : 0;
             }
             __syncthreads();
             block_exclusive_scan(s_vals, ntl, rs.off[3], rs.scan_tmp);
@@ -1584,7 +1601,7 @@ __global__ void __launch_bounds__(kThreads, GDE_MIN_BLOCKS) push_kernel(PushArgs
                     const long long b = max(lo, rs.off[3][k]) - rs.off[3][k];
                     const long long e = min(hi, rs.off[3][k + 1]) - rs.off[3][k];
                     if (b >= e) continue;
-                    retire_range<T, W>(a, rs.tiles[k], b * kRetireChunk, min((long long)n, e * kRetireChunk));
+                    retire_range<T, W>(a, rs.tiles[k], b, e);
                 }
             }
         }
