@@ -402,9 +402,28 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     if (rc != GDE_OK) return rc;
     const size_t es = prec64 ? 8 : 4;
     const size_t slab = (size_t)S * n * es;
+    // Interleaved FP32 solution slabs: when every query's {x, c} slab fits
+    // in a third of the free memory, each query keeps its own slab (zeroed
+    // here, in one pass) and its row is read out after the launch, so a
+    // retiring slot only clears its residual.
+    a.xq = 0;
+    if (a.xld && x_out) {
+        size_t freeb = 0, totb = 0;
+        cudaMemGetInfo(&freeb, &totb);
+        const size_t need = (size_t)nq * (size_t)a.xtile * 4;
+        if (need <= freeb / 3) {
+            void* xq = wsget(ctx, "Xq", need);
+            if (xq) {
+                a.X = xq;
+                a.XC = (float*)xq + 1;
+                a.xq = 1;
+            }
+        }
+    }
     CK(cudaEventRecord(ctx->ev[2], ctx->stream));
     CK(cudaMemsetAsync(a.R, 0, slab, ctx->stream));
-    CK(cudaMemsetAsync(a.X, 0, a.xld ? 2 * slab : slab, ctx->stream));  // interleaved: X and XC
+    if (a.xq) CK(cudaMemsetAsync(a.X, 0, (size_t)nq * (size_t)a.xtile * 4, ctx->stream));
+    else CK(cudaMemsetAsync(a.X, 0, a.xld ? 2 * slab : slab, ctx->stream));  // interleaved: X and XC
     if (a.R2) CK(cudaMemsetAsync(a.R2, 0, slab, ctx->stream));
     if (a.XC && !a.xld) CK(cudaMemsetAsync(a.XC, 0, (size_t)S * n * 4, ctx->stream));
     // ---- the query queue on the device ----
@@ -569,6 +588,10 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     rc = run_engine(ctx, a, prec64, 1, stats, &kernel_ms);
     if (rc != GDE_OK) return rc;
     // ---- results ----
+    // per-query solution slabs: every solution row at once, in caller order
+    if (a.xq)
+        CK(query_rows((const float*)a.X, a.xtile, G->perm_d, n, nq, d_seed, d_kind, Q.seed_add, dx, out64, ld_out,
+                      ctx->stream));
     // retired rows are in internal node order: permute them to caller order
     // through a wave buffer of a few rows (random reads stay in L2)
     if (G->perm_d) {
@@ -576,7 +599,7 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
         const int64_t wave = std::max<int64_t>(1, std::min<int64_t>(nq, (int64_t)(48 << 20) / row_bytes));
         void* tmp = dev("out_wave", (size_t)(wave * row_bytes));
         if (!tmp) return fail(ctx, GDE_ENOMEM, "output permutation buffer");
-        for (void* rows : {dx, dr}) {
+        for (void* rows : {a.xq ? nullptr : dx, dr}) {
             if (!rows) continue;
             for (int64_t q0 = 0; q0 < nq; q0 += wave) {
                 const int64_t w = std::min<int64_t>(wave, nq - q0);

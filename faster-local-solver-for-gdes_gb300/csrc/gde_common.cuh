@@ -209,6 +209,8 @@ struct PushArgs {
     int xld;                   // X / XC row stride; 0: the slabs' ld.  2 = interleaved
                                // {x, c} pairs (W = 1 Kahan slabs: XC = (float*)X + 1)
     int64_t xtile;             // X / XC offset between tiles (with xld != 0)
+    int xq;                    // served: X / XC slabs per query (indexed by query id), read out
+                               // after the launch; 0: per tile
     void* DX;                  // Chebyshev delta-x slab
     int32_t* cand;             // [ntiles][2][n] (list storage by parity)
     void* P;                   // [ntiles][n][W] push rows

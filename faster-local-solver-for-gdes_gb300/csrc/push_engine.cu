@@ -148,7 +148,8 @@ __device__ __forceinline__ T* slab_ptr(void* base, const PushArgs& a, int t) {
 __device__ __forceinline__ int64_t x_ld(const PushArgs& a) { return a.xld ? a.xld : a.ld; }
 template <typename T>
 __device__ __forceinline__ T* xslab_ptr(void* base, const PushArgs& a, int t) {
-    return reinterpret_cast<T*>(base) + (int64_t)t * (a.xld ? a.xtile : a.tile_stride);
+    const int64_t s = a.xq ? a.ts[t].qid : t;  // served with per-query solution slabs
+    return reinterpret_cast<T*>(base) + s * (a.xld ? a.xtile : a.tile_stride);
 }
 
 // Per-tile data staged in shared memory at the start of each tile's phase.
@@ -1430,6 +1431,20 @@ __device__ void retire_range(const PushArgs& a, int t, long long beg, long long 
     double* xo64 = (q.x_out && q.out64) ? reinterpret_cast<double*>(q.x_out) + orow : nullptr;
     // streaming (evict-first) loads and output stores: a retiring row is
     // read and written once and should not push the residual slabs out of L2
+    if (a.xq) {
+        // the solution stays in the query's own slab (read out after the
+        // launch): only the slot's residual is extracted and cleared here
+        for (long long v = beg + threadIdx.x; v < end; v += kThreads) {
+            const int64_t o = v * a.ld;
+            if (q.r_out) {
+                if (q.out64) reinterpret_cast<double*>(q.r_out)[orow + v] = (double)R[o];
+                else reinterpret_cast<float*>(q.r_out)[orow + v] = (float)R[o];
+            }
+            R[o] = T(0);
+            if (R2) R2[o] = T(0);
+        }
+        return;
+    }
     for (long long v = beg + threadIdx.x; v < end; v += kThreads) {
         const int64_t o = v * a.ld, xo = v * xld;
         double x = (double)__ldcs(X + xo);
