@@ -1141,45 +1141,63 @@ __device__ void scatter_warp_items_w1(const PushArgs& a, const PushItem* items, 
     }
 }
 
-// W = 1 short rows: one lane per row, kEdgeILP consecutive edges of the row
-// per step.  Lanes of a warp whose edges hit the same hub (degree-sorted
-// prefix) in a step add in shared memory first and one lane issues the
+// W = 1 short rows flattened per warp: a warp takes GROUP consecutive items
+// and spreads their edges evenly over its lanes, 32 * kEdgeILP edges per
+// step (the lane holding edge e finds its row by a binary search over the
+// warp's exclusive edge offsets), so a step carries every row's edges
+// instead of one row per lane.  Lanes of a step whose edges hit the same hub
+// (degree-sorted prefix) add in shared memory first and one lane issues the
 // global atomic; the crossing test on the combined add is the same test on
-// the stored value.
-template <typename T>
-__device__ void scatter_small_w1(const PushArgs& a, int t, const ScatterCtx<T, 1>& c, long long beg, long long end) {
+// the stored value.  (Flattening medium rows the same way measured slower
+// than a warp per medium row.)
+template <typename T, int GROUP>
+__device__ void scatter_flat_w1(const PushArgs& a, const PushItem* items, int step, const ScatterCtx<T, 1>& c,
+                                long long beg, long long end) {
     const DevGraph& g = a.g;
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const PushItem* bsmall = a.bsmall + (int64_t)t * g.n;
     const double theta = c.cross ? c.cs[0].theta : 0.0;
-    __shared__ T agg[kWarps][32];
-    for (long long kb = beg + (long long)warp * 32; kb < end; kb += (long long)kWarps * 32) {
+    __shared__ T fagg[kWarps][32];
+    for (long long kb = beg + (long long)warp * GROUP; kb < end; kb += (long long)kWarps * GROUP) {
         const long long k = kb + lane;
         int len = 0;
-        int64_t rp = 0;
+        long long rp = 0;
         T pv = T(0);
-        if (k < end) {
-            const PushItem it = bsmall[k];
+        if (lane < GROUP && k < end) {
+            const PushItem it = items[k * step];
             rp = it.rp;
             len = it.len;
             pv = c.Pw[it.fidx];
         }
-        int maxlen = len;
+        int incl = len;
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) maxlen = max(maxlen, __shfl_xor_sync(kFull, maxlen, o));
-        T p[kEdgeILP];
-#pragma unroll
-        for (int u = 0; u < kEdgeILP; ++u) p[u] = pv;
-        for (int j0 = 0; j0 < maxlen; j0 += kEdgeILP) {
+        for (int o = 1; o < 32; o <<= 1) {
+            const int y = __shfl_up_sync(kFull, incl, o);
+            if (lane >= o) incl += y;
+        }
+        const int total = __shfl_sync(kFull, incl, 31);
+        const int excl = incl - len;
+        for (int e0 = 0; e0 < total; e0 += 32 * kEdgeILP) {
             bool ok[kEdgeILP], hub_done[kEdgeILP], hub_cr[kEdgeILP];
             int v[kEdgeILP];
             uint32_t dc[kEdgeILP];
+            T p[kEdgeILP];
 #pragma unroll
             for (int u = 0; u < kEdgeILP; ++u) {
-                ok[u] = j0 + u < len;
+                const int e = e0 + u * 32 + lane;
+                ok[u] = e < total;
+                // the row holding edge e: the last lane whose offset is <= e
+                int r = 0;
+#pragma unroll
+                for (int b = 16; b > 0; b >>= 1) {
+                    const int ex = __shfl_sync(kFull, excl, (r + b) & 31);
+                    if (r + b < GROUP && ex <= e) r += b;
+                }
+                const long long rpr = __shfl_sync(kFull, rp, r);
+                const int exr = __shfl_sync(kFull, excl, r);
+                p[u] = __shfl_sync(kFull, pv, r);
                 v[u] = 0;
                 dc[u] = 0;
-                if (ok[u]) load_edge(g, rp + j0 + u, v[u], dc[u]);
+                if (ok[u]) load_edge(g, rpr + (e - exr), v[u], dc[u]);
                 hub_done[u] = false;
                 hub_cr[u] = false;
             }
@@ -1190,12 +1208,12 @@ __device__ void scatter_small_w1(const PushArgs& a, int t, const ScatterCtx<T, 1
                     if (!__any_sync(kFull, hub)) continue;
                     const unsigned peers = __match_any_sync(kFull, hub ? v[u] : -1 - lane);
                     const int leader = __ffs(peers) - 1;
-                    if (hub && lane == leader) agg[warp][lane] = T(0);
+                    if (hub && lane == leader) fagg[warp][lane] = T(0);
                     __syncwarp();
-                    if (hub) atomicAdd(&agg[warp][leader], pv);
+                    if (hub) atomicAdd(&fagg[warp][leader], p[u]);
                     __syncwarp();
                     if (hub && lane == leader) {
-                        const T tot = agg[warp][lane];
+                        const T tot = fagg[warp][lane];
                         T* addr = c.tgt + (int64_t)v[u] * a.ld;
                         if (c.cross) {
                             const T old = atomicAdd(addr, tot);
@@ -1218,8 +1236,6 @@ __device__ void scatter_small_w1(const PushArgs& a, int t, const ScatterCtx<T, 1
                         }
                     }
                     __syncwarp();
-                    // non-leader hub lanes are done; the leader keeps ok[u] for
-                    // the (deduplicated) touch append when tracking
                     hub_done[u] = hub;
                 }
             }
@@ -1636,7 +1652,7 @@ __global__ void __launch_bounds__(kThreads, GDE_MIN_BLOCKS) push_kernel(PushArgs
                 if constexpr (W == 1) {
                     if (sp == 2) scatter_warp_items_w1<T>(a, a.blarge + (int64_t)t * a.large_cap, 1, c, b, e);
                     else if (sp == 1) scatter_warp_items_w1<T>(a, a.bsmall + (int64_t)t * n + (n - 1), -1, c, b, e);
-                    else scatter_small_w1<T>(a, t, c, b, e);
+                    else scatter_flat_w1<T, 32>(a, a.bsmall + (int64_t)t * n, 1, c, b, e);
                 } else {
                     if (sp == 2) scatter_warp_items<T, W>(a, a.blarge + (int64_t)t * a.large_cap, 1, c, b, e);
                     else if (sp == 1) scatter_warp_items<T, W>(a, a.bsmall + (int64_t)t * n + (n - 1), -1, c, b, e);
