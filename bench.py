@@ -320,7 +320,10 @@ def run_ours(args):
     per_launch_bytes = bytes_total / launches
     roof = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
             "peak_kind": peak_kind,
-            "traffic": (traffic["dram_bytes_per_query"] * Q if traffic else None),
+            # the small capture's DRAM bytes per edge operation, scaled to this
+            # launch's operations (traffic grows with the pushes)
+            "traffic": (traffic["dram_bytes_per_oper"] * float(np.sum(opers)) / launches
+                        if traffic and opers else None),
             "algorithmic_bytes_per_launch": per_launch_bytes, "kernel": "push_kernel<float,%d>" % args.tile_w,
             "kernel_ms_per_launch": kernel_ms_total / launches}
     lat_sorted = np.sort(np.asarray(lat))
@@ -336,6 +339,7 @@ def run_ours(args):
         "mean_oper": float(np.mean(opers)) if opers else None,
         "rounds_total": agg["rounds"],
         "phase_ms": {k: float(sum(ph[k])) / args.steps for k in ph},
+        # per served step: the push launch, the slot seeding and the solution read-out
         "gpu_launches": int(launches + args.steps * 2),
         "roofline": roof,
         "e2e": {"value": e2e_value, "unit": "queries/s", "h2d_bytes_per_step": Q * (4 + 8),
