@@ -113,17 +113,19 @@ __global__ void permute_entries_kernel(const T* src, int64_t sld, T* dst, int64_
 
 // Served solutions kept per query as interleaved {x, Kahan term} slabs:
 // out[q][u] (caller order) = x - c at internal node perm[u], plus the Katz
-// seed correction xt[s_node] -= 1 (katz_solver.py:243).
+// seed correction xt[s_node] -= 1 (katz_solver.py:243) and the heat
+// kernel's xt / e^tau (hk_solver.py:295).
 template <typename O>
 __global__ void query_rows_kernel(const float* XI, int64_t xtile, const int32_t* perm, int64_t n, int64_t nq,
-                                  const int32_t* seed_int, const int32_t* kinds, double seed_add, O* out,
-                                  int64_t ld_out) {
+                                  const int32_t* seed_int, const int32_t* kinds, double seed_add, double hk_scale,
+                                  O* out, int64_t ld_out) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * nq; i += (int64_t)gridDim.x * blockDim.x) {
         const int64_t q = i / n, u = i % n;
         const int64_t v = perm ? (int64_t)perm[u] : u;
         const float2 xc = *reinterpret_cast<const float2*>(XI + q * xtile + 2 * v);
         double x = (double)xc.x - (double)xc.y;
         if (v == seed_int[q]) x += kinds ? (kinds[q] == KIND_KATZ ? -1.0 : 0.0) : seed_add;
+        if (kinds && kinds[q] == KIND_HK) x = x / hk_scale;
         out[q * ld_out + u] = (O)x;
     }
 }
@@ -187,15 +189,15 @@ cudaError_t permute_entries(const void* src, int64_t sld, void* dst, int64_t dld
 }
 
 cudaError_t query_rows(const float* XI, int64_t xtile, const int32_t* perm, int64_t n, int64_t nq,
-                       const int32_t* seed_int, const int32_t* kinds, double seed_add, void* out, int out64,
-                       int64_t ld_out, cudaStream_t st) {
+                       const int32_t* seed_int, const int32_t* kinds, double seed_add, double hk_scale, void* out,
+                       int out64, int64_t ld_out, cudaStream_t st) {
     if (n == 0 || nq == 0) return cudaSuccess;
     const int blocks = (int)std::min<int64_t>((n * nq + 255) / 256, 152 * 64);
     if (out64)
-        query_rows_kernel<double><<<blocks, 256, 0, st>>>(XI, xtile, perm, n, nq, seed_int, kinds, seed_add,
+        query_rows_kernel<double><<<blocks, 256, 0, st>>>(XI, xtile, perm, n, nq, seed_int, kinds, seed_add, hk_scale,
                                                            (double*)out, ld_out);
     else
-        query_rows_kernel<float><<<blocks, 256, 0, st>>>(XI, xtile, perm, n, nq, seed_int, kinds, seed_add,
+        query_rows_kernel<float><<<blocks, 256, 0, st>>>(XI, xtile, perm, n, nq, seed_int, kinds, seed_add, hk_scale,
                                                           (float*)out, ld_out);
     return cudaGetLastError();
 }

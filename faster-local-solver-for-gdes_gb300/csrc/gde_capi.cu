@@ -128,7 +128,7 @@ int alloc_tiles(gde_ctx* ctx, gde_graph* G, int ntiles, int W, int prec64, bool 
     a.ntiles = ntiles;
     // one-column FP32 Kahan slabs interleave the solution and its Kahan term
     // as {x, c} pairs, so a frontier node's update touches one sector
-    const bool inter = own_slabs && kahan && !prec64 && W == 1 && !need_r2;
+    const bool inter = own_slabs && kahan && !prec64 && W == 1;
     if (own_slabs) {
         a.ld = W;
         a.tile_stride = (int64_t)n * W;
@@ -590,8 +590,8 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     // ---- results ----
     // per-query solution slabs: every solution row at once, in caller order
     if (a.xq)
-        CK(query_rows((const float*)a.X, a.xtile, G->perm_d, n, nq, d_seed, d_kind, Q.seed_add, dx, out64, ld_out,
-                      ctx->stream));
+        CK(query_rows((const float*)a.X, a.xtile, G->perm_d, n, nq, d_seed, d_kind, Q.seed_add, Q.hk_scale, dx, out64,
+                      ld_out, ctx->stream));
     // retired rows are in internal node order: permute them to caller order
     // through a wave buffer of a few rows (random reads stay in L2)
     if (G->perm_d) {

@@ -437,7 +437,10 @@ __device__ __forceinline__ void emit_node_w1(const PushArgs& a, int t, int par, 
 // candidates are exactly last round's threshold crossings.  Each lane takes
 // kPrepILP candidates and issues every per-node load (residual, degree,
 // solution, Kahan term, row start and length) before using any of them.
-constexpr int kPrepILP = 2;
+#ifndef GDE_PREP_ILP
+#define GDE_PREP_ILP 2
+#endif
+constexpr int kPrepILP = GDE_PREP_ILP;
 
 template <typename T>
 __device__ void prep_w1_cross(const PushArgs& a, int t, const TileSh& sh, long long beg, long long end,
@@ -845,6 +848,7 @@ __device__ void zero_next_counters(const PushArgs& a, int t, int level) {
 template <typename T, int W>
 struct ScatterCtx {
     T* tgt;
+    int tld;                // row stride of tgt (the solution slab may interleave {x, c})
     const T* Pw;
     int32_t* mark;
     int32_t* next;
@@ -862,11 +866,17 @@ __device__ __forceinline__ ScatterCtx<T, W> scatter_ctx(const PushArgs& a, int t
     const int64_t n = a.g.n;
     const int par = level & 1;
     if (flags & SF_HK) {
-        // heat-kernel tiles never interleave X (xld == 0): rows stride a.ld
-        if (flags & SF_FINAL) c.tgt = slab_ptr<T>(a.X, a, t);
-        else c.tgt = slab_ptr<T>((level & 1) ? a.R : a.R2, a, t);
+        // the heat kernel's last level pushes straight into the solution
+        if (flags & SF_FINAL) {
+            c.tgt = xslab_ptr<T>(a.X, a, t);
+            c.tld = (int)x_ld(a);
+        } else {
+            c.tgt = slab_ptr<T>((level & 1) ? a.R : a.R2, a, t);
+            c.tld = a.ld;
+        }
     } else {
         c.tgt = slab_ptr<T>(a.R, a, t);
+        c.tld = a.ld;
     }
     c.Pw = reinterpret_cast<const T*>(a.P) + (int64_t)t * n * W;
     c.mark = a.mark + (int64_t)t * n;
@@ -917,7 +927,7 @@ __device__ __forceinline__ void edge_step(const PushArgs& a, const ScatterCtx<T,
                 __syncwarp();
                 if (hub && lane == leader) {
                     const T tot = agg[warp][lane];
-                    T* addr = c.tgt + (int64_t)v * a.ld;
+                    T* addr = c.tgt + (int64_t)v * c.tld;
                     if (c.cross) {
                         const T old = atomicAdd(addr, tot);
                         const T s = old + tot;
@@ -936,7 +946,7 @@ __device__ __forceinline__ void edge_step(const PushArgs& a, const ScatterCtx<T,
     if (ok && !combined) {
         if (c.cross) {
             Vec<T, VEC> old;
-            vatomic_ret<T, VEC>(c.tgt + (int64_t)v * a.ld + c0, p, old);
+            vatomic_ret<T, VEC>(c.tgt + (int64_t)v * c.tld + c0, p, old);
             const double dv = a.g.degf_exact ? (double)a.g.degf[v] : a.g.degd[v];
 #pragma unroll
             for (int k = 0; k < VEC; ++k) {
@@ -946,7 +956,7 @@ __device__ __forceinline__ void edge_step(const PushArgs& a, const ScatterCtx<T,
                 cr |= ((double)old.v[k] < thr) && ((double)s >= thr);
             }
         } else {
-            push_edge<T, VEC>(a.g, c.tgt, a.ld, c0, v, p, c.tgt_scale);
+            push_edge<T, VEC>(a.g, c.tgt, c.tld, c0, v, p, c.tgt_scale);
         }
     }
     if (c.cross) {
@@ -1059,7 +1069,7 @@ __device__ __forceinline__ void edges_w1(const PushArgs& a, const ScatterCtx<T, 
         }
 #pragma unroll
         for (int u = 0; u < kEdgeILP; ++u)
-            old[u] = glob[u] ? atomicAdd(c.tgt + (int64_t)v[u] * a.ld, p[u]) : T(0);
+            old[u] = glob[u] ? atomicAdd(c.tgt + (int64_t)v[u] * c.tld, p[u]) : T(0);
         bool cr[kEdgeILP];
 #pragma unroll
         for (int u = 0; u < kEdgeILP; ++u) {
@@ -1086,7 +1096,7 @@ __device__ __forceinline__ void edges_w1(const PushArgs& a, const ScatterCtx<T, 
             if (!ok[u] || hub_done[u] || p[u] == T(0)) continue;
             T q = p[u];
             if (c.tgt_scale) q = q / ((sizeof(T) == 4) ? (T)g.tfac_f[v[u]] : (T)g.tfac[v[u]]);  // InstantGNN.py:31
-            atomicAdd(c.tgt + (int64_t)v[u] * a.ld, q);
+            atomicAdd(c.tgt + (int64_t)v[u] * c.tld, q);
         }
         if (c.track) {
 #pragma unroll
@@ -1214,7 +1224,7 @@ __device__ void scatter_flat_w1(const PushArgs& a, const PushItem* items, int st
                     __syncwarp();
                     if (hub && lane == leader) {
                         const T tot = fagg[warp][lane];
-                        T* addr = c.tgt + (int64_t)v[u] * a.ld;
+                        T* addr = c.tgt + (int64_t)v[u] * c.tld;
                         if (c.cross) {
                             const T old = atomicAdd(addr, tot);
                             const T s = old + tot;
