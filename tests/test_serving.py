@@ -113,3 +113,43 @@ def test_served_mixed_hbm_budget_caps_slots(cl):
     with pytest.raises(L.GDEError) as ei:
         api.serve_mixed(Gd, kinds, seeds, 1e-6, alphas=0.1, hbm_budget_bytes=1000.0)
     assert ei.value.status == L.GDE_ENOMEM
+
+
+def test_served_fp32_mixed_kinds_close_to_fp64(cl):
+    """FP32 slots (interleaved {x, Kahan term} solution slabs kept per query and
+    read out after the launch): PPR, Katz and heat kernel against FP64 alone."""
+    g, Gd = cl
+    rng = np.random.default_rng(6)
+    nq = 15
+    kinds = np.array([L.PPR, L.KATZ, L.HK] * (nq // 3), dtype=np.int32)
+    rng.shuffle(kinds)
+    seeds = graphs.uniform_seeds(g, nq, seed=23)
+    eps = np.exp(rng.uniform(np.log(1e-6), np.log(1e-5), nq))
+    katz_alpha = 1.0 / (float(g.degree.max()) + 1.0)
+    alphas = np.where(kinds == L.KATZ, katz_alpha, 0.1)
+    tau = 5.0
+    served = api.serve_mixed(Gd, kinds, seeds, eps, alphas=alphas, tau=tau, prec="fp32", slots=4)
+    for i in range(nq):
+        if kinds[i] == L.HK:
+            alone = api.solve(Gd, L.HK, L.HK_LOCAL, seeds[i:i + 1], eps[i:i + 1], prec="fp64", tau=tau, want_r=False)
+        else:
+            alone = api.solve(Gd, int(kinds[i]), L.LOCAL_GD, seeds[i:i + 1], eps[i:i + 1], prec="fp64",
+                              alpha=float(alphas[i]), tile_w=1, want_r=False)
+        # FP32 rounding plus a few threshold flips; a wrong row order, seed
+        # correction or e^tau scale would be off by O(1)
+        assert rel_l1(served["x"][i], alone["x"][0]) < 1e-4, (i, int(kinds[i]))
+
+
+def test_served_fp32_residual_rows_meet_the_stopping_rule(cl):
+    """Served FP32 residual rows come back in caller order: every entry is below
+    its own eps * alpha * d_u, and x and r keep the PPR mass identity."""
+    g, Gd = cl
+    seeds = graphs.uniform_seeds(g, 10, seed=24)
+    eps = 1e-6
+    served = api.serve(Gd, L.PPR, seeds, eps, alpha=0.1, prec="fp32", want_r=True, slots=3)
+    deg = g.degree.astype(np.float64)
+    for i in range(len(seeds)):
+        x = served["x"][i].astype(np.float64)
+        r = served["r"][i].astype(np.float64)
+        assert (np.abs(r) < eps * 0.1 * deg * (1 + 1e-5)).all(), i
+        assert abs(x.sum() + r.sum() / 0.1 - 1.0) < 1e-5, i
