@@ -346,6 +346,14 @@ def run_ours(args):
                 "d2h_bytes_per_step": Q * g.n * 4 + Q * (8 + 4 + 4)},
     }
     out["clocks"] = clk.summary()
+    # the push's own ceiling: uniformly random FP32 atomics (with return) over
+    # an array the size of the slots' residual slabs, against the SCATTER
+    # phase's edge-push rate (its time includes the phase's barrier wait)
+    foot = int(res["stats"]["tiles"]) * args.tile_w * g.n
+    probe = api.probe_random_atomics(foot, True, ctx)
+    scat_rate = agg["col_vol"] / (sum(ph["scatter"]) / 1e3) / 1e9
+    out["random_access"] = {"scatter_atomics_gps": scat_rate, "probe_atomics_gps": probe,
+                            "frac": scat_rate / probe, "footprint_mb": foot * 4 / 1e6}
     if not args.no_baselines:
         # plain single-query GPU baseline (the x20 denominator)
         xs = torch.zeros(g.n, dtype=torch.float32, device=f"cuda:{local}")

@@ -45,6 +45,7 @@ class Stats(ctypes.Structure):
 SIGNATURES = {
     "gde_status_str": (ctypes.c_char_p, [_int]),
     "gde_version": (_int, []),
+    "gde_probe_random_atomics": (_int, [_p, _i64, _int, ctypes.POINTER(ctypes.c_double)]),
     "gde_ctx_create": (_int, [_int, ctypes.POINTER(_p)]),
     "gde_ctx_destroy": (_int, [_p]),
     "gde_last_error": (ctypes.c_char_p, [_p]),

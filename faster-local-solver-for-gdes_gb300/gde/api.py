@@ -349,6 +349,15 @@ def plain_ppr_local(graph: Graph, seed: int, alpha: float, eps: float, x_out=Non
     return oper.value, rounds.value
 
 
+def probe_random_atomics(n_floats: int, with_return: bool = True, ctx: Context | None = None) -> float:
+    """Uniformly random FP32 atomic adds over ``n_floats`` entries, in G atomics/s (the push's ceiling)."""
+    c = ctx or Context.get(0)
+    out = ctypes.c_double()
+    L.check(c.ptr, L.load().gde_probe_random_atomics(c.ptr, int(n_floats), int(with_return), ctypes.byref(out)),
+            "gde_probe_random_atomics")
+    return float(out.value)
+
+
 def hk_estimate_n(tau: float, eps: float) -> int:
     return int(L.load().gde_hk_estimate_n(tau, eps))
 

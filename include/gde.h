@@ -255,6 +255,15 @@ int gde_feature_update(gde_ctx *ctx, gde_graph *g, int32_t *h_indices, int64_t *
 int gde_plain_ppr_local(gde_ctx *ctx, gde_graph *g, int32_t seed, double alpha, double eps, float *x_out,
                         float *r_out, double *oper_out, int32_t *rounds_out);
 
+/* ---- random-access ceiling (measurement) ----
+ * No counterpart in the reference: the rate of uniformly random FP32
+ * atomic adds (with_return != 0: with their return value, as the push's
+ * crossing test uses them) over an array of n_floats entries, in G atomics/s
+ * (best of three launches of 8 blocks x 256 threads per SM, 64 atomics per
+ * thread).  The push kernel's residual scatter is bounded by this rate at its
+ * slabs' size, not by streaming HBM bandwidth. */
+int gde_probe_random_atomics(gde_ctx *ctx, int64_t n_floats, int with_return, double *gops_out);
+
 /* ---- single-query solve that allocates no device memory ----
  * No counterpart in the reference: an addition of this library for callers
  * that must not allocate device memory while serving a request (a host that

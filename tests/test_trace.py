@@ -43,3 +43,14 @@ def test_trace_timeline_is_ordered_and_barriers_hold():
         first_out = t[:, :, leave].min(axis=1)
         assert (first_out + TICK_NS >= last_in).all()
     assert api.trace_read().size == 0
+
+
+def test_random_atomic_probe_reports_a_rate():
+    """The random-access ceiling probe runs and gives a plausible positive rate."""
+    small = api.probe_random_atomics(1 << 20)
+    large = api.probe_random_atomics(64 << 20)
+    assert 0.1 < large < 10_000 and 0.1 < small < 10_000
+    # an L2-resident array is at least as fast as a 256 MB one
+    assert small > 0.8 * large
+    with pytest.raises(L.GDEError):
+        api.probe_random_atomics(0)
