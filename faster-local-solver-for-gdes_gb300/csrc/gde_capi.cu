@@ -504,7 +504,19 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     const size_t oes = out64 ? 8 : 4;
     void* dx = nullptr;
     void* dr = nullptr;
-    if (x_out) dx = (out_mem == GDE_MEM_DEVICE) ? x_out : dev("serve_x", (size_t)nq * ld_out * oes);
+    // pinned host rows the device can address (cudaHostAlloc'd or registered):
+    // per-query solution rows are written there directly after the launch,
+    // with no staging buffer and no separate copy
+    bool x_direct = false;
+    if (x_out && out_mem != GDE_MEM_DEVICE && a.xq) {
+        cudaPointerAttributes pa{};
+        if (cudaPointerGetAttributes(&pa, x_out) == cudaSuccess && pa.type == cudaMemoryTypeHost && pa.devicePointer) {
+            dx = pa.devicePointer;
+            x_direct = true;
+        }
+        cudaGetLastError();
+    }
+    if (x_out && !dx) dx = (out_mem == GDE_MEM_DEVICE) ? x_out : dev("serve_x", (size_t)nq * ld_out * oes);
     if (r_out) dr = (out_mem == GDE_MEM_DEVICE) ? r_out : dev("serve_r", (size_t)nq * ld_out * oes);
     if ((x_out && !dx) || (r_out && !dr)) return fail(ctx, GDE_ENOMEM, "output staging");
     // ---- the first S queries start in the slots ----
@@ -611,7 +623,8 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
         }
     }
     if (out_mem != GDE_MEM_DEVICE) {
-        if (x_out) CK(cudaMemcpyAsync(x_out, dx, (size_t)nq * ld_out * oes, cudaMemcpyDeviceToHost, ctx->stream));
+        if (x_out && !x_direct)
+            CK(cudaMemcpyAsync(x_out, dx, (size_t)nq * ld_out * oes, cudaMemcpyDeviceToHost, ctx->stream));
         if (r_out) CK(cudaMemcpyAsync(r_out, dr, (size_t)nq * ld_out * oes, cudaMemcpyDeviceToHost, ctx->stream));
     }
     std::vector<double> hop(nq);

@@ -153,3 +153,16 @@ def test_served_fp32_residual_rows_meet_the_stopping_rule(cl):
         r = served["r"][i].astype(np.float64)
         assert (np.abs(r) < eps * 0.1 * deg * (1 + 1e-5)).all(), i
         assert abs(x.sum() + r.sum() / 0.1 - 1.0) < 1e-5, i
+
+
+def test_served_rows_into_pinned_host_memory(cl):
+    """Pinned host rows are written directly by the device; pageable rows go through staging."""
+    import torch
+    g, Gd = cl
+    seeds = graphs.uniform_seeds(g, 12, seed=25)
+    pinned = torch.zeros((12, g.n), dtype=torch.float32).pin_memory()
+    a = api.serve(Gd, L.PPR, seeds, 1e-6, alpha=0.1, prec="fp32", x_out=pinned, device_out=False, slots=4)
+    b = api.serve(Gd, L.PPR, seeds, 1e-6, alpha=0.1, prec="fp32", slots=4)  # numpy rows
+    np.testing.assert_allclose(a["oper"], b["oper"], rtol=1e-3)
+    for i in range(12):
+        assert rel_l1(pinned[i].numpy(), b["x"][i].astype(np.float64)) < 1e-5, i
