@@ -547,8 +547,10 @@ def run_c5(args):
     Pd = torch.zeros_like(Xd)
     Rd = Xd.clone()
     stream = torch.cuda.ExternalStream(api.ctx_stream(G.ctx), device=dev)
+    # --tuning tile_w=W: columns per tile (0 = the library's default)
+    tw = int(dict(kv.split("=") for kv in filter(None, args.tuning.split(","))).get("tile_w", 0))
     t0 = time.perf_counter()
-    api.feature_push(G, L.IGN, Pd, Rd, eps, alpha=ALPHA, beta=beta, prec="fp32")
+    api.feature_push(G, L.IGN, Pd, Rd, eps, alpha=ALPHA, beta=beta, prec="fp32", tile_w=tw)
     torch.cuda.synchronize()
     init_s = time.perf_counter() - t0
     mlp = {}
@@ -567,7 +569,7 @@ def run_c5(args):
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
             outs.append(api.feature_update(G, L.IGN, indices, degree, dyn.Us[s], dyn.Vs[s], True, Pd, Rd, Xd, eps,
-                                           alpha=ALPHA, beta=beta, prec="fp32"))
+                                           alpha=ALPHA, beta=beta, prec="fp32", tile_w=tw))
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
@@ -582,7 +584,7 @@ def run_c5(args):
         "dtype": "f32", "data": "synthetic",
         "config": {"workload": "instantgnn_update_fp32_128col_chung_lu_169k", "n": n, "features": F,
                    "snapshots": snaps, "edges_per_snapshot": int(dyn.Us.shape[1]), "alpha": ALPHA, "beta": beta,
-                   "eps": eps, "initial_push_s": init_s},
+                   "eps": eps, "initial_push_s": init_s, "tile_w": tw or "default"},
         "column_updates_per_s": snaps * F / (total_ms / 1e3),
         "push_kernel_ms_per_step": agg["kernel_ms"] / snaps,
         "mean_oper_per_column": float(np.mean([o["oper"].mean() for o in outs])),
