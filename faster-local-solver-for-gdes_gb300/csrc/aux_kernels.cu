@@ -105,10 +105,9 @@ __global__ void permute_rows_kernel(const T* src, int64_t sld, T* dst, int64_t d
 template <typename T>
 __global__ void permute_entries_kernel(const T* src, int64_t sld, T* dst, int64_t dld, const int32_t* perm, int64_t n,
                                        int64_t rows) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * rows; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t r = i / n, u = i % n;
-        dst[r * dld + u] = src[r * sld + perm[u]];
-    }
+    for (int64_t r = blockIdx.y; r < rows; r += gridDim.y)
+        for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x)
+            dst[r * dld + u] = src[r * sld + perm[u]];
 }
 
 // Served solutions kept per query as interleaved {x, Kahan term} slabs:
@@ -119,14 +118,44 @@ template <typename O>
 __global__ void query_rows_kernel(const float* XI, int64_t xtile, const int32_t* perm, int64_t n, int64_t nq,
                                   const int32_t* seed_int, const int32_t* kinds, double seed_add, double hk_scale,
                                   O* out, int64_t ld_out) {
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n * nq; i += (int64_t)gridDim.x * blockDim.x) {
-        const int64_t q = i / n, u = i % n;
-        const int64_t v = perm ? (int64_t)perm[u] : u;
-        const float2 xc = *reinterpret_cast<const float2*>(XI + q * xtile + 2 * v);
-        double x = (double)xc.x - (double)xc.y;
-        if (v == seed_int[q]) x += kinds ? (kinds[q] == KIND_KATZ ? -1.0 : 0.0) : seed_add;
-        if (kinds && kinds[q] == KIND_HK) x = x / hk_scale;
-        out[q * ld_out + u] = (O)x;
+    // rows by blockIdx.y, nodes by blockIdx.x: no 64-bit division per entry
+    for (int64_t q = blockIdx.y; q < nq; q += gridDim.y) {
+        const float* xq = XI + q * xtile;
+        const int64_t s = seed_int[q];
+        const double add = kinds ? (kinds[q] == KIND_KATZ ? -1.0 : 0.0) : seed_add;
+        const bool hk = kinds && kinds[q] == KIND_HK;
+        O* oq = out + q * ld_out;
+        for (int64_t u = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; u < n; u += (int64_t)gridDim.x * blockDim.x) {
+            const int64_t v = perm ? (int64_t)perm[u] : u;
+            const float2 xc = *reinterpret_cast<const float2*>(xq + 2 * v);
+            double x = (double)xc.x - (double)xc.y;
+            if (v == s) x += add;
+            if (hk) x = x / hk_scale;
+            oq[u] = (O)x;
+        }
+    }
+}
+
+// The same read-out walking each slab in internal order (sequential {x, c}
+// reads) and scattering into the caller-order row, which stays in L2 while
+// it is written; used for device rows.
+template <typename O>
+__global__ void query_rows_scatter_kernel(const float* XI, int64_t xtile, const int32_t* iperm, int64_t n, int64_t nq,
+                                          const int32_t* seed_int, const int32_t* kinds, double seed_add,
+                                          double hk_scale, O* out, int64_t ld_out) {
+    for (int64_t q = blockIdx.y; q < nq; q += gridDim.y) {
+        const float2* xq = reinterpret_cast<const float2*>(XI + q * xtile);
+        const int64_t s = seed_int[q];
+        const double add = kinds ? (kinds[q] == KIND_KATZ ? -1.0 : 0.0) : seed_add;
+        const bool hk = kinds && kinds[q] == KIND_HK;
+        O* oq = out + q * ld_out;
+        for (int64_t v = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; v < n; v += (int64_t)gridDim.x * blockDim.x) {
+            const float2 xc = xq[v];
+            double x = (double)xc.x - (double)xc.y;
+            if (v == s) x += add;
+            if (hk) x = x / hk_scale;
+            oq[iperm[v]] = (O)x;
+        }
     }
 }
 
@@ -178,8 +207,7 @@ cudaError_t permute_rows(const void* src, int64_t sld, void* dst, int64_t dld, c
 cudaError_t permute_entries(const void* src, int64_t sld, void* dst, int64_t dld, const int32_t* perm, int64_t n,
                             int64_t rows, int elem, cudaStream_t st) {
     if (n == 0 || rows == 0) return cudaSuccess;
-    const int64_t total = n * rows;
-    const int blocks = (int)std::min<int64_t>((total + 255) / 256, 8192);
+    const dim3 blocks((unsigned)std::min<int64_t>((n + 255) / 256, 2048), (unsigned)std::min<int64_t>(rows, 65535));
     if (elem == 8)
         permute_entries_kernel<double><<<blocks, 256, 0, st>>>((const double*)src, sld, (double*)dst, dld, perm, n,
                                                                 rows);
@@ -188,11 +216,20 @@ cudaError_t permute_entries(const void* src, int64_t sld, void* dst, int64_t dld
     return cudaGetLastError();
 }
 
-cudaError_t query_rows(const float* XI, int64_t xtile, const int32_t* perm, int64_t n, int64_t nq,
-                       const int32_t* seed_int, const int32_t* kinds, double seed_add, double hk_scale, void* out,
-                       int out64, int64_t ld_out, cudaStream_t st) {
+cudaError_t query_rows(const float* XI, int64_t xtile, const int32_t* perm, const int32_t* iperm, int64_t n,
+                       int64_t nq, const int32_t* seed_int, const int32_t* kinds, double seed_add, double hk_scale,
+                       void* out, int out64, int64_t ld_out, cudaStream_t st) {
     if (n == 0 || nq == 0) return cudaSuccess;
-    const int blocks = (int)std::min<int64_t>((n * nq + 255) / 256, 152 * 64);
+    const dim3 blocks((unsigned)std::min<int64_t>((n + 255) / 256, 2048), (unsigned)std::min<int64_t>(nq, 65535));
+    if (iperm) {
+        if (out64)
+            query_rows_scatter_kernel<double><<<blocks, 256, 0, st>>>(XI, xtile, iperm, n, nq, seed_int, kinds,
+                                                                       seed_add, hk_scale, (double*)out, ld_out);
+        else
+            query_rows_scatter_kernel<float><<<blocks, 256, 0, st>>>(XI, xtile, iperm, n, nq, seed_int, kinds,
+                                                                      seed_add, hk_scale, (float*)out, ld_out);
+        return cudaGetLastError();
+    }
     if (out64)
         query_rows_kernel<double><<<blocks, 256, 0, st>>>(XI, xtile, perm, n, nq, seed_int, kinds, seed_add, hk_scale,
                                                            (double*)out, ld_out);

@@ -602,8 +602,8 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     // ---- results ----
     // per-query solution slabs: every solution row at once, in caller order
     if (a.xq)
-        CK(query_rows((const float*)a.X, a.xtile, G->perm_d, n, nq, d_seed, d_kind, Q.seed_add, Q.hk_scale, dx, out64,
-                      ld_out, ctx->stream));
+        CK(query_rows((const float*)a.X, a.xtile, G->perm_d, x_direct ? nullptr : G->iperm_d, n, nq, d_seed, d_kind,
+                      Q.seed_add, Q.hk_scale, dx, out64, ld_out, ctx->stream));
     // retired rows are in internal node order: permute them to caller order
     // through a wave buffer of a few rows (random reads stay in L2)
     if (G->perm_d) {
@@ -923,6 +923,11 @@ int gde_graph_upload(gde_ctx* ctx, int64_t n, int64_t cap, const int64_t* indptr
     if (G->relabeled) {
         CK(cudaMalloc(&G->perm_d, n * sizeof(int32_t)));
         CK(cudaMemcpyAsync(G->perm_d, G->h_perm.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+        std::vector<int32_t> inv(n);
+        for (int64_t u = 0; u < n; u++) inv[G->h_perm[u]] = (int32_t)u;
+        CK(cudaMalloc(&G->iperm_d, n * sizeof(int32_t)));
+        CK(cudaMemcpyAsync(G->iperm_d, inv.data(), n * sizeof(int32_t), cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaStreamSynchronize(ctx->stream));  // inv is released on return
     }
     G->g.perm = G->perm_d;
     // hubs: the degree-sorted prefix of nodes with more than 64 neighbours;
@@ -950,7 +955,7 @@ int gde_graph_free(gde_graph* G) {
     cudaSetDevice(G->ctx->device);
     cudaStreamSynchronize(G->ctx->stream);
     cudaFree(G->row_ptr); cudaFree(G->col); cudaFree(G->row_len); cudaFree(G->degf); cudaFree(G->degd);
-    cudaFree(G->nfac); cudaFree(G->tfac); cudaFree(G->tfac_f); cudaFree(G->perm_d);
+    cudaFree(G->nfac); cudaFree(G->tfac); cudaFree(G->tfac_f); cudaFree(G->perm_d); cudaFree(G->iperm_d);
     cudaFree(G->col_deg); cudaFree(G->rec);
     cudaFree(G->pw1); cudaFree(G->pwb);
     delete G;

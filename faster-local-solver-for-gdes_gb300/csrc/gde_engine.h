@@ -56,10 +56,12 @@ cudaError_t permute_entries(const void* src, int64_t sld, void* dst, int64_t dld
 // Served solutions kept per query ({x, Kahan term} slabs with tile offset
 // xtile, internal node order) -> caller-order rows out[q * ld_out + u]
 // (aux_kernels.cu); the Katz seed entry gets -1 (kinds null: seed_add) and
-// heat-kernel rows are divided by hk_scale = e^tau.
-cudaError_t query_rows(const float* XI, int64_t xtile, const int32_t* perm, int64_t n, int64_t nq,
-                       const int32_t* seed_int, const int32_t* kinds, double seed_add, double hk_scale, void* out,
-                       int out64, int64_t ld_out, cudaStream_t st);
+// heat-kernel rows are divided by hk_scale = e^tau.  With iperm (internal ->
+// caller) the slabs are read in internal order and scattered into the rows
+// (device rows); else the rows are gathered through perm (null: no relabel).
+cudaError_t query_rows(const float* XI, int64_t xtile, const int32_t* perm, const int32_t* iperm, int64_t n,
+                       int64_t nq, const int32_t* seed_int, const int32_t* kinds, double seed_add, double hk_scale,
+                       void* out, int out64, int64_t ld_out, cudaStream_t st);
 
 // Graph helpers (aux_kernels.cu).
 cudaError_t graph_apply_entries(int32_t* col, const int64_t* pos, const int32_t* val, int64_t k, cudaStream_t st);

@@ -73,6 +73,7 @@ struct gde_graph {
     bool relabeled = false;
     std::vector<int32_t> h_perm;
     int32_t* perm_d = nullptr;
+    int32_t* iperm_d = nullptr;  // internal id -> caller id (relabelled graphs)
     uint32_t* col_deg = nullptr;
     gde::NodeRec* rec = nullptr;
     int32_t node_in(int64_t u) const { return relabeled ? h_perm[u] : (int32_t)u; }
