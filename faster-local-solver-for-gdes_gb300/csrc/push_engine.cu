@@ -171,15 +171,9 @@ struct TileSh {
     double col_theta[kMaxW];
 };
 
-constexpr int kMaxTiles = 4096;
-
 __device__ __forceinline__ bool is_absorbing(const DevGraph& g, int u) {
     int len = g.row_len[u];
     return len == 0 || (len == 1 && g.col[g.row_ptr[u]] == u);
-}
-
-__device__ __forceinline__ bool hk_last_level(const TileSh& sh) {
-    return (sh.tp.method == M_HK_TAYLOR) ? (sh.level >= sh.tp.n_levels) : (sh.level + 1 >= sh.tp.n_levels);
 }
 
 // Load the state of tile t at launch iteration `it` (block-wide).
