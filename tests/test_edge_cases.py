@@ -132,3 +132,26 @@ def test_device_outputs(cl):
     assert np.isfinite(xd).all()
     # same algorithm, FP32 atomics in a different order: a few threshold flips at most
     assert np.abs(xd - host["x"]).sum() / np.abs(host["x"]).sum() < 1e-4
+
+
+def test_served_on_a_padded_graph_matches_compact():
+    """Served FP32 and FP64 queries on an unrelabelled padded CSR (no permutation on the
+    read-out) agree with the relabelled compact graph."""
+    g = graphs.chung_lu(800, 2.2, 6.0, 80.0, seed=7)
+    n = g.n
+    deg = np.diff(g.indptr)
+    cap = deg + 2
+    ip = np.zeros(n + 1, np.int64)
+    np.cumsum(cap, out=ip[1:])
+    ix = np.full(ip[-1], n, np.int32)
+    for u in range(n):
+        ix[ip[u]:ip[u] + deg[u]] = g.indices[g.indptr[u]:g.indptr[u + 1]]
+    Gp = api.Graph(ip, ix, row_len=deg.astype(np.int64), degree=deg.astype(np.float64))
+    Gc = api.Graph(g.indptr, g.indices)
+    seeds = graphs.uniform_seeds(g, 9, seed=11)
+    for prec, tol in (("fp64", 1e-12), ("fp32", 1e-5)):
+        a = api.serve(Gp, L.KATZ, seeds, 1e-6, alpha=1.0 / (float(deg.max()) + 1.0), prec=prec, slots=3)
+        b = api.serve(Gc, L.KATZ, seeds, 1e-6, alpha=1.0 / (float(deg.max()) + 1.0), prec=prec, slots=3)
+        for i in range(len(seeds)):
+            xa, xb = a["x"][i].astype(np.float64), b["x"][i].astype(np.float64)
+            assert np.abs(xa - xb).sum() <= tol * max(np.abs(xb).sum(), 1.0), (prec, i)
