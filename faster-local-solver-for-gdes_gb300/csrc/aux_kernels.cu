@@ -159,6 +159,23 @@ __global__ void query_rows_scatter_kernel(const float* XI, int64_t xtile, const 
     }
 }
 
+// Per-node degree tables of the nodes an edge batch touched (rec[i] for node
+// ids[i]); the InstantGNN tables only when nf is given.
+__global__ void node_tables_kernel(int64_t nn, const NodeTables* rec, int32_t* row_len, double* degd, float* degf,
+                                   double* nfac, double* tfac, float* tfac_f) {
+    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nn; i += (int64_t)gridDim.x * blockDim.x) {
+        const NodeTables r = rec[i];
+        row_len[r.id] = r.len;
+        degd[r.id] = r.degd;
+        degf[r.id] = (float)r.degd;
+        if (nfac) {
+            nfac[r.id] = r.nf;
+            tfac[r.id] = r.tf;
+            tfac_f[r.id] = (float)r.tf;
+        }
+    }
+}
+
 __global__ void apply_entries_kernel(int32_t* col, const int64_t* pos, const int32_t* val, int64_t k) {
     for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < k; i += (int64_t)gridDim.x * blockDim.x)
         col[pos[i]] = val[i];
@@ -236,6 +253,14 @@ cudaError_t query_rows(const float* XI, int64_t xtile, const int32_t* perm, cons
     else
         query_rows_kernel<float><<<blocks, 256, 0, st>>>(XI, xtile, perm, n, nq, seed_int, kinds, seed_add, hk_scale,
                                                           (float*)out, ld_out);
+    return cudaGetLastError();
+}
+
+cudaError_t node_tables(int64_t nn, const NodeTables* rec, int32_t* row_len, double* degd, float* degf, double* nfac,
+                        double* tfac, float* tfac_f, cudaStream_t st) {
+    if (nn == 0) return cudaSuccess;
+    const int blocks = (int)std::min<int64_t>((nn + 255) / 256, 4096);
+    node_tables_kernel<<<blocks, 256, 0, st>>>(nn, rec, row_len, degd, degf, nfac, tfac, tfac_f);
     return cudaGetLastError();
 }
 

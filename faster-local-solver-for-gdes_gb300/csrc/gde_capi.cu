@@ -1476,6 +1476,51 @@ int gde_internal_graph_refresh(gde_ctx* ctx, gde_graph* G, const int64_t* h_degr
     int rc = upload_degrees(ctx, G);
     if (rc != GDE_OK) return rc;
     if (ign) return upload_ign_tables(ctx, G, beta);
+    if (G->nfac && !std::isnan(G->ign_beta)) return upload_ign_tables(ctx, G, G->ign_beta);
+    return GDE_OK;
+}
+
+// The same after an edge batch that changed the degrees of `nodes` only: the
+// column entries, and the degree and InstantGNN tables of those nodes.
+int gde_internal_graph_refresh_nodes(gde_ctx* ctx, gde_graph* G, const int64_t* h_degree, const int64_t* nodes,
+                                     int64_t nn, const int64_t* pos, const int32_t* val, int64_t nchg, double beta,
+                                     int ign) {
+    // the InstantGNN tables are kept for the graph's last beta: another beta rebuilds them all;
+    // tables built earlier follow every later edit, whatever the kind of the update
+    if (ign && (!G->nfac || std::isnan(G->ign_beta) || G->ign_beta != beta))
+        return gde_internal_graph_refresh(ctx, G, h_degree, pos, val, nchg, beta, ign);
+    const bool tabs = G->nfac && !std::isnan(G->ign_beta);
+    const double tb = G->ign_beta;
+    if (nchg > 0) {
+        int64_t* d_pos = (int64_t*)wsget(ctx, "edit_pos", nchg * 8);
+        int32_t* d_val = (int32_t*)wsget(ctx, "edit_val", nchg * 4);
+        if (!d_pos || !d_val) return fail(ctx, GDE_ENOMEM, "edit buffers");
+        CK(cudaMemcpyAsync(d_pos, pos, nchg * 8, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(d_val, val, nchg * 4, cudaMemcpyHostToDevice, ctx->stream));
+        CK(graph_apply_entries(G->col, d_pos, d_val, nchg, ctx->stream));
+    }
+    if (nn == 0) return GDE_OK;
+    std::vector<NodeTables> rec((size_t)nn);
+    for (int64_t i = 0; i < nn; i++) {
+        const int64_t u = nodes[i];
+        const double d = (double)h_degree[u];
+        G->g.vol += d - G->h_deg[u];
+        G->h_len[u] = h_degree[u];
+        G->h_deg[u] = d;
+        if ((double)(float)d != d) G->g.degf_exact = 0;
+        NodeTables& r = rec[i];
+        r.id = (int32_t)u;
+        r.len = (int32_t)h_degree[u];
+        r.degd = d;
+        r.nf = tabs ? std::pow(d, 1 - tb) : 0.0;  // as upload_ign_tables
+        r.tf = tabs ? std::pow(d, tb) : 0.0;
+    }
+    NodeTables* d_rec = (NodeTables*)wsget(ctx, "edit_nodes", (size_t)nn * sizeof(NodeTables));
+    if (!d_rec) return fail(ctx, GDE_ENOMEM, "edit buffers");
+    CK(cudaMemcpyAsync(d_rec, rec.data(), (size_t)nn * sizeof(NodeTables), cudaMemcpyHostToDevice, ctx->stream));
+    CK(node_tables(nn, d_rec, G->row_len, G->degd, G->degf, tabs ? G->nfac : nullptr, tabs ? G->tfac : nullptr,
+                   tabs ? G->tfac_f : nullptr, ctx->stream));
+    CK(cudaStreamSynchronize(ctx->stream));  // rec is released on return
     return GDE_OK;
 }
 

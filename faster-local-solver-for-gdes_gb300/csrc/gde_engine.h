@@ -63,6 +63,15 @@ cudaError_t query_rows(const float* XI, int64_t xtile, const int32_t* perm, cons
                        int64_t nq, const int32_t* seed_int, const int32_t* kinds, double seed_add, double hk_scale,
                        void* out, int out64, int64_t ld_out, cudaStream_t st);
 
+// One touched node's degree tables after an edge batch.
+struct NodeTables {
+    int32_t id, len;
+    double degd, nf, tf;  // degree; InstantGNN d^(1-beta), d^beta
+};
+// Write the tables of nn touched nodes (nfac null: degrees only).
+cudaError_t node_tables(int64_t nn, const NodeTables* rec, int32_t* row_len, double* degd, float* degf, double* nfac,
+                        double* tfac, float* tfac_f, cudaStream_t st);
+
 // Graph helpers (aux_kernels.cu).
 cudaError_t graph_apply_entries(int32_t* col, const int64_t* pos, const int32_t* val, int64_t k, cudaStream_t st);
 

@@ -35,6 +35,9 @@ int gde_internal_feature_push(gde_ctx* ctx, gde_graph* G, const gde_params* p, i
                               gde_stats* stats);
 int gde_internal_graph_refresh(gde_ctx* ctx, gde_graph* G, const int64_t* h_degree, const int64_t* pos,
                                const int32_t* val, int64_t nchg, double beta, int ign);
+int gde_internal_graph_refresh_nodes(gde_ctx* ctx, gde_graph* G, const int64_t* h_degree, const int64_t* nodes,
+                                     int64_t nn, const int64_t* pos, const int32_t* val, int64_t nchg, double beta,
+                                     int ign);
 int gde_internal_graph_host(gde_graph* G, const int64_t** indptr, const int64_t** len, int64_t* n);
 void* gde_internal_wsget(gde_ctx* ctx, const char* name, size_t bytes);
 int gde_internal_fail(gde_ctx* ctx, int code, const char* msg);
@@ -636,8 +639,15 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
     pos.erase(std::unique(pos.begin(), pos.end()), pos.end());
     val.resize(pos.size());
     for (size_t i = 0; i < pos.size(); i++) val[i] = h_indices[pos[i]];
-    int rc = gde_internal_graph_refresh(ctx, G, h_degree, pos.data(), val.data(), (int64_t)pos.size(), p->beta,
-                                        kind == KIND_IGN);
+    // only the nodes whose degree changed get new degree tables
+    std::vector<int64_t> touched;
+    touched.reserve(ins.keys.size() + del.keys.size());
+    for (int64_t u : ins.keys) touched.push_back(u);
+    for (int64_t u : del.keys) touched.push_back(u);
+    std::sort(touched.begin(), touched.end());
+    touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
+    int rc = gde_internal_graph_refresh_nodes(ctx, G, h_degree, touched.data(), (int64_t)touched.size(), pos.data(),
+                                              val.data(), (int64_t)pos.size(), p->beta, kind == KIND_IGN);
     if (rc != GDE_OK) return rc;
     if (status != GDE_OK)
         return gde_internal_fail(ctx, status, status == GDE_ECAPACITY ? "padded row has no slack for an insertion"

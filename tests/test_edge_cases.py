@@ -155,3 +155,35 @@ def test_served_on_a_padded_graph_matches_compact():
         for i in range(len(seeds)):
             xa, xb = a["x"][i].astype(np.float64), b["x"][i].astype(np.float64)
             assert np.abs(xa - xb).sum() <= tol * max(np.abs(xb).sum(), 1.0), (prec, i)
+
+
+def test_tables_follow_edits_of_another_kind():
+    """An InstantGNN push after a dynamic-PPR edit batch (insertions and deletions) on the same
+    graph sees the edited degrees: it equals the push on a fresh upload of the edited arrays."""
+    import torch
+    import golden_cases as GC
+    dy = GC.dyn()
+    n = len(dy["indptr"]) - 1
+    ip = dy["indptr"].copy()
+    ix = dy["indices"].astype(np.int32).copy()
+    dg = dy["degree"].astype(np.int64).copy()
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    X = dy["X"]
+    alpha, eps, beta = 0.1, 1e-4, 0.5
+    P = torch.zeros(X.shape, dtype=torch.float64, device="cuda")
+    R = torch.from_numpy(X.copy()).cuda()
+    api.feature_push(Gd, L.IGN, P, R, eps, alpha=alpha, beta=beta, prec="fp64")  # builds the beta tables
+    Pu = torch.zeros((n, 2), dtype=torch.float64, device="cuda")
+    Ru = torch.zeros((n, 2), dtype=torch.float64, device="cuda")
+    api.feature_update(Gd, L.UPPR, ix, dg, dy["Us"][0], dy["Vs"][0], False, Pu, Ru, None, eps, alpha=alpha,
+                       prec="fp64")
+    assert not np.array_equal(dg, dy["degree"])  # the batch changed degrees
+    fresh = api.Graph(ip, ix.copy(), row_len=dg.copy(), degree=dg.astype(np.float64))
+    out = []
+    for G in (Gd, fresh):
+        P2 = torch.zeros(X.shape, dtype=torch.float64, device="cuda")
+        R2 = torch.from_numpy(X.copy()).cuda()
+        res = api.feature_push(G, L.IGN, P2, R2, eps, alpha=alpha, beta=beta, prec="fp64")
+        out.append((res["oper"], P2.cpu().numpy()))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-12, atol=1e-15)
