@@ -549,6 +549,9 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
         }
         DeviceInsert D = device_insert(ctx, G, h_indices, h_degree, us, vs, k, kind, p->beta);
         if (D.status != GDE_OK) return D.status;
+        // InstantGNN tables built for an earlier call are not updated by this
+        // kind's edit: the next InstantGNN call rebuilds them
+        if (kind != KIND_IGN) G->ign_beta = NAN;
         if (!D.fallback) {
             cudaStream_t st = gde_internal_stream(ctx);
             const int prec64 = (p->prec == GDE_FP64);
