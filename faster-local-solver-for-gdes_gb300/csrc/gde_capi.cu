@@ -411,7 +411,11 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
         size_t freeb = 0, totb = 0;
         cudaMemGetInfo(&freeb, &totb);
         const size_t need = (size_t)nq * (size_t)a.xtile * 4;
-        if (need <= freeb / 3) {
+        // under an HBM budget the query slabs count against it with the slots
+        const bool in_budget = budget_bytes <= 0.0 ||
+                               (double)S * (double)served_slot_bytes(n, G->g.cap, prec64, any_hk, base) +
+                                       (double)need <= budget_bytes;
+        if (need <= freeb / 3 && in_budget) {
             void* xq = wsget(ctx, "Xq", need);
             if (xq) {
                 a.X = xq;
