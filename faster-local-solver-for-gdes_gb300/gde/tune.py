@@ -22,6 +22,8 @@ from gde import api
 SHAPES = [
     {"tile_w": 1, "slots": 32},
     {"tile_w": 1, "slots": 64},
+    {"tile_w": 1, "slots": 128},
+    {"tile_w": 1, "slots": 256},
     {"tile_w": 4},
     {"tile_w": 8},
     {"tile_w": 16},
