@@ -285,6 +285,8 @@ def run_ours(args):
             opers.extend(res["oper"].tolist())
             launches += max(1, int(np.ceil(st["tiles"] / 4096)))
     torch.cuda.synchronize()
+    if world > 1:
+        torch.distributed.barrier()
     total_ms = float(sum(times))
     if world > 1:
         t = torch.tensor([total_ms], device=f"cuda:{local}", dtype=torch.float64)
@@ -305,7 +307,12 @@ def run_ours(args):
         e1.record(stream)
         e1.synchronize()
         e2e_ms.append(e0.elapsed_time(e1))
-    e2e_value = Q * max(1, args.e2e_steps) * world / (sum(e2e_ms) / 1e3) if e2e_ms else None
+    e2e_total = float(sum(e2e_ms))
+    if world > 1 and e2e_ms:
+        t = torch.tensor([e2e_total], device=f"cuda:{local}", dtype=torch.float64)
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)  # the slowest replica
+        e2e_total = float(t.item())
+    e2e_value = Q * max(1, args.e2e_steps) * world / (e2e_total / 1e3) if e2e_ms else None
 
     if rank != 0:
         if world > 1:
