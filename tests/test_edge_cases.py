@@ -187,3 +187,27 @@ def test_tables_follow_edits_of_another_kind():
         out.append((res["oper"], P2.cpu().numpy()))
     np.testing.assert_array_equal(out[0][0], out[1][0])
     np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-12, atol=1e-15)
+
+
+@pytest.mark.parametrize("kind", [L.IGN, L.UPPR])
+def test_feature_push_one_column_tiles_match_wide_tiles(kind):
+    """One-column tiles (flattened short-row scatter, target scaling per edge) give the
+    same FP64 result as 8-column tiles."""
+    import torch
+    import golden_cases as GC
+    dy = GC.dyn()
+    ip = dy["indptr"].copy()
+    ix = dy["indices"].astype(np.int32).copy()
+    dg = dy["degree"].astype(np.int64).copy()
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    X = np.concatenate([dy["X"], dy["X"][:, :2] * 0.5], axis=1)  # 8 columns
+    out = []
+    for W in (1, 8):
+        P = torch.zeros(X.shape, dtype=torch.float64, device="cuda")
+        R = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+        res = api.feature_push(Gd, kind, P, R, 1e-5, alpha=0.1, beta=0.5 if kind == L.IGN else 0.0,
+                               prec="fp64", tile_w=W)
+        out.append((res["oper"], P.cpu().numpy(), R.cpu().numpy()))
+    np.testing.assert_allclose(out[0][0], out[1][0], rtol=1e-12)
+    np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-10, atol=1e-14)
+    np.testing.assert_allclose(out[0][2], out[1][2], rtol=1e-10, atol=1e-14)
