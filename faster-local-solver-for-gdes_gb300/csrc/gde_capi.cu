@@ -1274,7 +1274,7 @@ static int feature_push_impl(gde_ctx* ctx, gde_graph* G, const gde_params* p, in
         return gde_internal_sor_feature_push(ctx, G, p, F, Pm, Rm, ld, eps, dc, ncand, oper_out, stats);
     }
     int W = p->tile_w;
-    if (W <= 0) W = prec64 ? 8 : 16;
+    if (W <= 0) W = 8;  // 8 columns per tile (FP32: four blocks per SM); narrower and wider measured slower
     while (W > 1 && (F % W != 0 || ld % W != 0)) W >>= 1;
     if (!valid_w(W)) return fail(ctx, GDE_EINVAL, "tile_w must be 1, 2, 4, 8, 16 or 32");
     const int nt_total = (int)(F / W);

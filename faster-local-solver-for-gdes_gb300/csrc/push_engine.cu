@@ -31,16 +31,16 @@ namespace {
 
 // Resident blocks per SM requested from the compiler (bounds registers) and
 // independent edges in flight per lane in the W = 1 scatter; both can be
-// overridden at build time for tuning.  The one-column FP32 kernel (served
-// and batched queries) trades a few spilled bytes for a fourth block per SM:
-// its memory-latency-bound phases gain more from the extra warps (+3 to +7%
-// queries/s) than the spills cost; the wider and FP64 kernels spill more and
-// keep three.
+// overridden at build time for tuning.  FP32 kernels of up to 8 columns
+// trade a few spilled bytes for a fourth block per SM: their memory-latency-
+// bound phases gain more from the extra warps (served PPR +3 to +7%, the
+// 8-column InstantGNN push +4%) than the spills cost; 16- and 32-column and
+// FP64 kernels spill more and keep three.
 #ifndef GDE_MIN_BLOCKS
 #define GDE_MIN_BLOCKS 3
 #endif
-#ifndef GDE_MIN_BLOCKS_W1F
-#define GDE_MIN_BLOCKS_W1F 4
+#ifndef GDE_MIN_BLOCKS_F32
+#define GDE_MIN_BLOCKS_F32 4
 #endif
 #ifndef GDE_EDGE_ILP
 #define GDE_EDGE_ILP 4
@@ -1498,7 +1498,7 @@ __device__ __forceinline__ void trace_point(const PushArgs& a, int it, int k) {
 }
 
 template <typename T, int W>
-__global__ void __launch_bounds__(kThreads, (W == 1 && sizeof(T) == 4) ? GDE_MIN_BLOCKS_W1F : GDE_MIN_BLOCKS)
+__global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN_BLOCKS_F32 : GDE_MIN_BLOCKS)
     push_kernel(PushArgs a) {
     __shared__ TileSh sh;
     __shared__ PrepSh ps;
