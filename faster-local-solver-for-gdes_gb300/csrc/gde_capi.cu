@@ -110,6 +110,31 @@ void fill_tuning(const gde_params* p, PushArgs& a) {
     a.allow_dense = 1;
 }
 
+// Katz near its convergence radius (alpha * lambda_max close to 1) computes
+// in FP64 whatever precision was asked: its series then converges slowly
+// and FP32 residuals lose the stopping rule's accuracy.  The largest degree
+// bounds lambda_max from above and settles most calls; when it cannot, the
+// graph's Lanczos estimate (gde_katz_spectral_bounds, run once and cached
+// until the graph is edited) decides.
+constexpr double kKatzFp64Ratio = 0.9;
+int katz_compute_prec(gde_ctx* ctx, gde_graph* G, const gde_params* p) {
+    if (p->kind != KIND_KATZ || p->prec == GDE_FP64) return p->prec;
+    if (G->dmax < 0.0) {
+        double m = 0.0;
+        for (double d : G->h_deg) m = std::max(m, d);
+        G->dmax = m;
+    }
+    if (p->alpha * G->dmax < kKatzFp64Ratio) return p->prec;
+    if (std::isnan(G->lam_max_est)) {
+        double lmax = 0.0, lmin = 0.0;
+        if (gde_katz_spectral_bounds(ctx, G, p->alpha, 300, 1e-8, &lmax, &lmin, nullptr, nullptr) != GDE_OK) {
+            G->lam_max_est = G->dmax;  // no estimate: keep the bound
+            ctx->err.clear();
+        }
+    }
+    return (p->alpha * G->lam_max_est >= kKatzFp64Ratio) ? GDE_FP64 : p->prec;
+}
+
 bool valid_w(int W) { return W == 1 || W == 2 || W == 4 || W == 8 || W == 16 || W == 32; }
 
 // Workspace for `ntiles` tiles of width W over n nodes.
@@ -797,6 +822,9 @@ int gde_serve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
     }
     if (stats) memset(stats, 0, sizeof(*stats));
     if (nq == 0) return GDE_OK;
+    gde_params pp = *p;
+    pp.prec = katz_compute_prec(ctx, G, p);
+    p = &pp;
     return solve_served(ctx, G, p, nq, seeds, eps, arrival_ms, x_out, r_out, out64, out_mem, ld_out, oper_out,
                         rounds_out, lat_ms_out, stats);
 }
@@ -981,7 +1009,6 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
     CK(cudaSetDevice(ctx->device));
     const int64_t n = G->g.n;
     const int kind = p->kind, method = p->method;
-    const int prec64 = (p->prec == GDE_FP64);
     if (kind != KIND_PPR && kind != KIND_KATZ && kind != KIND_HK) return fail(ctx, GDE_EINVAL, "kind must be PPR, KATZ or HK");
     const bool hk = method_is_hk(method);
     if (hk != (kind == KIND_HK)) return fail(ctx, GDE_EINVAL, "heat-kernel methods go with GDE_HK only");
@@ -996,6 +1023,10 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
     if (hk && !(p->tau >= 1.0)) return fail(ctx, GDE_EINVAL, "tau must be >= 1 (hk_solver.py:35)");
     if (stats) memset(stats, 0, sizeof(*stats));
     if (nq == 0) return GDE_OK;
+    gde_params pp = *p;
+    pp.prec = katz_compute_prec(ctx, G, p);
+    p = &pp;
+    const int prec64 = (p->prec == GDE_FP64);
 
     // PPR / Katz local GD with one column per tile runs as a served queue:
     // slots cycle through the queries inside one persistent launch.
@@ -1536,6 +1567,7 @@ int gde_internal_graph_host(gde_graph* G, const int64_t** indptr, const int64_t*
 }
 
 void* gde_internal_wsget(gde_ctx* ctx, const char* name, size_t bytes) { return wsget(ctx, name, bytes); }
+void gde_internal_set_lam_max(gde_graph* G, double lam) { G->lam_max_est = lam; }
 int gde_internal_fail(gde_ctx* ctx, int code, const char* msg) { return fail(ctx, code, msg); }
 cudaStream_t gde_internal_stream(gde_ctx* ctx) { return ctx->stream; }
 const double* gde_internal_npush(gde_graph* G) { return G->nfac; }

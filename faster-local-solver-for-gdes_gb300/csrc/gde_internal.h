@@ -74,6 +74,8 @@ struct gde_graph {
     std::vector<int32_t> h_perm;
     int32_t* perm_d = nullptr;
     int32_t* iperm_d = nullptr;  // internal id -> caller id (relabelled graphs)
+    double dmax = -1.0;          // largest degree (< 0: not computed since the last edit)
+    double lam_max_est = NAN;    // adjacency spectral radius from gde_katz_spectral_bounds (NaN: none)
     uint32_t* col_deg = nullptr;
     gde::NodeRec* rec = nullptr;
     int32_t node_in(int64_t u) const { return relabeled ? h_perm[u] : (int32_t)u; }

@@ -536,7 +536,11 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
     for (int64_t u = 0; u < n; u++)
         if (h_degree[u] != hlen[u])
             return gde_internal_fail(ctx, GDE_EINVAL, "host degree array differs from the resident graph");
-    if (k > 0) G->ncolors = 0;  // the edges change: the SOR colouring is rebuilt on its next use
+    if (k > 0) {
+        G->ncolors = 0;  // the edges change: the SOR colouring is rebuilt on its next use,
+        G->dmax = -1.0;  // the degree bound recomputed and the spectral estimate dropped
+        G->lam_max_est = NAN;
+    }
     // ---- insert-only batches: the edit, the repair keys and the push all on the device ----
     bool dev_ok = only_insert && k > 0 && G->deg_is_len;
     for (int64_t e = 0; dev_ok && e < k; e++)

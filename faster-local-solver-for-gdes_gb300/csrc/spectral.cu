@@ -19,6 +19,8 @@
 #include "gde_common.cuh"
 #include "gde_engine.h"
 
+void gde_internal_set_lam_max(gde_graph* G, double lam);
+
 using namespace gde;
 
 int gde_internal_fail(gde_ctx* ctx, int code, const char* msg);
@@ -202,6 +204,7 @@ extern "C" int gde_katz_spectral_bounds(gde_ctx* ctx, gde_graph* G, double alpha
     }
 #undef SP_CK
     if (!converged) tridiag_extremes(a, b, (int)a.size(), &lo, &hi);
+    if (converged) gde_internal_set_lam_max(G, hi);  // lets Katz solves judge their distance to the radius
     if (lam_max) *lam_max = hi;
     if (lam_min) *lam_min = lo;
     // eigenvalues of Q = I - alpha A lie in [1 - alpha lam_max, 1 - alpha lam_min]

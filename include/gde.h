@@ -61,7 +61,7 @@ typedef struct gde_server gde_server;
 typedef struct {
     int kind;          /* GDE_PPR / GDE_KATZ / GDE_HK */
     int method;        /* GDE_LOCAL_GD ... GDE_HK_TAYLOR */
-    int prec;          /* GDE_FP64 / GDE_FP32 */
+    int prec;          /* GDE_FP64 / GDE_FP32 (Katz with alpha * lambda_max >= 0.9 computes in FP64) */
     int tile_w;        /* columns per tile (1,2,4,8,16,32); 0 = autotuned choice */
     double alpha;      /* PPR / Katz alpha */
     double tau;        /* heat-kernel temperature */

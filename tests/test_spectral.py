@@ -53,3 +53,28 @@ def test_bounds_drive_katz_cheby():
     xo, _, _ = O.cheby(g.n, g.indptr, g.indices, g.degree.astype(np.float64), s, alpha, 1e-9, False, katz=True,
                        l_max=l_max, mu_min=mu_min, sync=True)
     assert np.abs(res["x"][0] - xo).sum() / np.abs(xo).sum() < 1e-10
+
+
+@pytest.mark.gpu
+def test_katz_near_its_radius_computes_in_fp64():
+    """An FP32 Katz request with alpha * lambda_max >= 0.9 is computed in FP64: its operation
+    counts equal the FP64 solve's exactly (FP32 residuals would flip thresholds)."""
+    from gde import _lib as L
+    from gde import api, graphs
+    g = graphs.chung_lu(3000, 2.1, 8.0, 300.0, seed=12)
+    Gd = api.Graph(g.indptr, g.indices)
+    lam = api.katz_spectral_bounds(Gd, 0.01)["lam_max"]
+    seeds = graphs.uniform_seeds(g, 6, seed=3)
+    alpha = 0.95 / lam
+    for tile_w in (1, 4):
+        r32 = api.solve(Gd, L.KATZ, L.LOCAL_GD, seeds, 1e-6, prec="fp32", alpha=alpha, tile_w=tile_w)
+        r64 = api.solve(Gd, L.KATZ, L.LOCAL_GD, seeds, 1e-6, prec="fp64", alpha=alpha, tile_w=tile_w)
+        np.testing.assert_allclose(r32["oper"], r64["oper"], rtol=1e-12)
+        assert r32["x"].dtype == np.float32  # the rows keep the requested format
+        for i in range(len(seeds)):
+            ref = r64["x"][i]
+            assert np.abs(r32["x"][i].astype(np.float64) - ref).sum() <= 1e-6 * np.abs(ref).sum()
+    # a fresh graph object (no cached estimate) decides the same way, through its own Lanczos run
+    G2 = api.Graph(g.indptr, g.indices)
+    r = api.solve(G2, L.KATZ, L.LOCAL_GD, seeds, 1e-6, prec="fp32", alpha=alpha, tile_w=1)
+    np.testing.assert_allclose(r["oper"], r64["oper"], rtol=1e-12)
