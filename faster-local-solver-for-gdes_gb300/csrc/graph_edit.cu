@@ -24,6 +24,7 @@
 #include <vector>
 
 #include "gde_common.cuh"
+#include "gde_device.cuh"
 #include "gde_engine.h"
 #include "gde_internal.h"
 
@@ -392,6 +393,190 @@ int ensure_power_tables(gde_ctx* ctx, gde_graph* G, double beta) {
     return GDE_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Batches with deletions (updetaGraph with onlyinsert = False,
+// InstantGNN.py:137-180 / ppr_solver.py:723-766) on the device.  The
+// reference edits sequentially: whether an edge is inserted or deleted, the
+// degree-1 guards and the swap-with-last moves all depend on the earlier
+// edges of the batch that share an endpoint.  Edges that share no endpoint
+// commute, so the batch runs as a dataflow: an edge executes once every
+// earlier edge on both of its endpoints has, which reproduces the
+// sequential result exactly.  Each node keeps the position of its next edge
+// (`next`); every round a warp per ready edge scans the row, edits both rows
+// and advances its endpoints; the earliest pending edge is always ready, so
+// a batch of k edges ends within k rounds.
+// ---------------------------------------------------------------------------
+struct MixOp {
+    int32_t u, v;    // endpoints (caller ids of the padded graph)
+    int32_t tu, tv;  // their touched-node indices
+    int32_t pu, pv;  // this edge's position in each endpoint's edge list
+};
+
+enum : uint8_t { MIX_NOOP = 0, MIX_INSERT = 1, MIX_DELETE = 2 };
+
+__global__ void mix_edit_kernel(const int64_t* row_ptr, int32_t* col, int32_t* row_len, const MixOp* ops, int k,
+                                int* next, uint8_t* done, uint8_t* outcome, int* ndone, GridBarrier* bar, int* err) {
+    const int lane = threadIdx.x & 31;
+    const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int nwarps = (gridDim.x * blockDim.x) >> 5;
+    for (int round = 0; round <= k; ++round) {
+        for (int e = warp; e < k; e += nwarps) {
+            const MixOp op = ops[e];
+            int ready = 0;  // decided by lane 0 for the whole warp
+            if (lane == 0)
+                ready = !*(volatile uint8_t*)&done[e] && ld_volatile_i(&next[op.tu]) == op.pu &&
+                        ld_volatile_i(&next[op.tv]) == op.pv;
+            if (!__shfl_sync(0xffffffffu, ready, 0)) continue;
+            __threadfence();  // the earlier edges' writes before this edge's reads
+            const int64_t ru = row_ptr[op.u], rv = row_ptr[op.v];
+            const int du = __ldcg(&row_len[op.u]), dv = __ldcg(&row_len[op.v]);
+            // first position of v in u's row (InstantGNN.py:153-155)
+            int found = -1;
+            for (int i0 = 0; i0 < du && found < 0; i0 += 32) {
+                const bool m = (i0 + lane < du) && __ldcg(&col[ru + i0 + lane]) == op.v;
+                const unsigned b = __ballot_sync(0xffffffffu, m);
+                if (b) found = i0 + __ffs(b) - 1;
+            }
+            uint8_t oc = MIX_NOOP;
+            if (found >= 0) {
+                if (du > 1 && dv > 1) {  // the degree-1 guard keeps the edge (:157-158)
+                    // swap-with-last in u's row; every u in v's row takes v's last entry (:159-162)
+                    const int32_t lastv = __ldcg(&col[rv + dv - 1]);
+                    if (lane == 0) col[ru + found] = __ldcg(&col[ru + du - 1]);
+                    for (int j = lane; j < dv; j += 32)
+                        if (__ldcg(&col[rv + j]) == op.u) col[rv + j] = lastv;
+                    if (lane == 0) {
+                        row_len[op.u] = du - 1;
+                        row_len[op.v] = dv - 1;
+                    }
+                    oc = MIX_DELETE;
+                }
+            } else {
+                // append to both rows (:171-174); slack was checked on the host
+                if (lane == 0) {
+                    col[ru + du] = op.v;
+                    col[rv + dv] = op.u;
+                    row_len[op.u] = du + 1;
+                    row_len[op.v] = dv + 1;
+                }
+                oc = MIX_INSERT;
+            }
+            __threadfence();  // every lane's edit visible before the endpoints move on
+            __syncwarp();
+            if (lane == 0) {
+                outcome[e] = oc;
+                __threadfence();
+                next[op.tu] = op.pu + 1;
+                next[op.tv] = op.pv + 1;
+                done[e] = 1;
+                atomicAdd(ndone, 1);
+            }
+            __syncwarp();
+        }
+        // every block reads the count between two barriers, before any edge of
+        // the next round runs, so all of them leave in the same round
+        if (!grid_barrier(bar, err)) return;
+        const bool fin = ld_volatile_i(ndone) >= k;
+        if (!grid_barrier(bar, err)) return;
+        if (fin) return;
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(err, 0, GDE_EHANG);
+}
+
+struct MixResult {
+    int status = GDE_OK;
+    bool fallback = false;         // not eligible (self-loop, no slack): the host pass runs instead
+    std::vector<uint8_t> outcome;  // per edge: MIX_NOOP / MIX_INSERT / MIX_DELETE
+};
+
+MixResult device_mixed_edit(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree, const int32_t* us,
+                            const int32_t* vs, int64_t k) {
+    MixResult M;
+    const int64_t n = G->g.n;
+    const int64_t* indptr;
+    const int64_t* hlen;
+    int64_t nn;
+    gde_internal_graph_host(G, &indptr, &hlen, &nn);
+    if (k >= ((int64_t)1 << 30)) { M.fallback = true; return M; }
+    // touched nodes, and each edge's position in its endpoints' edge lists
+    std::unordered_map<int32_t, int32_t> tix;
+    tix.reserve((size_t)(2 * k));
+    std::vector<int32_t> cnt;
+    std::vector<MixOp> ops((size_t)k);
+    for (int64_t e = 0; e < k; e++) {
+        const int32_t u = us[e], v = vs[e];
+        if (u == v) { M.fallback = true; return M; }  // self-loops keep the host pass
+        auto a = tix.emplace(u, (int32_t)cnt.size());
+        if (a.second) cnt.push_back(0);
+        auto b = tix.emplace(v, (int32_t)cnt.size());
+        if (b.second) cnt.push_back(0);
+        MixOp& op = ops[(size_t)e];
+        op.u = u; op.v = v;
+        op.tu = a.first->second; op.tv = b.first->second;
+        op.pu = cnt[op.tu]++;
+        op.pv = cnt[op.tv]++;
+    }
+    // slack: a node gains at most one entry per edge touching it
+    for (const auto& kv : tix)
+        if (h_degree[kv.first] + cnt[kv.second] > indptr[kv.first + 1] - indptr[kv.first]) {
+            M.fallback = true;
+            return M;
+        }
+    const int64_t T = (int64_t)cnt.size();
+    cudaStream_t st = ctx->stream;
+    auto ws = [&](const char* name, size_t bytes) { return gde_internal_wsget(ctx, name, std::max<size_t>(bytes, 8)); };
+    MixOp* d_ops = (MixOp*)ws("mix_ops", (size_t)k * sizeof(MixOp));
+    int* d_next = (int*)ws("mix_next", (size_t)T * 4);
+    uint8_t* d_done = (uint8_t*)ws("mix_done", (size_t)k);
+    uint8_t* d_out = (uint8_t*)ws("mix_out", (size_t)k);
+    int* d_ndone = (int*)ws("mix_ndone", 4);
+    if (!d_ops || !d_next || !d_done || !d_out || !d_ndone) {
+        M.status = gde_internal_fail(ctx, GDE_ENOMEM, "edit batch buffers");
+        return M;
+    }
+    auto ck = [&](cudaError_t e2, const char* what) {
+        if (e2 != cudaSuccess && M.status == GDE_OK) M.status = gde_internal_fail(ctx, GDE_ECUDA, what);
+    };
+    ck(cudaMemcpyAsync(d_ops, ops.data(), (size_t)k * sizeof(MixOp), cudaMemcpyHostToDevice, st), "edit upload");
+    ck(cudaMemsetAsync(d_next, 0, (size_t)T * 4, st), "edit init");
+    ck(cudaMemsetAsync(d_done, 0, (size_t)k, st), "edit init");
+    ck(cudaMemsetAsync(d_ndone, 0, 4, st), "edit init");
+    ck(cudaMemsetAsync(ctx->bar, 0, sizeof(GridBarrier), st), "edit init");
+    ck(cudaMemsetAsync(ctx->derr, 0, sizeof(int), st), "edit init");
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mix_edit_kernel, kEdT, 0);
+    const int64_t want = (k * 32 + kEdT - 1) / kEdT;  // a warp per edge at most
+    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(per_sm, 1) * ctx->sms, want));
+    const int64_t* row_ptr = G->g.row_ptr;
+    int32_t* col = G->col;
+    int32_t* rl = G->row_len;
+    int ki = (int)k;
+    GridBarrier* bar = ctx->bar;
+    int* err = ctx->derr;
+    void* args[] = {(void*)&row_ptr, (void*)&col, (void*)&rl, (void*)&d_ops, (void*)&ki, (void*)&d_next,
+                    (void*)&d_done, (void*)&d_out, (void*)&d_ndone, (void*)&bar, (void*)&err};
+    if (M.status == GDE_OK)
+        ck(cudaLaunchCooperativeKernel((void*)mix_edit_kernel, dim3(grid), dim3(kEdT), args, 0, st), "edit launch");
+    int herr = 0;
+    ck(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st), "edit status");
+    ck(cudaStreamSynchronize(st), "edit kernel");
+    if (M.status != GDE_OK) return M;
+    if (herr != 0) {
+        M.status = gde_internal_fail(ctx, GDE_EHANG, "edit batch: a device-side wait ran out");
+        return M;
+    }
+    // the edited rows and degrees back into the caller's host arrays
+    M.outcome.resize((size_t)k);
+    std::vector<int32_t> len32((size_t)n);
+    ck(cudaMemcpyAsync(M.outcome.data(), d_out, (size_t)k, cudaMemcpyDeviceToHost, st), "edit readback");
+    ck(cudaMemcpyAsync(h_indices, col, (size_t)G->g.cap * 4, cudaMemcpyDeviceToHost, st), "edit readback");
+    ck(cudaMemcpyAsync(len32.data(), rl, (size_t)n * 4, cudaMemcpyDeviceToHost, st), "edit readback");
+    ck(cudaStreamSynchronize(st), "edit readback");
+    if (M.status != GDE_OK) return M;
+    for (const auto& kv : tix) h_degree[kv.first] = len32[(size_t)kv.first];
+    return M;
+}
+
 struct DeviceInsert {
     int status = GDE_OK;
     bool fallback = false;       // capacity exceeded: the host pass reproduces the partial edit
@@ -591,6 +776,7 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
             const double oper_repair = 2.0 * (double)D.nkeys + 2.0 * (double)D.inserted;
             if (oper_out)
                 for (int64_t c = 0; c < F; c++) oper_out[c] = opers[c] + (kind == KIND_UPPR ? oper_repair : 0.0);
+            if (stats) stats->edit_path = GDE_EDIT_DEVICE_INSERT;
             return GDE_OK;
         }
     }
@@ -600,7 +786,30 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
     std::vector<int64_t> pos;
     std::vector<int32_t> val;
     int status = GDE_OK;
-    for (int64_t e = 0; e < k; e++) {
+    // batches with deletions run as a dataflow on the device (device_mixed_edit);
+    // each edge's outcome there rebuilds the reference's insert / delete maps
+    bool on_device = false;
+    if (!only_insert && k > 0 && G->deg_is_len) {
+        bool ok = true;
+        for (int64_t e = 0; ok && e < k; e++) ok = us[e] >= 0 && us[e] < n && vs[e] >= 0 && vs[e] < n;
+        if (ok) {
+            MixResult M = device_mixed_edit(ctx, G, h_indices, h_degree, us, vs, k);
+            if (M.status != GDE_OK) return M.status;
+            if (!M.fallback) {
+                on_device = true;
+                for (int64_t e = 0; e < k; e++) {
+                    if (M.outcome[(size_t)e] == MIX_INSERT) {
+                        ins.add(us[e], vs[e]);
+                        ins.add(vs[e], us[e]);
+                    } else if (M.outcome[(size_t)e] == MIX_DELETE) {
+                        del.add(us[e], vs[e]);
+                        del.add(vs[e], us[e]);
+                    }
+                }
+            }
+        }
+    }
+    for (int64_t e = 0; e < k && !on_device; e++) {
         int64_t u = us[e], v = vs[e];
         if (u < 0 || u >= n || v < 0 || v >= n) { status = GDE_EINVAL; break; }
         bool insertion = true;
@@ -735,5 +944,6 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
     }
     if (oper_out)
         for (int64_t c = 0; c < F; c++) oper_out[c] = opers[c] + (kind == KIND_UPPR ? oper_repair : 0.0);
+    if (stats) stats->edit_path = on_device ? GDE_EDIT_DEVICE_DATAFLOW : GDE_EDIT_HOST;
     return GDE_OK;
 }

@@ -91,7 +91,13 @@ typedef struct {
     double check_ms;            /* push-kernel time split by phase (global-check / prep / scatter), */
     double prep_ms;             /* each including the wait at the phase's closing grid barrier */
     double scatter_ms;
+    int edit_path;              /* gde_feature_update: how the edge batch was applied (GDE_EDIT_*) */
 } gde_stats;
+
+/* gde_stats.edit_path */
+#define GDE_EDIT_HOST 0             /* sequential host pass (self-loops, no slack to spare, relabelled) */
+#define GDE_EDIT_DEVICE_INSERT 1    /* insert-only batch on the device */
+#define GDE_EDIT_DEVICE_DATAFLOW 2  /* batch with deletions on the device, as a dataflow over the edges */
 
 /* ---- context / errors ---- */
 const char *gde_status_str(int status);

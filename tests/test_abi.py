@@ -58,3 +58,27 @@ def test_null_arguments_are_rejected_without_a_gpu(lib):
     assert lib.gde_graph_upload(None, 10, 0, None, None, None, None, ctypes.byref(out)) == L.GDE_EINVAL
     assert lib.gde_ctx_destroy(None) == L.GDE_EINVAL
     assert lib.gde_graph_free(None) == L.GDE_EINVAL
+
+
+def _struct_fields(name):
+    src = re.sub(r"/\*.*?\*/", "", open(HEADER).read(), flags=re.S)
+    body = re.search(r"typedef struct \{([^{}]*)\}\s*" + name + r";", src).group(1)
+    return re.findall(r"([a-z_0-9]+)\s*;", body)
+
+
+@pytest.mark.parametrize("cname,py", [("gde_params", L.Params), ("gde_stats", L.Stats)])
+def test_ctypes_structs_mirror_the_header(cname, py, tmp_path):
+    """Field names, order, offsets and size of the ctypes mirrors equal the C layout (gcc)."""
+    names = _struct_fields(cname)
+    assert names == [f for f, _ in py._fields_]
+    prog = tmp_path / "layout.c"
+    lines = ['#include <stddef.h>', '#include <stdio.h>', '#include "gde.h"', "int main(void) {",
+             f'  printf("%zu\\n", sizeof({cname}));']
+    lines += [f'  printf("%zu\\n", offsetof({cname}, {f}));' for f in names]
+    prog.write_text("\n".join(lines + ["  return 0;", "}"]) + "\n")
+    exe = tmp_path / "layout"
+    import subprocess
+    subprocess.run(["gcc", "-I", os.path.dirname(HEADER), str(prog), "-o", str(exe)], check=True)
+    got = [int(v) for v in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert got[0] == ctypes.sizeof(py)
+    assert got[1:] == [getattr(py, f).offset for f in names]

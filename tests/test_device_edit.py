@@ -1,0 +1,149 @@
+"""Edge batches with deletions applied on the device (dataflow over the batch).
+
+``updetaGraph`` (InstantGNN.py:137-180) walks the batch in order: an edge
+whose endpoint is already in the row is deleted (swap with the row's last
+entry) when both endpoints keep a neighbour, otherwise it is appended to both
+rows.  The device pass keeps that sequential meaning exactly: each edge waits
+until every earlier edge that shares an endpoint has been applied.  These
+tests check, on padded graphs with slack, that the device pass ran
+(``gde_stats.edit_path``) and that the edited arrays, the repaired residuals
+and the push are the same as the oracle's sequential pass.  A batch that
+overflows a row's slack falls back to the host pass and must give the same
+result.
+"""
+import numpy as np
+import pytest
+
+from gde import _lib as L
+from gde import api, graphs
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+EDIT_HOST, EDIT_DEVICE_DATAFLOW = 0, 2
+
+
+def _padded(g, slack):
+    n = g.n
+    deg = np.diff(g.indptr).astype(np.int64)
+    ip = np.zeros(n + 1, np.int64)
+    np.cumsum(deg + slack, out=ip[1:])
+    ix = np.full(ip[-1], n, np.int32)
+    for u in range(n):
+        ix[ip[u]:ip[u] + deg[u]] = g.indices[g.indptr[u]:g.indptr[u + 1]]
+    return ip, ix, deg
+
+
+def _mixed_batch(g, k_del, k_ins, k_rep, seed, hub=None, hub_times=0):
+    """Deletions of present edges, insertions of new pairs, some pairs twice (toggles), shuffled."""
+    rng = np.random.default_rng(seed)
+    n = g.n
+    src = np.repeat(np.arange(n), np.diff(g.indptr))
+    pick = rng.choice(len(src), size=k_del, replace=False)
+    dels = np.stack([src[pick], g.indices[pick]], 1)
+    ins = rng.integers(0, n, size=(k_ins, 2))
+    ins = ins[ins[:, 0] != ins[:, 1]]
+    rep = np.concatenate([dels, ins])[rng.choice(len(dels) + len(ins), size=k_rep)]
+    e = np.concatenate([dels, ins, rep])
+    e = e[rng.permutation(len(e))]
+    if hub is not None:
+        # the hub's edges come last, each pair twice in a row (insert, then delete again): the
+        # row never grows by more than one entry, but the batch touches it hub_times times
+        others = rng.choice(np.setdiff1d(np.arange(n), [hub]), size=hub_times // 2, replace=False)
+        pairs = np.repeat(np.stack([np.full(len(others), hub), others], 1), 2, axis=0)
+        e = np.concatenate([e, pairs])
+    return e[:, 0].astype(np.int32), e[:, 1].astype(np.int32)
+
+
+def _run_uppr(g, slack, us, vs, seeds, alpha=0.1, eps=1e-5):
+    import torch
+    n = g.n
+    ip, ix, dg = _padded(g, slack)
+    ix_o, dg_o = ix.copy(), dg.copy()
+    F = len(seeds)
+    Po = np.zeros((F, n))
+    Ro = np.zeros((F, n))
+    for f, s in enumerate(seeds):
+        Ro[f, s] = alpha
+    O.update_ppr(n, ip, ix_o, dg_o, alpha, eps, 1.0, Po, Ro, np.zeros(0, np.int32), np.zeros(0, np.int32), sync=True)
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    P = torch.from_numpy(np.ascontiguousarray(Po.T)).cuda()
+    R = torch.from_numpy(np.ascontiguousarray(Ro.T)).cuda()
+    oo = O.update_ppr(n, ip, ix_o, dg_o, alpha, eps, 1.0, Po, Ro, us, vs, sync=True)
+    res = api.feature_update(Gd, L.UPPR, ix, dg, us, vs, False, P, R, None, eps, alpha=alpha, prec="fp64",
+                             tile_w=1)
+    np.testing.assert_array_equal(ix, ix_o)
+    np.testing.assert_array_equal(dg, dg_o)
+    np.testing.assert_allclose(res["oper"], oo, rtol=1e-12)
+    np.testing.assert_allclose(P.cpu().numpy().T, Po, rtol=1e-9, atol=1e-13)
+    np.testing.assert_allclose(R.cpu().numpy().T, Ro, rtol=1e-9, atol=1e-13)
+    return res, Gd, ix, dg
+
+
+def test_mixed_batch_runs_on_device_and_matches_sequential_pass():
+    g = graphs.chung_lu(3000, 2.2, 6.0, 120.0, seed=21)
+    us, vs = _mixed_batch(g, 400, 400, 120, seed=5)
+    deg0 = np.diff(g.indptr)
+    res, Gd, ix, dg = _run_uppr(g, 64, us, vs, graphs.uniform_seeds(g, 2, seed=3))
+    assert res["stats"]["edit_path"] == EDIT_DEVICE_DATAFLOW
+    assert (dg < deg0).any() and (dg > deg0).any()  # the batch both deleted and inserted
+
+
+def test_mixed_batch_then_push_on_the_edited_graph_matches_a_fresh_upload():
+    """After the device edit, the device copy of the graph (rows, degrees, tables) is the edited one."""
+    import torch
+    g = graphs.chung_lu(3000, 2.2, 6.0, 120.0, seed=23)
+    us, vs = _mixed_batch(g, 300, 300, 60, seed=8)
+    res, Gd, ix, dg = _run_uppr(g, 48, us, vs, graphs.uniform_seeds(g, 1, seed=4))
+    assert res["stats"]["edit_path"] == EDIT_DEVICE_DATAFLOW
+    ip, _, _ = _padded(g, 48)
+    fresh = api.Graph(ip, ix.copy(), row_len=dg.copy(), degree=dg.astype(np.float64))
+    seeds = graphs.uniform_seeds(g, 4, seed=9)
+    a = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, 1e-7, prec="fp64", alpha=0.15, tile_w=1)
+    b = api.solve(fresh, L.PPR, L.LOCAL_GD, seeds, 1e-7, prec="fp64", alpha=0.15, tile_w=1)
+    np.testing.assert_allclose(a["x"], b["x"], rtol=1e-12, atol=1e-16)
+    X = np.random.default_rng(2).standard_normal((g.n, 3))
+    out = []
+    for G in (Gd, fresh):
+        P = torch.zeros(X.shape, dtype=torch.float64, device="cuda")
+        R = torch.from_numpy(X.copy()).cuda()
+        r = api.feature_push(G, L.IGN, P, R, 1e-4, alpha=0.1, beta=0.5, prec="fp64")
+        out.append((r["oper"], P.cpu().numpy()))
+    np.testing.assert_array_equal(out[0][0], out[1][0])
+    np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-12, atol=1e-15)
+
+
+def test_row_without_slack_falls_back_to_the_host_pass():
+    g = graphs.chung_lu(3000, 2.2, 6.0, 120.0, seed=22)
+    hub = int(np.argmax(np.diff(g.indptr)))
+    us, vs = _mixed_batch(g, 100, 100, 20, seed=6, hub=hub, hub_times=12)
+    res, _, _, _ = _run_uppr(g, 4, us, vs, graphs.uniform_seeds(g, 2, seed=3))
+    assert res["stats"]["edit_path"] == EDIT_HOST
+
+
+@pytest.mark.parametrize("algo", ["fwdbatch"])
+def test_instantgnn_mixed_batch_on_device(algo):
+    import torch
+    g = graphs.chung_lu(2500, 2.2, 6.0, 100.0, seed=31)
+    n = g.n
+    us, vs = _mixed_batch(g, 250, 250, 50, seed=12)
+    ip, ix, dg = _padded(g, 64)
+    ix_o, dg_o = ix.copy(), dg.copy()
+    X = np.random.default_rng(7).standard_normal((n, 2))
+    alpha, eps, beta = 0.1, 1e-4, 0.5
+    Po = np.zeros_like(X)
+    Ro = X.copy()
+    O.ign_sync(n, ip, ix_o, dg_o, alpha, eps, beta, Po, Ro)
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    P = torch.zeros(X.shape, dtype=torch.float64, device="cuda")
+    R = torch.from_numpy(X.copy()).cuda()
+    Xd = torch.from_numpy(X.copy()).cuda()
+    api.feature_push(Gd, L.IGN, P, R, eps, alpha=alpha, beta=beta, prec="fp64")
+    _, oo = O.ign_update(n, ip, ix_o, dg_o, alpha, eps, 1.0, Po, Ro, X, us, vs, beta, algo, sync=True)
+    res = api.feature_update(Gd, L.IGN, ix, dg, us, vs, False, P, R, Xd, eps, alpha=alpha, beta=beta, prec="fp64")
+    assert res["stats"]["edit_path"] == EDIT_DEVICE_DATAFLOW
+    np.testing.assert_array_equal(ix, ix_o)
+    np.testing.assert_array_equal(dg, dg_o)
+    np.testing.assert_allclose(res["oper"], oo, rtol=1e-12)
+    np.testing.assert_allclose(P.cpu().numpy(), Po, rtol=1e-9, atol=1e-13)
+    np.testing.assert_allclose(R.cpu().numpy(), Ro, rtol=1e-9, atol=1e-13)
