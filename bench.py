@@ -62,6 +62,9 @@ def parse():
                     help="c2: served PPR on the 2.36M graph (the headline); c3: 1,024 seeds per launch with "
                          "per-seed eps on the 100k graph; c4: served PPR/Katz/heat-kernel mix with Poisson "
                          "arrivals on R-MAT scale 22; c5: InstantGNN 128-column snapshot updates")
+    ap.add_argument("--edit", default="insert", choices=["insert", "mixed"],
+                    help="c5: insert-only snapshots, or a sliding window that also deletes the previous snapshot's "
+                         "edges (updetaGraph with onlyinsert = False)")
     ap.add_argument("--mlp", action="store_true",
                     help="c5: train the MLP classifier on the device-resident features after the initial push and "
                          "after the last snapshot (outside the timed region)")
@@ -606,6 +609,16 @@ def run_c5(args):
         labels = torch.from_numpy((X @ rng.standard_normal((F, 40))).argmax(1)).to(dev)
         split = consumer.random_split(n, dev, seed=4)
         mlp["initial"] = consumer.train_eval(Pd, labels, split)
+    mixed = args.edit == "mixed"
+    batches = []
+    for s in range(snaps):
+        us, vs = dyn.Us[s], dyn.Vs[s]
+        if mixed and s > 0:
+            # the previous snapshot's edges leave while this one's arrive, shuffled together
+            perm = np.random.default_rng(100 + s).permutation(2 * us.shape[0])
+            us = np.concatenate([dyn.Us[s - 1], us])[perm]
+            vs = np.concatenate([dyn.Vs[s - 1], vs])[perm]
+        batches.append((np.ascontiguousarray(us, dtype=np.int32), np.ascontiguousarray(vs, dtype=np.int32)))
     times, outs = [], []
     with ClockSampler(local) as clk:
         for s in range(snaps):
@@ -613,8 +626,8 @@ def run_c5(args):
             e0 = torch.cuda.Event(enable_timing=True)
             e1 = torch.cuda.Event(enable_timing=True)
             e0.record(stream)
-            outs.append(api.feature_update(G, L.IGN, indices, degree, dyn.Us[s], dyn.Vs[s], True, Pd, Rd, Xd, eps,
-                                           alpha=ALPHA, beta=beta, prec="fp32", tile_w=tw))
+            outs.append(api.feature_update(G, L.IGN, indices, degree, batches[s][0], batches[s][1], not mixed, Pd,
+                                           Rd, Xd, eps, alpha=ALPHA, beta=beta, prec="fp32", tile_w=tw))
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
@@ -622,16 +635,21 @@ def run_c5(args):
     agg = {k: sum(o["stats"][k] for o in outs) for k in ("union_vol", "col_vol", "col_nodes", "kernel_ms")}
     achieved = algorithmic_bytes(agg) / (max(agg["kernel_ms"], 1e-9) / 1e3) / 1e9
     peak, peak_kind = measured_peak()
+    edits = f"{int(dyn.Us.shape[1]):,} inserted" + (" and as many deleted" if mixed else "")
     out = {
-        "metric": "InstantGNN snapshot updates/s (128 FP32 columns, 59,375 inserted edges per snapshot)",
+        "metric": f"InstantGNN snapshot updates/s (128 FP32 columns, {edits} edges per snapshot)",
         "value": snaps / (total_ms / 1e3), "unit": "snapshots/s", "n_gpus": 1, "steps": snaps, "warmup": 0,
         "ms_per_step": total_ms / snaps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
         "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "instantgnn_update_fp32_128col_chung_lu_169k", "n": n, "features": F,
+        "config": {"workload": "instantgnn_update_" + ("mixed_" if mixed else "") + "fp32_128col_chung_lu_169k",
+                   "n": n, "features": F,
                    "snapshots": snaps, "edges_per_snapshot": int(dyn.Us.shape[1]), "alpha": ALPHA, "beta": beta,
                    "eps": eps, "initial_push_s": init_s, "tile_w": tw or "default"},
         "column_updates_per_s": snaps * F / (total_ms / 1e3),
         "push_kernel_ms_per_step": agg["kernel_ms"] / snaps,
+        "edit_ms_per_step": sum(o["stats"]["edit_ms"] for o in outs) / snaps,
+        "edit_paths": {p: sum(1 for o in outs if o["stats"]["edit_path"] == i)
+                       for i, p in enumerate(("host", "device_insert", "device_dataflow"))},
         "mean_oper_per_column": float(np.mean([o["oper"].mean() for o in outs])),
         "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                      "peak_kind": peak_kind, "traffic": None},

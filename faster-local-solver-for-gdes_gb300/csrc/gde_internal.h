@@ -64,6 +64,7 @@ struct gde_graph {
     int ncolors = 0;
     std::vector<int64_t> h_indptr;
     std::vector<int64_t> h_len;
+    std::vector<int32_t> edit_last;  // per node, -1 between edge batches (scratch of the device edit)
     std::vector<double> h_deg;
     bool deg_is_len = true;
     // Static graphs are stored relabelled by descending degree: push targets

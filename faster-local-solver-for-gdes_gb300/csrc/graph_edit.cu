@@ -18,6 +18,7 @@
 
 #include <cmath>
 #include <algorithm>
+#include <chrono>
 #include <cstring>
 #include <string>
 #include <unordered_map>
@@ -327,18 +328,21 @@ __global__ void ins_keys_kernel(const int* cnt, const int* kidx, int64_t n, int3
 }
 
 // Repair factors of each touched node (InstantGNN.py:304-307 / ppr_solver.py:777-788).
-__global__ void ins_repair_keys_kernel(const int32_t* keys, int nkeys, const int* cnt, const int* off,
-                                       const int32_t* row_len, int kind, double beta, const double* pw1,
-                                       const double* pwb, RepairKey* out) {
+// (del_cnt null: insert-only batch, no delete lists)
+__global__ void ins_repair_keys_kernel(const int32_t* keys, int nkeys, const int* cnt, const int* del_cnt,
+                                       const int* off, const int32_t* row_len, int kind, double beta,
+                                       const double* pw1, const double* pwb, RepairKey* out) {
     for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nkeys; i += gridDim.x * blockDim.x) {
         const int u = keys[i];
         const int d = row_len[u];
-        const int od = d - cnt[u];
+        const int cd = del_cnt ? del_cnt[u] : 0;
+        const int od = d - cnt[u] + cd;
         RepairKey K;
         K.u = u;
         K.ins_beg = off[u];
         K.ins_end = off[u] + cnt[u];
-        K.del_beg = K.del_end = K.ins_end;
+        K.del_beg = K.ins_end;
+        K.del_end = K.ins_end + cd;
         if (kind == KIND_IGN) {
             K.a1 = pow((double)d / (double)od, 1.0 - beta);
             K.a2 = pw1[od];
@@ -399,138 +403,276 @@ int ensure_power_tables(gde_ctx* ctx, gde_graph* G, double beta) {
 // reference edits sequentially: whether an edge is inserted or deleted, the
 // degree-1 guards and the swap-with-last moves all depend on the earlier
 // edges of the batch that share an endpoint.  Edges that share no endpoint
-// commute, so the batch runs as a dataflow: an edge executes once every
-// earlier edge on both of its endpoints has, which reproduces the
-// sequential result exactly.  Each node keeps the position of its next edge
-// (`next`); every round a warp per ready edge scans the row, edits both rows
-// and advances its endpoints; the earliest pending edge is always ready, so
-// a batch of k edges ends within k rounds.
+// commute, so the batch runs as a dataflow: an edge executes once the
+// previous edge on each of its endpoints (`pu`, `pv`, found on the host) has,
+// which reproduces the sequential result exactly.  A warp takes the edges
+// e = w, w + W, ... in batch order and waits on their predecessors' done
+// flags.  The lowest pending edge of the whole batch has all its
+// predecessors done, and every block is resident (cooperative launch), so
+// the batch always progresses; each flag has at most two waiters.
 // ---------------------------------------------------------------------------
 struct MixOp {
     int32_t u, v;    // endpoints (caller ids of the padded graph)
-    int32_t tu, tv;  // their touched-node indices
-    int32_t pu, pv;  // this edge's position in each endpoint's edge list
+    int32_t pu, pv;  // the previous edge of the batch on u / on v, or -1
 };
 
 enum : uint8_t { MIX_NOOP = 0, MIX_INSERT = 1, MIX_DELETE = 2 };
 
+constexpr int kScanVec = 8;  // 16-byte loads in flight per lane while a warp scans a row
+
+// First position of x in col[r, r + d), or -1.  The aligned middle of the row
+// is read as int4 with kScanVec loads in flight per lane (1024 entries per
+// step); the unaligned head and the tail are read entry by entry.
+__device__ __forceinline__ int warp_find_first(const int32_t* col, int64_t r, int d, int32_t x, int lane) {
+    const int head = min(d, (int)((4 - (r & 3)) & 3));
+    if (head > 0) {
+        const unsigned b = __ballot_sync(0xffffffffu, lane < head && __ldcg(&col[r + lane]) == x);
+        if (b) return __ffs(b) - 1;
+    }
+    const int4* vec = reinterpret_cast<const int4*>(col + r + head);
+    const int nv = (d - head) >> 2;
+    for (int i0 = 0; i0 < nv; i0 += 32 * kScanVec) {
+        int4 c[kScanVec];
+#pragma unroll
+        for (int j = 0; j < kScanVec; ++j) {
+            const int idx = i0 + 32 * j + lane;
+            c[j] = idx < nv ? __ldcg(&vec[idx]) : make_int4(-1, -1, -1, -1);  // ids are >= 0
+        }
+#pragma unroll
+        for (int j = 0; j < kScanVec; ++j) {
+            const int w = c[j].x == x ? 0 : c[j].y == x ? 1 : c[j].z == x ? 2 : c[j].w == x ? 3 : 4;
+            const unsigned b = __ballot_sync(0xffffffffu, w < 4);
+            if (b) {
+                const int src = __ffs(b) - 1;
+                return head + 4 * (i0 + 32 * j + src) + __shfl_sync(0xffffffffu, w, src);
+            }
+        }
+    }
+    const int t0 = head + 4 * nv;
+    if (t0 < d) {
+        const unsigned b = __ballot_sync(0xffffffffu, t0 + lane < d && __ldcg(&col[r + t0 + lane]) == x);
+        if (b) return t0 + __ffs(b) - 1;
+    }
+    return -1;
+}
+
+// Every x in col[r, r + d) becomes y (same access pattern).
+__device__ __forceinline__ void warp_replace_all(int32_t* col, int64_t r, int d, int32_t x, int32_t y, int lane) {
+    const int head = min(d, (int)((4 - (r & 3)) & 3));
+    if (lane < head && __ldcg(&col[r + lane]) == x) col[r + lane] = y;
+    const int4* vec = reinterpret_cast<const int4*>(col + r + head);
+    const int nv = (d - head) >> 2;
+    for (int i0 = 0; i0 < nv; i0 += 32 * kScanVec) {
+        int4 c[kScanVec];
+#pragma unroll
+        for (int j = 0; j < kScanVec; ++j) {
+            const int idx = i0 + 32 * j + lane;
+            c[j] = idx < nv ? __ldcg(&vec[idx]) : make_int4(-1, -1, -1, -1);
+        }
+#pragma unroll
+        for (int j = 0; j < kScanVec; ++j) {
+            int32_t* q = col + r + head + 4 * (int64_t)(i0 + 32 * j + lane);
+            if (c[j].x == x) q[0] = y;
+            if (c[j].y == x) q[1] = y;
+            if (c[j].z == x) q[2] = y;
+            if (c[j].w == x) q[3] = y;
+        }
+    }
+    const int t0 = head + 4 * nv;
+    if (t0 + lane < d && __ldcg(&col[r + t0 + lane]) == x) col[r + t0 + lane] = y;
+}
+
+// state[0]: set when an insertion found no slack in its rows (the batch is
+// then abandoned and the host pass runs it).  A wait that outlasts
+// `poll_limit` polls sets GDE_EHANG in err; either flag stops every waiter.
+// Since a node's edges run in batch order, the node's insert and delete
+// counters give each applied edge its rank among the node's insertions or
+// deletions (rank[2e], rank[2e + 1] for u, v): the repair's neighbour lists
+// come out in batch order without a sort.
 __global__ void mix_edit_kernel(const int64_t* row_ptr, int32_t* col, int32_t* row_len, const MixOp* ops, int k,
-                                int* next, uint8_t* done, uint8_t* outcome, int* ndone, GridBarrier* bar, int* err) {
+                                uint8_t* done, uint8_t* outcome, int* ins_cnt, int* del_cnt, int* rank, int* state,
+                                int64_t poll_limit, int* err) {
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
-    for (int round = 0; round <= k; ++round) {
-        for (int e = warp; e < k; e += nwarps) {
-            const MixOp op = ops[e];
-            int ready = 0;  // decided by lane 0 for the whole warp
-            if (lane == 0)
-                ready = !*(volatile uint8_t*)&done[e] && ld_volatile_i(&next[op.tu]) == op.pu &&
-                        ld_volatile_i(&next[op.tv]) == op.pv;
-            if (!__shfl_sync(0xffffffffu, ready, 0)) continue;
-            __threadfence();  // the earlier edges' writes before this edge's reads
-            const int64_t ru = row_ptr[op.u], rv = row_ptr[op.v];
-            const int du = __ldcg(&row_len[op.u]), dv = __ldcg(&row_len[op.v]);
-            // first position of v in u's row (InstantGNN.py:153-155)
-            int found = -1;
-            for (int i0 = 0; i0 < du && found < 0; i0 += 32) {
-                const bool m = (i0 + lane < du) && __ldcg(&col[ru + i0 + lane]) == op.v;
-                const unsigned b = __ballot_sync(0xffffffffu, m);
-                if (b) found = i0 + __ffs(b) - 1;
-            }
-            uint8_t oc = MIX_NOOP;
-            if (found >= 0) {
-                if (du > 1 && dv > 1) {  // the degree-1 guard keeps the edge (:157-158)
-                    // swap-with-last in u's row; every u in v's row takes v's last entry (:159-162)
-                    const int32_t lastv = __ldcg(&col[rv + dv - 1]);
-                    if (lane == 0) col[ru + found] = __ldcg(&col[ru + du - 1]);
-                    for (int j = lane; j < dv; j += 32)
-                        if (__ldcg(&col[rv + j]) == op.u) col[rv + j] = lastv;
-                    if (lane == 0) {
-                        row_len[op.u] = du - 1;
-                        row_len[op.v] = dv - 1;
-                    }
-                    oc = MIX_DELETE;
+    for (int e = warp; e < k; e += nwarps) {
+        const MixOp op = ops[e];
+        int go = 1;
+        if (lane == 0) {
+            int64_t polls = 0;
+            unsigned ns = 32;
+            while ((op.pu >= 0 && !*(volatile const uint8_t*)&done[op.pu]) ||
+                   (op.pv >= 0 && !*(volatile const uint8_t*)&done[op.pv])) {
+                if (ld_volatile_i(err) != 0 || ld_volatile_i(state) != 0) { go = 0; break; }
+                if (++polls > poll_limit) {
+                    atomicCAS(err, 0, GDE_EHANG);
+                    go = 0;
+                    break;
                 }
-            } else {
-                // append to both rows (:171-174); slack was checked on the host
-                if (lane == 0) {
-                    col[ru + du] = op.v;
-                    col[rv + dv] = op.u;
-                    row_len[op.u] = du + 1;
-                    row_len[op.v] = dv + 1;
-                }
-                oc = MIX_INSERT;
+                __nanosleep(ns);
+                ns = min(ns * 2u, 256u);
             }
-            __threadfence();  // every lane's edit visible before the endpoints move on
-            __syncwarp();
-            if (lane == 0) {
-                outcome[e] = oc;
-                __threadfence();
-                next[op.tu] = op.pu + 1;
-                next[op.tv] = op.pv + 1;
-                done[e] = 1;
-                atomicAdd(ndone, 1);
-            }
-            __syncwarp();
         }
-        // every block reads the count between two barriers, before any edge of
-        // the next round runs, so all of them leave in the same round
-        if (!grid_barrier(bar, err)) return;
-        const bool fin = ld_volatile_i(ndone) >= k;
-        if (!grid_barrier(bar, err)) return;
-        if (fin) return;
+        if (!__shfl_sync(0xffffffffu, go, 0)) return;
+        __threadfence();  // the predecessors' writes before this edge's reads
+        const int64_t ru = row_ptr[op.u], rv = row_ptr[op.v];
+        const int du = __ldcg(&row_len[op.u]), dv = __ldcg(&row_len[op.v]);
+        // first position of v in u's row (InstantGNN.py:153-155)
+        const int found = warp_find_first(col, ru, du, op.v, lane);
+        uint8_t oc = MIX_NOOP;
+        if (found >= 0) {
+            if (du > 1 && dv > 1) {  // the degree-1 guard keeps the edge (:157-158)
+                // swap-with-last in u's row; every u in v's row takes v's last entry (:159-162)
+                const int32_t lastv = __ldcg(&col[rv + dv - 1]);
+                if (lane == 0) col[ru + found] = __ldcg(&col[ru + du - 1]);
+                warp_replace_all(col, rv, dv, op.u, lastv, lane);
+                if (lane == 0) {
+                    row_len[op.u] = du - 1;
+                    row_len[op.v] = dv - 1;
+                }
+                oc = MIX_DELETE;
+            }
+        } else if (ru + du >= row_ptr[op.u + 1] || rv + dv >= row_ptr[op.v + 1]) {
+            // no slack left for the append: nothing is written, the batch stops
+            if (lane == 0) atomicExch(state, 1);
+            return;
+        } else {
+            // append to both rows (:171-174)
+            if (lane == 0) {
+                col[ru + du] = op.v;
+                col[rv + dv] = op.u;
+                row_len[op.u] = du + 1;
+                row_len[op.v] = dv + 1;
+            }
+            oc = MIX_INSERT;
+        }
+        if (lane == 0 && oc != MIX_NOOP) {
+            int* c = oc == MIX_INSERT ? ins_cnt : del_cnt;
+            const int a = __ldcg(&c[op.u]), b = __ldcg(&c[op.v]);
+            rank[2 * e] = a;
+            rank[2 * e + 1] = b;
+            c[op.u] = a + 1;
+            c[op.v] = b + 1;
+        }
+        __threadfence();  // every lane's edit visible before the successors start
+        __syncwarp();
+        if (lane == 0) {
+            outcome[e] = oc;
+            __threadfence();
+            *(volatile uint8_t*)&done[e] = 1;
+        }
+        __syncwarp();
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicCAS(err, 0, GDE_EHANG);
 }
 
-struct MixResult {
+// Repair-list section of each node with insertions: its inserted neighbours,
+// then its deleted ones (InstantGNN.py:298-314 walks a node's insert list and
+// then its delete list).
+__global__ void mix_sizes_kernel(const int* ins_cnt, const int* del_cnt, int64_t n, int* size) {
+    for (int64_t w = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; w < n; w += (int64_t)gridDim.x * blockDim.x)
+        size[w] = ins_cnt[w] > 0 ? ins_cnt[w] + del_cnt[w] : 0;
+}
+
+__global__ void mix_fill_kernel(const MixOp* ops, const uint8_t* outcome, const int* rank, int k, const int* ins_cnt,
+                                const int* off, int32_t* nbr) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < k; e += gridDim.x * blockDim.x) {
+        const uint8_t oc = outcome[e];
+        if (oc == MIX_NOOP) continue;
+        const MixOp op = ops[e];
+        const int cu = ins_cnt[op.u], cv = ins_cnt[op.v];
+        if (oc == MIX_INSERT) {
+            nbr[off[op.u] + rank[2 * e]] = op.v;
+            nbr[off[op.v] + rank[2 * e + 1]] = op.u;
+        } else {
+            if (cu > 0) nbr[off[op.u] + cu + rank[2 * e]] = op.v;
+            if (cv > 0) nbr[off[op.v] + cv + rank[2 * e + 1]] = op.u;
+        }
+    }
+}
+
+// New degree tables of the touched nodes (row_len already edited).
+__global__ void mix_tables_kernel(const int32_t* nodes, int64_t nt, const int32_t* row_len, float* degf, double* degd,
+                                  double* nfac, double* tfac, float* tfac_f, const double* pw1, const double* pwb) {
+    for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < nt; t += (int64_t)gridDim.x * blockDim.x) {
+        const int u = nodes[t];
+        const int d = row_len[u];
+        degf[u] = (float)d;
+        degd[u] = (double)d;
+        if (nfac && pw1) {
+            nfac[u] = pw1[d];
+            tfac[u] = pwb[d];
+            tfac_f[u] = (float)pwb[d];
+        }
+    }
+}
+
+// A warp per touched node: its degree, and (buf non-null) its row's whole
+// capacity packed at off[t].
+__global__ void mix_gather_kernel(const int64_t* row_ptr, const int32_t* col, const int32_t* row_len,
+                                  const int32_t* nodes, const int64_t* off, int64_t nt, int32_t* buf, int32_t* lens) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t t = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; t < nt; t += nw) {
+        const int32_t u = nodes[t];
+        if (lane == 0) lens[t] = row_len[u];
+        if (!buf) continue;
+        const int64_t r = row_ptr[u], c = row_ptr[u + 1] - r;
+        for (int64_t i = lane; i < c; i += 32) buf[off[t] + i] = col[r + i];
+    }
+}
+
+// What a device edit leaves for the repair and the push: the nodes with
+// insertions (keys), their repair factors and neighbour lists, on the device.
+struct DeviceEdit {
     int status = GDE_OK;
-    bool fallback = false;         // not eligible (self-loop, no slack): the host pass runs instead
-    std::vector<uint8_t> outcome;  // per edge: MIX_NOOP / MIX_INSERT / MIX_DELETE
+    bool fallback = false;       // the host pass runs the batch instead
+    const int32_t* keys = nullptr;
+    int nkeys = 0;
+    RepairKey* rkeys = nullptr;
+    const int32_t* nbr = nullptr;
+    int64_t repair_nbr = 0;      // entries of the keys' neighbour lists
 };
 
-MixResult device_mixed_edit(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree, const int32_t* us,
-                            const int32_t* vs, int64_t k) {
-    MixResult M;
+DeviceEdit device_mixed_edit(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree, const int32_t* us,
+                             const int32_t* vs, int64_t k, int kind, double beta) {
+    DeviceEdit M;
     const int64_t n = G->g.n;
     const int64_t* indptr;
     const int64_t* hlen;
     int64_t nn;
     gde_internal_graph_host(G, &indptr, &hlen, &nn);
     if (k >= ((int64_t)1 << 30)) { M.fallback = true; return M; }
-    // touched nodes, and each edge's position in its endpoints' edge lists
-    std::unordered_map<int32_t, int32_t> tix;
-    tix.reserve((size_t)(2 * k));
-    std::vector<int32_t> cnt;
+    for (int64_t e = 0; e < k; e++)
+        if (us[e] == vs[e]) { M.fallback = true; return M; }  // self-loops keep the host pass
+    // each edge's predecessor on either endpoint: the last earlier edge touching it
+    std::vector<int32_t>& last = G->edit_last;  // -1 outside this function
+    if ((int64_t)last.size() != n) last.assign((size_t)n, -1);
     std::vector<MixOp> ops((size_t)k);
+    std::vector<int32_t> touched;
     for (int64_t e = 0; e < k; e++) {
         const int32_t u = us[e], v = vs[e];
-        if (u == v) { M.fallback = true; return M; }  // self-loops keep the host pass
-        auto a = tix.emplace(u, (int32_t)cnt.size());
-        if (a.second) cnt.push_back(0);
-        auto b = tix.emplace(v, (int32_t)cnt.size());
-        if (b.second) cnt.push_back(0);
         MixOp& op = ops[(size_t)e];
-        op.u = u; op.v = v;
-        op.tu = a.first->second; op.tv = b.first->second;
-        op.pu = cnt[op.tu]++;
-        op.pv = cnt[op.tv]++;
+        op.u = u;
+        op.v = v;
+        op.pu = last[u];
+        op.pv = last[v];
+        if (op.pu < 0) touched.push_back(u);
+        if (op.pv < 0) touched.push_back(v);
+        last[u] = last[v] = (int32_t)e;
     }
-    // slack: a node gains at most one entry per edge touching it
-    for (const auto& kv : tix)
-        if (h_degree[kv.first] + cnt[kv.second] > indptr[kv.first + 1] - indptr[kv.first]) {
-            M.fallback = true;
-            return M;
-        }
-    const int64_t T = (int64_t)cnt.size();
+    for (const int32_t u : touched) last[u] = -1;
+    const int64_t nt = (int64_t)touched.size();
     cudaStream_t st = ctx->stream;
     auto ws = [&](const char* name, size_t bytes) { return gde_internal_wsget(ctx, name, std::max<size_t>(bytes, 8)); };
     MixOp* d_ops = (MixOp*)ws("mix_ops", (size_t)k * sizeof(MixOp));
-    int* d_next = (int*)ws("mix_next", (size_t)T * 4);
     uint8_t* d_done = (uint8_t*)ws("mix_done", (size_t)k);
     uint8_t* d_out = (uint8_t*)ws("mix_out", (size_t)k);
-    int* d_ndone = (int*)ws("mix_ndone", 4);
-    if (!d_ops || !d_next || !d_done || !d_out || !d_ndone) {
+    int* d_rank = (int*)ws("mix_rank", (size_t)k * 8);
+    int* d_icnt = (int*)ws("mix_icnt", (size_t)n * 4);
+    int* d_dcnt = (int*)ws("mix_dcnt", (size_t)n * 4);
+    int* d_state = (int*)ws("mix_state", 8);
+    int32_t* d_nodes = (int32_t*)ws("mix_nodes", (size_t)nt * 4);
+    if (!d_ops || !d_done || !d_out || !d_rank || !d_icnt || !d_dcnt || !d_state || !d_nodes) {
         M.status = gde_internal_fail(ctx, GDE_ENOMEM, "edit batch buffers");
         return M;
     }
@@ -538,10 +680,11 @@ MixResult device_mixed_edit(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int6
         if (e2 != cudaSuccess && M.status == GDE_OK) M.status = gde_internal_fail(ctx, GDE_ECUDA, what);
     };
     ck(cudaMemcpyAsync(d_ops, ops.data(), (size_t)k * sizeof(MixOp), cudaMemcpyHostToDevice, st), "edit upload");
-    ck(cudaMemsetAsync(d_next, 0, (size_t)T * 4, st), "edit init");
+    ck(cudaMemcpyAsync(d_nodes, touched.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, st), "edit upload");
     ck(cudaMemsetAsync(d_done, 0, (size_t)k, st), "edit init");
-    ck(cudaMemsetAsync(d_ndone, 0, 4, st), "edit init");
-    ck(cudaMemsetAsync(ctx->bar, 0, sizeof(GridBarrier), st), "edit init");
+    ck(cudaMemsetAsync(d_icnt, 0, (size_t)n * 4, st), "edit init");
+    ck(cudaMemsetAsync(d_dcnt, 0, (size_t)n * 4, st), "edit init");
+    ck(cudaMemsetAsync(d_state, 0, 8, st), "edit init");
     ck(cudaMemsetAsync(ctx->derr, 0, sizeof(int), st), "edit init");
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mix_edit_kernel, kEdT, 0);
@@ -551,45 +694,131 @@ MixResult device_mixed_edit(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int6
     int32_t* col = G->col;
     int32_t* rl = G->row_len;
     int ki = (int)k;
-    GridBarrier* bar = ctx->bar;
+    // a wait is bounded by the whole batch running in sequence (>= 1 us a poll)
+    int64_t poll_limit = std::max<int64_t>((int64_t)1 << 22, 64 * k);
     int* err = ctx->derr;
-    void* args[] = {(void*)&row_ptr, (void*)&col, (void*)&rl, (void*)&d_ops, (void*)&ki, (void*)&d_next,
-                    (void*)&d_done, (void*)&d_out, (void*)&d_ndone, (void*)&bar, (void*)&err};
+    void* args[] = {(void*)&row_ptr, (void*)&col,    (void*)&rl,     (void*)&d_ops,   (void*)&ki,
+                    (void*)&d_done,  (void*)&d_out,  (void*)&d_icnt, (void*)&d_dcnt,  (void*)&d_rank,
+                    (void*)&d_state, (void*)&poll_limit, (void*)&err};
     if (M.status == GDE_OK)
         ck(cudaLaunchCooperativeKernel((void*)mix_edit_kernel, dim3(grid), dim3(kEdT), args, 0, st), "edit launch");
-    int herr = 0;
+    int herr = 0, hfull = 0;
     ck(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st), "edit status");
+    ck(cudaMemcpyAsync(&hfull, d_state, 4, cudaMemcpyDeviceToHost, st), "edit status");
     ck(cudaStreamSynchronize(st), "edit kernel");
     if (M.status != GDE_OK) return M;
-    if (herr != 0) {
-        M.status = gde_internal_fail(ctx, GDE_EHANG, "edit batch: a device-side wait ran out");
+    if (herr != 0 || hfull != 0) {
+        // An insertion found a row full (or a wait ran out).  Edges after it
+        // in batch order may already be applied, so the touched rows go back
+        // to the caller's arrays (still unedited); for a full row the host
+        // pass then reproduces the reference's partial edit and its capacity
+        // error.
+        std::vector<int64_t> nodes, pos;
+        std::vector<int32_t> val;
+        nodes.reserve(touched.size());
+        for (const int32_t u : touched) {
+            nodes.push_back(u);
+            for (int64_t i = indptr[u]; i < indptr[u + 1]; i++) {
+                pos.push_back(i);
+                val.push_back(h_indices[i]);
+            }
+        }
+        M.status = gde_internal_graph_refresh_nodes(ctx, G, h_degree, nodes.data(), (int64_t)nodes.size(),
+                                                    pos.data(), val.data(), (int64_t)pos.size(), NAN, 0);
+        if (M.status == GDE_OK && herr != 0)
+            M.status = gde_internal_fail(ctx, GDE_EHANG, "edit batch: a device-side wait ran out");
+        M.fallback = true;
         return M;
     }
-    // the edited rows and degrees back into the caller's host arrays
-    M.outcome.resize((size_t)k);
-    std::vector<int32_t> len32((size_t)n);
-    ck(cudaMemcpyAsync(M.outcome.data(), d_out, (size_t)k, cudaMemcpyDeviceToHost, st), "edit readback");
-    ck(cudaMemcpyAsync(h_indices, col, (size_t)G->g.cap * 4, cudaMemcpyDeviceToHost, st), "edit readback");
-    ck(cudaMemcpyAsync(len32.data(), rl, (size_t)n * 4, cudaMemcpyDeviceToHost, st), "edit readback");
+    // ---- repair lists, keys and degree tables, all on the device ----
+    const int nbk = (int)std::min<int64_t>(4096, (n + kEdT - 1) / kEdT + 1);
+    const int tb = (int)std::min<int64_t>(4096, (k + kEdT - 1) / kEdT + 1);
+    int* d_size = (int*)ws("mix_size", (size_t)n * 4);
+    int* d_off = (int*)ws("mix_off", (size_t)(n + 1) * 4);
+    int* d_flag = (int*)ws("mix_flag", (size_t)n * 4);
+    int* d_kidx = (int*)ws("mix_kidx", (size_t)(n + 1) * 4);
+    if (!d_size || !d_off || !d_flag || !d_kidx) {
+        M.status = gde_internal_fail(ctx, GDE_ENOMEM, "edit batch buffers");
+        return M;
+    }
+    mix_sizes_kernel<<<nbk, kEdT, 0, st>>>(d_icnt, d_dcnt, n, d_size);
+    if (exclusive_scan(ctx, d_size, d_off, n, st) != GDE_OK) { M.status = GDE_ENOMEM; return M; }
+    ins_flags_kernel<<<nbk, kEdT, 0, st>>>(d_icnt, d_flag, n);
+    if (exclusive_scan(ctx, d_flag, d_kidx, n, st) != GDE_OK) { M.status = GDE_ENOMEM; return M; }
+    int hcount[2] = {0, 0};  // list entries, keys
+    ck(cudaMemcpyAsync(&hcount[0], d_off + n, 4, cudaMemcpyDeviceToHost, st), "edit counts");
+    ck(cudaMemcpyAsync(&hcount[1], d_kidx + n, 4, cudaMemcpyDeviceToHost, st), "edit counts");
+    ck(cudaStreamSynchronize(st), "edit counts");
+    if (M.status != GDE_OK) return M;
+    const int total = hcount[0], nkeys = hcount[1];
+    int32_t* d_nbr = (int32_t*)ws("mix_nbr", (size_t)total * 4);
+    int32_t* d_keys = (int32_t*)ws("mix_keys", (size_t)nkeys * 4);
+    RepairKey* d_rk = (RepairKey*)ws("mix_rkeys", (size_t)nkeys * sizeof(RepairKey));
+    if (!d_nbr || !d_keys || !d_rk) {
+        M.status = gde_internal_fail(ctx, GDE_ENOMEM, "repair keys");
+        return M;
+    }
+    mix_fill_kernel<<<tb, kEdT, 0, st>>>(d_ops, d_out, d_rank, ki, d_icnt, d_off, d_nbr);
+    ins_keys_kernel<<<nbk, kEdT, 0, st>>>(d_icnt, d_kidx, n, d_keys);
+    if (nkeys > 0)
+        ins_repair_keys_kernel<<<(nkeys + kEdT - 1) / kEdT, kEdT, 0, st>>>(d_keys, nkeys, d_icnt, d_dcnt, d_off,
+                                                                          G->row_len, kind, beta, G->pw1, G->pwb,
+                                                                          d_rk);
+    const bool ign = (kind == KIND_IGN);
+    if (nt > 0)
+        mix_tables_kernel<<<(int)std::min<int64_t>(4096, (nt + kEdT - 1) / kEdT), kEdT, 0, st>>>(
+            d_nodes, nt, G->row_len, G->degf, G->degd, ign ? G->nfac : nullptr, G->tfac, G->tfac_f,
+            ign ? G->pw1 : nullptr, G->pwb);
+    ck(cudaGetLastError(), "edit repair lists");
+    // ---- the edited rows and degrees back into the caller's host arrays ----
+    // The touched rows' whole capacity (slack included, as the sequential
+    // pass leaves it), gathered on the device, or the whole array when the
+    // touched rows hold most of it.
+    std::vector<int64_t> off((size_t)nt + 1, 0);
+    for (int64_t t = 0; t < nt; t++) off[(size_t)t + 1] = off[(size_t)t] + indptr[touched[t] + 1] - indptr[touched[t]];
+    const bool whole = 2 * off[(size_t)nt] > G->g.cap;
+    int64_t* d_roff = (int64_t*)ws("mix_roff", (size_t)(nt + 1) * 8);
+    int32_t* d_lens = (int32_t*)ws("mix_lens", (size_t)nt * 4);
+    int32_t* d_buf = whole ? nullptr : (int32_t*)ws("mix_rows", (size_t)off[(size_t)nt] * 4);
+    if (!d_roff || !d_lens || (!whole && !d_buf)) {
+        M.status = gde_internal_fail(ctx, GDE_ENOMEM, "edit readback buffers");
+        return M;
+    }
+    std::vector<int32_t> lens((size_t)nt);
+    std::vector<int32_t> rows(whole ? 0 : (size_t)off[(size_t)nt]);
+    ck(cudaMemcpyAsync(d_roff, off.data(), (size_t)(nt + 1) * 8, cudaMemcpyHostToDevice, st), "edit readback");
+    const int gb = (int)std::min<int64_t>(4096, (nt * 32 + kEdT - 1) / kEdT + 1);
+    mix_gather_kernel<<<gb, kEdT, 0, st>>>(row_ptr, col, rl, d_nodes, d_roff, nt, d_buf, d_lens);
+    ck(cudaGetLastError(), "edit gather");
+    ck(cudaMemcpyAsync(lens.data(), d_lens, (size_t)nt * 4, cudaMemcpyDeviceToHost, st), "edit readback");
+    if (whole)
+        ck(cudaMemcpyAsync(h_indices, col, (size_t)G->g.cap * 4, cudaMemcpyDeviceToHost, st), "edit readback");
+    else
+        ck(cudaMemcpyAsync(rows.data(), d_buf, (size_t)off[(size_t)nt] * 4, cudaMemcpyDeviceToHost, st),
+           "edit readback");
     ck(cudaStreamSynchronize(st), "edit readback");
     if (M.status != GDE_OK) return M;
-    for (const auto& kv : tix) h_degree[kv.first] = len32[(size_t)kv.first];
+    for (int64_t t = 0; t < nt; t++) {
+        const int32_t u = touched[(size_t)t];
+        const int64_t d = lens[(size_t)t];
+        G->g.vol += (double)(d - h_degree[u]);
+        h_degree[u] = d;
+        G->h_len[u] = d;
+        G->h_deg[u] = (double)d;
+        if (!whole)
+            std::copy(rows.begin() + off[(size_t)t], rows.begin() + off[(size_t)t + 1], h_indices + indptr[u]);
+    }
+    M.keys = d_keys;
+    M.nkeys = nkeys;
+    M.rkeys = d_rk;
+    M.nbr = d_nbr;
+    M.repair_nbr = total;
     return M;
 }
 
-struct DeviceInsert {
-    int status = GDE_OK;
-    bool fallback = false;       // capacity exceeded: the host pass reproduces the partial edit
-    const int32_t* keys = nullptr;
-    int nkeys = 0;
-    RepairKey* rkeys = nullptr;
-    const int32_t* nbr = nullptr;
-    int64_t inserted = 0;
-};
-
-DeviceInsert device_insert(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree, const int32_t* us,
+DeviceEdit device_insert(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree, const int32_t* us,
                            const int32_t* vs, int64_t k, int kind, double beta) {
-    DeviceInsert R;
+    DeviceEdit R;
     const int64_t n = G->g.n;
     cudaStream_t st = gde_internal_stream(ctx);
     auto ws = [&](const char* name, size_t bytes) { return gde_internal_wsget(ctx, name, std::max<size_t>(bytes, 8)); };
@@ -673,8 +902,9 @@ DeviceInsert device_insert(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64
     }
     ins_keys_kernel<<<nbk, kEdT, 0, st>>>(d_cnt, d_kidx, n, d_keys);
     if (nkeys > 0)
-        ins_repair_keys_kernel<<<(nkeys + kEdT - 1) / kEdT, kEdT, 0, st>>>(d_keys, nkeys, d_cnt, d_off, G->row_len,
-                                                                          kind, beta, G->pw1, G->pwb, d_rk);
+        ins_repair_keys_kernel<<<(nkeys + kEdT - 1) / kEdT, kEdT, 0, st>>>(d_keys, nkeys, d_cnt, nullptr, d_off,
+                                                                          G->row_len, kind, beta, G->pw1, G->pwb,
+                                                                          d_rk);
     DI_CK(cudaGetLastError());
     // ---- the same edit on the caller's host arrays and the host mirror ----
     std::vector<int64_t> hpos(total);
@@ -697,7 +927,7 @@ DeviceInsert device_insert(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64
     R.nkeys = nkeys;
     R.rkeys = d_rk;
     R.nbr = d_nbr;
-    R.inserted = total / 2;
+    R.repair_nbr = total;
     return R;
 }
 
@@ -707,6 +937,10 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
                                   const int32_t* us, const int32_t* vs, int64_t k, int only_insert,
                                   const gde_params* p, int64_t F, void* Pm, void* Rm, const void* Xm, int64_t ld,
                                   double eps, double* oper_out, gde_stats* stats) {
+    const auto t_entry = std::chrono::steady_clock::now();
+    auto since_entry = [&]() {
+        return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_entry).count();
+    };
     if (!ctx || !G || !p || !h_indices || !h_degree || (k > 0 && (!us || !vs)))
         return gde_internal_fail(ctx, GDE_EINVAL, "bad update arguments");
     const int kind = p->kind;
@@ -726,8 +960,9 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
         G->dmax = -1.0;  // the degree bound recomputed and the spectral estimate dropped
         G->lam_max_est = NAN;
     }
-    // ---- insert-only batches: the edit, the repair keys and the push all on the device ----
-    bool dev_ok = only_insert && k > 0 && G->deg_is_len;
+    // ---- the edit, the repair keys and the push all on the device: insert-only
+    // batches in one pass, batches with deletions as a dataflow over the edges ----
+    bool dev_ok = k > 0 && G->deg_is_len;
     for (int64_t e = 0; dev_ok && e < k; e++)
         dev_ok = us[e] >= 0 && us[e] < n && vs[e] >= 0 && vs[e] < n && us[e] != vs[e];
     if (dev_ok) {
@@ -736,7 +971,8 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
             if (rc0 == GDE_OK) rc0 = ensure_power_tables(ctx, G, p->beta);
             if (rc0 != GDE_OK) return rc0;
         }
-        DeviceInsert D = device_insert(ctx, G, h_indices, h_degree, us, vs, k, kind, p->beta);
+        DeviceEdit D = only_insert ? device_insert(ctx, G, h_indices, h_degree, us, vs, k, kind, p->beta)
+                                   : device_mixed_edit(ctx, G, h_indices, h_degree, us, vs, k, kind, p->beta);
         if (D.status != GDE_OK) return D.status;
         // InstantGNN tables built for an earlier call are not updated by this
         // kind's edit: the next InstantGNN call rebuilds them
@@ -765,6 +1001,7 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
                 if (e != cudaSuccess) return gde_internal_fail(ctx, GDE_ECUDA, cudaGetErrorString(e));
             }
             std::vector<double> opers(F, 0.0);
+            const double edit_ms = since_entry();
             if (D.nkeys > 0) {
                 int rc = gde_internal_feature_push(ctx, G, p, F, Pm, Rm, ld, eps, D.keys, D.nkeys, opers.data(),
                                                    stats);
@@ -773,10 +1010,13 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
                 memset(stats, 0, sizeof(*stats));
             }
             // the beta = 0 PPR update counts the repair work (ppr_solver.py:776-792)
-            const double oper_repair = 2.0 * (double)D.nkeys + 2.0 * (double)D.inserted;
+            const double oper_repair = 2.0 * (double)D.nkeys + (double)D.repair_nbr;
             if (oper_out)
                 for (int64_t c = 0; c < F; c++) oper_out[c] = opers[c] + (kind == KIND_UPPR ? oper_repair : 0.0);
-            if (stats) stats->edit_path = GDE_EDIT_DEVICE_INSERT;
+            if (stats) {
+                stats->edit_path = only_insert ? GDE_EDIT_DEVICE_INSERT : GDE_EDIT_DEVICE_DATAFLOW;
+                stats->edit_ms = edit_ms;
+            }
             return GDE_OK;
         }
     }
@@ -786,30 +1026,7 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
     std::vector<int64_t> pos;
     std::vector<int32_t> val;
     int status = GDE_OK;
-    // batches with deletions run as a dataflow on the device (device_mixed_edit);
-    // each edge's outcome there rebuilds the reference's insert / delete maps
-    bool on_device = false;
-    if (!only_insert && k > 0 && G->deg_is_len) {
-        bool ok = true;
-        for (int64_t e = 0; ok && e < k; e++) ok = us[e] >= 0 && us[e] < n && vs[e] >= 0 && vs[e] < n;
-        if (ok) {
-            MixResult M = device_mixed_edit(ctx, G, h_indices, h_degree, us, vs, k);
-            if (M.status != GDE_OK) return M.status;
-            if (!M.fallback) {
-                on_device = true;
-                for (int64_t e = 0; e < k; e++) {
-                    if (M.outcome[(size_t)e] == MIX_INSERT) {
-                        ins.add(us[e], vs[e]);
-                        ins.add(vs[e], us[e]);
-                    } else if (M.outcome[(size_t)e] == MIX_DELETE) {
-                        del.add(us[e], vs[e]);
-                        del.add(vs[e], us[e]);
-                    }
-                }
-            }
-        }
-    }
-    for (int64_t e = 0; e < k && !on_device; e++) {
+    for (int64_t e = 0; e < k; e++) {
         int64_t u = us[e], v = vs[e];
         if (u < 0 || u >= n || v < 0 || v >= n) { status = GDE_EINVAL; break; }
         bool insertion = true;
@@ -932,6 +1149,7 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
     }
     // ---- (3) push from the repaired nodes (InstantGNN.py:315-325) ----
     std::vector<double> opers(F, 0.0);
+    const double edit_ms = since_entry();
     if (!cand.empty()) {
         int32_t* d_cand = (int32_t*)gde_internal_wsget(ctx, "update_cand", cand.size() * 4);
         if (!d_cand) return gde_internal_fail(ctx, GDE_ENOMEM, "candidate list");
@@ -944,6 +1162,9 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
     }
     if (oper_out)
         for (int64_t c = 0; c < F; c++) oper_out[c] = opers[c] + (kind == KIND_UPPR ? oper_repair : 0.0);
-    if (stats) stats->edit_path = on_device ? GDE_EDIT_DEVICE_DATAFLOW : GDE_EDIT_HOST;
+    if (stats) {
+        stats->edit_path = GDE_EDIT_HOST;
+        stats->edit_ms = edit_ms;
+    }
     return GDE_OK;
 }

@@ -35,7 +35,8 @@ class Stats(ctypes.Structure):
     _fields_ = [("kernel_ms", _dbl), ("total_ms", _dbl), ("rounds", _i64), ("dense_rounds", _i64),
                 ("union_vol", _dbl), ("col_vol", _dbl), ("union_nodes", ctypes.c_uint64),
                 ("col_nodes", ctypes.c_uint64), ("tiles", _int), ("tile_w", _int),
-                ("check_ms", _dbl), ("prep_ms", _dbl), ("scatter_ms", _dbl), ("edit_path", _int)]
+                ("check_ms", _dbl), ("prep_ms", _dbl), ("scatter_ms", _dbl), ("edit_path", _int),
+                ("edit_ms", _dbl)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

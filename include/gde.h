@@ -92,6 +92,7 @@ typedef struct {
     double prep_ms;             /* each including the wait at the phase's closing grid barrier */
     double scatter_ms;
     int edit_path;              /* gde_feature_update: how the edge batch was applied (GDE_EDIT_*) */
+    double edit_ms;             /* gde_feature_update: host time from the call to the push (edit + repair) */
 } gde_stats;
 
 /* gde_stats.edit_path */

@@ -7,9 +7,9 @@ rows.  The device pass keeps that sequential meaning exactly: each edge waits
 until every earlier edge that shares an endpoint has been applied.  These
 tests check, on padded graphs with slack, that the device pass ran
 (``gde_stats.edit_path``) and that the edited arrays, the repaired residuals
-and the push are the same as the oracle's sequential pass.  A batch that
-overflows a row's slack falls back to the host pass and must give the same
-result.
+and the push are the same as the oracle's sequential pass.  A batch whose
+insertion finds a row full is handed to the host pass, which applies the
+edges before it and reports ``GDE_ECAPACITY``.
 """
 import numpy as np
 import pytest
@@ -113,12 +113,57 @@ def test_mixed_batch_then_push_on_the_edited_graph_matches_a_fresh_upload():
     np.testing.assert_allclose(out[0][1], out[1][1], rtol=1e-12, atol=1e-15)
 
 
-def test_row_without_slack_falls_back_to_the_host_pass():
+def test_row_touched_more_often_than_its_slack_stays_on_the_device():
+    """The slack test is exact (made when an insertion runs), not a bound from the batch."""
     g = graphs.chung_lu(3000, 2.2, 6.0, 120.0, seed=22)
     hub = int(np.argmax(np.diff(g.indptr)))
     us, vs = _mixed_batch(g, 100, 100, 20, seed=6, hub=hub, hub_times=12)
     res, _, _, _ = _run_uppr(g, 4, us, vs, graphs.uniform_seeds(g, 2, seed=3))
-    assert res["stats"]["edit_path"] == EDIT_HOST
+    assert res["stats"]["edit_path"] == EDIT_DEVICE_DATAFLOW
+
+
+def test_batch_that_fills_a_row_gives_the_host_pass_partial_edit_and_error():
+    """A row without slack for an insertion: the device run is abandoned, the touched rows go back to
+    the caller's arrays, and the host pass applies the edges before that one and reports the error."""
+    import torch
+    g = graphs.chung_lu(3000, 2.2, 6.0, 120.0, seed=24)
+    n = g.n
+    slack = 2
+    ip, ix, dg = _padded(g, slack)
+    rng = np.random.default_rng(17)
+    us, vs = _mixed_batch(g, 150, 150, 30, seed=9)
+    low = int(np.argmin(np.diff(g.indptr)))
+    new = rng.choice(np.setdiff1d(np.arange(n), np.concatenate([[low], g.indices[g.indptr[low]:g.indptr[low + 1]]])),
+                     size=slack + 1, replace=False)
+    cut = len(us) // 2
+    us = np.concatenate([us[:cut], np.full(slack + 1, low, np.int32), us[cut:]]).astype(np.int32)
+    vs = np.concatenate([vs[:cut], new.astype(np.int32), vs[cut:]]).astype(np.int32)
+    # the expected partial edit: the oracle, edge by edge, up to the insertion that finds a row full
+    ix_o, dg_o = ix.copy(), dg.copy()
+    stop = None
+    for e in range(len(us)):
+        u, v = int(us[e]), int(vs[e])
+        row = ix_o[ip[u]:ip[u] + dg_o[u]]
+        present = (row == v).any()
+        if not present and (dg_o[u] >= ip[u + 1] - ip[u] or dg_o[v] >= ip[v + 1] - ip[v]):
+            stop = e
+            break
+        O.update_graph(n, ip, ix_o, dg_o, us[e:e + 1], vs[e:e + 1], False)
+    assert stop is not None and stop <= cut + slack
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    P = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    R = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    with pytest.raises(L.GDEError) as ei:
+        api.feature_update(Gd, L.UPPR, ix, dg, us, vs, False, P, R, None, 1e-5, alpha=0.1, prec="fp64", tile_w=1)
+    assert ei.value.status == L.GDE_ECAPACITY
+    np.testing.assert_array_equal(ix, ix_o)
+    np.testing.assert_array_equal(dg, dg_o)
+    # the device copy holds the same partial edit
+    fresh = api.Graph(ip, ix.copy(), row_len=dg.copy(), degree=dg.astype(np.float64))
+    seeds = graphs.uniform_seeds(g, 3, seed=5)
+    a = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, 1e-7, prec="fp64", alpha=0.15, tile_w=1)
+    b = api.solve(fresh, L.PPR, L.LOCAL_GD, seeds, 1e-7, prec="fp64", alpha=0.15, tile_w=1)
+    np.testing.assert_allclose(a["x"], b["x"], rtol=1e-12, atol=1e-16)
 
 
 @pytest.mark.parametrize("algo", ["fwdbatch"])
