@@ -1021,6 +1021,10 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
             return fail(ctx, GDE_EINVAL, "eps * degree[s_node] > 1 (ppr_solver.py:213)");
     }
     if (hk && !(p->tau >= 1.0)) return fail(ctx, GDE_EINVAL, "tau must be >= 1 (hk_solver.py:35)");
+    // HK relaxation: 0 or 1 is none; the relaxed push converges for 0 < omega < 2
+    const bool relax = (method == M_HK_LOCAL || method == M_HK_GLOBAL) && p->omega != 0.0 && p->omega != 1.0;
+    if (relax && !(p->omega > 0.0 && p->omega < 2.0)) return fail(ctx, GDE_EINVAL, "HK omega must be in (0, 2)");
+    if (relax && p->prec != GDE_FP64) return fail(ctx, GDE_EINVAL, "HK relaxation omega != 1 runs in FP64");
     if (stats) memset(stats, 0, sizeof(*stats));
     if (nq == 0) return GDE_OK;
     gde_params pp = *p;
@@ -1142,6 +1146,7 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
             P.x_gain = 1.0;
             P.coef_tab = d_ctab;
             P.psi_tab = hk ? d_psi[td.N] : nullptr;
+            P.omega = relax ? p->omega : 0.0;
             TileState& S = ts[t];
             memset(&S, 0, sizeof(S));
             S.dense_next[0] = method_is_global(method) ? 1 : 0;
@@ -1246,7 +1251,8 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
                 int64_t q = td.qs[c];
                 double oper;
                 if (method == M_GLOBAL_GD || method == M_GLOBAL_CHEBY) oper = (double)C.rounds * ((double)n + m_vol);
-                else if (method == M_HK_GLOBAL) oper = (double)C.rounds * (m_vol + (double)n);
+                else if (method == M_HK_GLOBAL)
+                    oper = (double)(relax ? C.sweep_sum : (int64_t)C.rounds) * (m_vol + (double)n);
                 else if (method == M_HK_TAYLOR) oper = 0.0;
                 else oper = C.oper;
                 if (oper_out) oper_out[q] = oper;

@@ -93,7 +93,13 @@ struct TileParams {           // host-written, read-only during a launch
     const double* coef_tab;   // Chebyshev: beta_t (PPR) or (beta1_t, beta2_t) pairs (Katz), per round
     const double* psi_tab;    // HK: psi[0..N]
     int64_t seed_base;        // unused by the kernel (bookkeeping)
+    double omega;             // HK: relaxation of hk_sor_queue (0 and 1: none)
 };
+
+// HK relaxation omega != 1 (hk_solver.py:248-264): each push moves omega r
+// and keeps (1 - omega) r at its level.
+__host__ __device__ inline bool hk_relaxed(const TileParams& tp) { return tp.omega != 0.0 && tp.omega != 1.0; }
+constexpr int kMaxRelax = 1 << 16;  // bound on the sub-pushes of one node at one level
 
 // Counter discipline (no phase ever reads a field another block writes in
 // the same phase).  Round r of a tile has level = ts.round + it, parity
@@ -160,6 +166,8 @@ struct ColState {             // one per column slot
     int check_cnt[2];         // global methods: nodes above threshold (parity)
     int seed;                 // seed node (-1 for feature columns)
     int pad;
+    int hk_sweeps[2];         // HK global sweeps, omega != 1: sweeps of the level (parity), max over nodes
+    int64_t sweep_sum;        // HK global sweeps, omega != 1: sweeps over all levels
     unsigned long long finish_ns;  // %globaltimer when the column finished (0 = not yet)
 };
 

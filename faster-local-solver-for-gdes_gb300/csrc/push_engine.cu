@@ -169,7 +169,27 @@ struct TileSh {
     int final_level;        // HK: pushes of this level go into X
     int col_live[kMaxW];
     double col_theta[kMaxW];
+    int col_sweeps[kMaxW];  // HK global sweeps with omega != 1: sweeps of this level
 };
+
+// HK relaxation (hk_solver.py:248-264, :266-280): a push moves omega r into
+// the solution and the next level and keeps r - omega r at this level.  The
+// node pushes `fixed` times (global sweeps), or while its residual stays at
+// or above thr (local queue); returns the total moved, the sub-pushes and
+// the residual left, which the level then drops (:284).
+__device__ __forceinline__ double hk_relax(double r, double omega, double thr, int fixed, int* subs, double* left) {
+    double moved = 0.0;
+    int s = 0;
+    do {
+        const double ru = omega * r;
+        moved += ru;
+        r -= ru;
+        ++s;
+    } while (s < kMaxRelax && (fixed > 0 ? s < fixed : fabs(r) >= thr));
+    *subs = s;
+    *left = r;
+    return moved;
+}
 
 __device__ __forceinline__ bool is_absorbing(const DevGraph& g, int u) {
     int len = g.row_len[u];
@@ -220,7 +240,65 @@ __device__ void load_tile(const PushArgs& a, int t, int it, TileSh& sh) {
         if (live && (m == M_GLOBAL_GD || m == M_GLOBAL_CHEBY) && c.check_cnt[sh.parity] == 0) live = 0;
         sh.col_theta[threadIdx.x] = c.theta;
         sh.col_live[threadIdx.x] = live;
+        sh.col_sweeps[threadIdx.x] = max(1, c.hk_sweeps[sh.parity]);
     }
+    __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// HK global sweeps with omega != 1 (hk_solver.py:266-280): a level repeats
+// its sweep over all nodes until no residual is at or above threshold, so
+// every node takes the same number of sweeps, the most any node needs.  This
+// phase finds that number before the level's PREP pushes.
+// ---------------------------------------------------------------------------
+template <typename T, int W>
+__device__ void hk_sweeps_phase(const PushArgs& a, int t, int it) {
+    constexpr int VEC = (sizeof(T) == 4) ? (W >= 4 ? 4 : W) : (W >= 2 ? 2 : 1);
+    constexpr int L = W / VEC;
+    __shared__ int s_live[kMaxW];
+    __shared__ double s_theta[kMaxW];
+    __shared__ int s_max[kMaxW];
+    const int64_t n = a.g.n;
+    const TileParams& tp = a.tp[t];
+    const int level = it - a.ts[t].t0;
+    const int par = level & 1;
+    const T* R = slab_ptr<T>(par ? a.R2 : a.R, a, t);
+    const double psi = tp.psi_tab[level];
+    const double nl = (double)tp.n_levels;
+    if (threadIdx.x < W) {
+        const ColState& c = a.cs[(int64_t)t * W + threadIdx.x];
+        s_live[threadIdx.x] = (threadIdx.x < tp.ncols) && c.live;
+        s_theta[threadIdx.x] = c.theta;
+        s_max[threadIdx.x] = 1;
+    }
+    __syncthreads();
+    const int c0 = (threadIdx.x % L) * VEC;
+    int mx[VEC];
+#pragma unroll
+    for (int i = 0; i < VEC; ++i) mx[i] = 1;
+    const int64_t gid = ((int64_t)blockIdx.x * kThreads + threadIdx.x) / L;
+    const int64_t ng = (int64_t)gridDim.x * kThreads / L;
+    for (int64_t u = gid; u < n; u += ng) {
+        Vec<T, VEC> rv;
+        vload<T, VEC>(R + u * a.ld + c0, rv);
+        const double d = a.g.degd[u];
+#pragma unroll
+        for (int i = 0; i < VEC; ++i) {
+            const double r = (double)rv.v[i];
+            if (!s_live[c0 + i] || r == 0.0) continue;
+            const double thr = ((s_theta[c0 + i] * d) / nl) / psi;
+            int subs;
+            double left;
+            hk_relax(r, tp.omega, thr, 0, &subs, &left);
+            mx[i] = max(mx[i], subs);
+        }
+    }
+#pragma unroll
+    for (int i = 0; i < VEC; ++i)
+        if (mx[i] > 1) atomicMax(&s_max[c0 + i], mx[i]);
+    __syncthreads();
+    if (threadIdx.x < W && s_max[threadIdx.x] > 1)
+        atomicMax(&a.cs[(int64_t)t * W + threadIdx.x].hk_sweeps[par], s_max[threadIdx.x]);
     __syncthreads();
 }
 
@@ -685,6 +763,20 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
                             push.v[k] = (T)pv;
                             xadd.v[k] = (kind == KIND_IGN && !absorb) ? (T)(sh.tp.x_gain * rv) : r.v[k];
                             r.v[k] = T(0);
+                            if constexpr (sizeof(T) == 8) {  // HK relaxation runs in FP64 only (host-checked)
+                                if (kind == KIND_HK && hk_relaxed(sh.tp)) {
+                                    const double thr = ((thr_scale[k] * du) / (double)sh.tp.n_levels) / sh.psi;
+                                    int subs;
+                                    double left;
+                                    const double moved = hk_relax(rv, sh.tp.omega, thr,
+                                                                  global ? sh.col_sweeps[c0 + k] : 0, &subs, &left);
+                                    if (sh.final_level) push.v[k] = moved / du;
+                                    else push.v[k] = ((sh.tp.tau / ((double)sh.level + 1.)) * moved) / du;
+                                    xadd.v[k] = moved;
+                                    r.v[k] = left;
+                                    my_oper[k] += (double)(subs - 1) * du;  // the first sub-push is counted below
+                                }
+                            }
                         }
                         wrote = true;
                         my_nodes[k] += 1;
@@ -838,8 +930,13 @@ __device__ void zero_next_counters(const PushArgs& a, int t, int level) {
         ts.union_vol[np] = 0.0;
     }
     if (threadIdx.x < W) {
-        a.cs[(int64_t)t * W + threadIdx.x].round_active[np] = 0;
-        a.cs[(int64_t)t * W + threadIdx.x].check_cnt[np] = 0;
+        ColState& c = a.cs[(int64_t)t * W + threadIdx.x];
+        c.round_active[np] = 0;
+        c.check_cnt[np] = 0;
+        if (a.tp[t].method == M_HK_GLOBAL && hk_relaxed(a.tp[t])) {
+            c.sweep_sum += max(1, c.hk_sweeps[np ^ 1]);  // this level's sweeps, final after the CHECK phase
+            c.hk_sweeps[np] = 0;
+        }
     }
 }
 
@@ -1556,7 +1653,8 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
                 rs.tiles[k] = t;
                 rs.level[k] = it - a.ts[t].t0;
                 const int m = a.tp[t].method;
-                if (m == M_GLOBAL_GD || m == M_GLOBAL_CHEBY) rs.any_check = 1;
+                if (m == M_GLOBAL_GD || m == M_GLOBAL_CHEBY || (m == M_HK_GLOBAL && hk_relaxed(a.tp[t])))
+                    rs.any_check = 1;
             }
         }
         if (threadIdx.x == 0) rs.ntl = (int)rs.off[0][a.ntiles];
@@ -1570,6 +1668,8 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
             for (int k = 0; k < ntl; ++k) {
                 const int t = rs.tiles[k];
                 const int m = a.tp[t].method;
+                if constexpr (sizeof(T) == 8)
+                    if (m == M_HK_GLOBAL && hk_relaxed(a.tp[t])) hk_sweeps_phase<T, W>(a, t, it);
                 if (m != M_GLOBAL_GD && m != M_GLOBAL_CHEBY) continue;
                 check_phase<T, W>(a, t, it, s_cnt);
             }

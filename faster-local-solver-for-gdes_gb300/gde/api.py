@@ -101,8 +101,10 @@ def make_params(kind: int, method: int, prec: str = "fp64", tile_w: int = 0, alp
 def solve(graph: Graph, kind: int, method: int, seeds, eps, *, prec: str = "fp64", out64: bool | None = None,
           want_x: bool = True, want_r: bool = True, x_out=None, r_out=None, device_out: bool = False,
           tile_w: int = 0, alpha: float = 0.0, tau: float = 0.0, l_max: float = 0.0, mu_min: float = 0.0,
-          max_rounds: int = 0, tuning: dict | None = None) -> dict:
+          max_rounds: int = 0, tuning: dict | None = None, omega: float = 1.0) -> dict:
     """Solve one query per seed; returns dict(x, r, oper, rounds, stats).
+
+    ``omega`` (heat-kernel level push only): relaxation of hk_sor_queue, in (0, 2).
 
     ``x_out`` / ``r_out`` may be caller buffers (numpy / torch, host or
     device per ``device_out``) of shape [nq, n] (HK residual: [nq, 2, n]).
@@ -134,7 +136,8 @@ def solve(graph: Graph, kind: int, method: int, seeds, eps, *, prec: str = "fp64
     oper = np.zeros(nq, dtype=np.float64)
     rounds = np.zeros(nq, dtype=np.int32)
     lat = np.zeros(nq, dtype=np.float32)
-    p = make_params(kind, method, prec, tile_w, alpha, tau, l_max, mu_min, max_rounds=max_rounds, tuning=tuning)
+    p = make_params(kind, method, prec, tile_w, alpha, tau, l_max, mu_min, omega=omega, max_rounds=max_rounds,
+                    tuning=tuning)
     st = L.Stats()
     status = lib.gde_solve(graph.ctx.ptr, graph.ptr, ctypes.byref(p), nq, _ptr(seeds), _ptr(eps),
                            _ptr(x_out) if want_x else None, _ptr(r_out) if want_r else None, int(out64),

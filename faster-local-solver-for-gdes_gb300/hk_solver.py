@@ -2,9 +2,13 @@
 
     h = e^{-tau} sum_k tau^k/k! (A D^{-1})^k e_s, truncated at N = estimate_n(tau, eps/2)
 
-``hk_sor_queue`` runs the level-synchronous push (omega = 1) on the GPU:
-level j's active nodes move r_j into x and push tau/(j+1) r_j/d into level
-j+1; the last level pushes r/d straight into x (hk_solver.py:235-295).
+``hk_sor_queue`` runs the level-synchronous push on the GPU: level j's
+active nodes move r_j into x and push tau/(j+1) r_j/d into level j+1; the
+last level pushes r/d straight into x (hk_solver.py:235-295).  With a
+relaxation omega != 1 a node moves omega r and keeps r - omega r at its
+level, and relaxes again while that stays at or above its threshold
+(hk_solver.py:248-264); the global form sweeps all nodes together as the
+reference does (:266-280).
 ``hk_taylor_approx`` is the global Taylor series (hk_solver.py:51-80).
 """
 from __future__ import annotations
@@ -48,29 +52,35 @@ def hk_taylor_approx(n, indptr, indices, degree, s_node, tau, eps):
 def hk_sor_queue(n, indptr, indices, degree, s_node, tau, eps, omega, local):
     """Level push (hk_solver.py:206-295) -> (est_n, xt, rt[2, n], oper, beta_t, run_time, algo_time).
 
-    The GPU push is level-synchronous with omega = 1 (the reference's "ahk"
-    configuration); other omega values are refused rather than silently
-    changed.  beta_t is not tracked by the GPU path and is returned empty.
+    omega = 1 and the global form (local=False) give the reference's result.
+    The local form with omega != 1 relaxes every node at or above threshold
+    until its kept residual drops below it.  The reference's queue instead
+    re-enqueues a node only if it is not yet queued for the next level
+    (hk_solver.py:262), a test that depends on the queue order and that
+    leaves most of (1 - omega) r unpushed.  beta_t is not tracked by the GPU
+    path and is returned empty.
     """
-    if omega != 1.0:
-        raise NotImplementedError("hk_sor_queue on the GPU implements omega = 1 (level-synchronous push)")
     g = graph_for(indptr, indices, degree)
     with Timer() as t:
-        r = api.solve(g, L.HK, L.HK_LOCAL if local else L.HK_GLOBAL, [s_node], [eps], prec="fp64", tau=tau)
+        r = api.solve(g, L.HK, L.HK_LOCAL if local else L.HK_GLOBAL, [s_node], [eps], prec="fp64", tau=tau,
+                      omega=float(omega))
     est_n = estimate_n(tau, .5 * eps)
     return est_n, r["x"][0], r["r"][0], float(r["oper"][0]), [], t.dt, t.dt
 
 
 def solve_a_graph_all(n, indptr, indices, degree, tau, eps, omega, graph_name, s_nodes):
-    """(hk_solver.py:303-366) with the omega = 1 ("ahk") entries computed; SOR entries stay zero."""
+    """(hk_solver.py:303-366): local and global SOR with ``omega``, then the omega = 1 ("ahk") pair.
+
+    The Taylor and relax entries stay zero, as the reference leaves them.
+    """
     test_num = len(s_nodes)
     z = lambda: np.zeros(test_num, dtype=np.int64)  # noqa: E731
     zt = lambda: np.zeros(test_num)  # noqa: E731
-    la_o, la_t, ga_o, ga_t = z(), zt(), z(), zt()
-    for ii in range(test_num):
-        res = hk_sor_queue(n, indptr, indices, degree, int(s_nodes[ii]), tau, eps, 1.0, True)
-        la_o[ii], la_t[ii] = res[3], res[6]
-    for ii in range(test_num):
-        res = hk_sor_queue(n, indptr, indices, degree, int(s_nodes[ii]), tau, eps, 1.0, False)
-        ga_o[ii], ga_t[ii] = res[3], res[6]
-    return (s_nodes, z(), zt(), z(), zt(), la_o, la_t, ga_o, ga_t, z(), zt(), z(), zt())
+    out = []
+    for om, local in ((omega, True), (omega, False), (1.0, True), (1.0, False)):
+        o, t = z(), zt()
+        for ii in range(test_num):
+            res = hk_sor_queue(n, indptr, indices, degree, int(s_nodes[ii]), tau, eps, om, local)
+            o[ii], t[ii] = res[3], res[6]
+        out += [o, t]
+    return (s_nodes, *out, z(), zt(), z(), zt())

@@ -714,6 +714,85 @@ double orc_hk_sor_queue(i64 n, const i64 *indptr, const i32 *indices, const doub
     return oper;
 }
 
+/* Level-synchronous form of hk_sor_queue (the GPU's order).  Level j
+ * pushes every node whose residual is at or above its threshold, each with
+ * its relaxation sub-pushes back to back (omega r moved, r - omega r kept,
+ * while the kept part stays at or above the threshold), in node order.
+ * Without a queue there is no re-enqueue test on the next level's mark
+ * (hk_solver.py:262), the only order-dependent step of the reference's local
+ * form.  The global form is the reference's (:266-280): all nodes sweep
+ * together until no residual is at or above threshold, so each node takes
+ * the largest sub-push count any node needs. */
+static double hk_relax_moved(double r, double omega, double thr, i64 fixed, i64 *subs, double *left) {
+    double moved = 0.;
+    i64 k = 0;
+    do {
+        double ru = omega * r;
+        moved += ru;
+        r -= ru;
+        k++;
+    } while (k < 65536 && (fixed > 0 ? k < fixed : fabs(r) >= thr));
+    *subs = k;
+    *left = r;
+    return moved;
+}
+
+double orc_hk_sor_sync(i64 n, const i64 *indptr, const i32 *indices, const double *degree, i64 s, double tau,
+                       double eps, double omega, int local, double *xt, double *r2, i64 *est_n_out) {
+    double m = 0.0, oper = 0.;
+    for (i64 i = 0; i < n; i++) m += degree[i];
+    memset(xt, 0, (size_t)n * sizeof(double));
+    memset(r2, 0, (size_t)(2 * n) * sizeof(double));
+    double *rt[2] = {r2, r2 + n};
+    rt[0][s] = 1.;
+    i64 est_n = orc_hk_estimate_n(tau, .5 * eps);
+    double *psi = (double *)calloc((size_t)est_n + 1, sizeof(double));
+    psi[est_n] = 1.;
+    for (i64 i = est_n - 1; i >= 0; i--) psi[i] = psi[i + 1] * tau / ((double)i + 1.) + 1.;
+    double *eps_vec = (double *)malloc((size_t)n * sizeof(double));
+    for (i64 i = 0; i < n; i++) eps_vec[i] = exp(tau) * eps * degree[i] / (double)est_n;
+    for (i64 j = 0; j < est_n; j++) {
+        double *rc = rt[j % 2], *rn = rt[(j + 1) % 2];
+        i64 sweeps = 0, any = 0;
+        for (i64 u = 0; u < n; u++) {
+            double thr = eps_vec[u] / psi[j];
+            if (fabs(rc[u]) >= thr) any = 1;
+            if (!local) {
+                i64 k;
+                double left;
+                hk_relax_moved(rc[u], omega, thr, 0, &k, &left);
+                if (k > sweeps) sweeps = k;
+            }
+        }
+        if (local && !any) break;
+        for (i64 u = 0; u < n; u++) {
+            double thr = eps_vec[u] / psi[j];
+            if (local ? fabs(rc[u]) < thr : rc[u] == 0.) continue;
+            i64 k;
+            double left;
+            double moved = hk_relax_moved(rc[u], omega, thr, local ? 0 : sweeps, &k, &left);
+            if (local) oper += (double)k * degree[u];
+            xt[u] += moved;
+            rc[u] = left;
+            for (i64 e = indptr[u]; e < indptr[u + 1]; e++) {
+                i64 v = indices[e];
+                if (j + 1 == est_n)
+                    xt[v] += moved / degree[u];
+                else
+                    rn[v] += ((tau / ((double)j + 1.)) * moved) / degree[u];
+            }
+        }
+        if (!local) oper += (double)sweeps * (m + (double)n);
+        memset(rc, 0, (size_t)n * sizeof(double));
+    }
+    double et = exp(tau);
+    for (i64 i = 0; i < n; i++) xt[i] /= et;
+    free(psi);
+    free(eps_vec);
+    *est_n_out = est_n;
+    return oper;
+}
+
 /* hk_taylor_approx, :51-80 */
 i64 orc_hk_taylor(i64 n, const i64 *indptr, const i32 *indices, const double *degree, i64 s, double tau,
                   double eps, double *xt) {

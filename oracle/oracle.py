@@ -61,6 +61,8 @@ def lib():
         L.orc_hk_estimate_n.argtypes = [_dbl, _dbl]
         L.orc_hk_sor_queue.restype = _dbl
         L.orc_hk_sor_queue.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _dbl, _int, _p, _p, _p]
+        L.orc_hk_sor_sync.restype = _dbl
+        L.orc_hk_sor_sync.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _dbl, _int, _p, _p, _p]
         L.orc_hk_taylor.restype = _i64
         L.orc_hk_taylor.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _p]
         L.orc_ign_static_column.restype = None
@@ -168,14 +170,20 @@ def hk_estimate_n(t, eps):
     return int(lib().orc_hk_estimate_n(t, eps))
 
 
-def hk_sor_queue(n, indptr, indices, degree, s, tau, eps, omega, local):
-    """``hk_solver.hk_sor_queue`` (hk_solver.py:206-295) -> (est_n, x, r[2,n], oper)."""
+def hk_sor_queue(n, indptr, indices, degree, s, tau, eps, omega, local, sync=False):
+    """``hk_solver.hk_sor_queue`` (hk_solver.py:206-295) -> (est_n, x, r[2,n], oper).
+
+    sync=True: the level-synchronous form (every node at or above threshold
+    relaxes at its level, no re-enqueue test on the next level's mark); equal
+    to the reference for omega = 1 and for the global form.
+    """
     indptr, indices, degree = _graph(indptr, indices, degree)
     x = np.zeros(n)
     r = np.zeros((2, n))
     est = np.zeros(1, dtype=np.int64)
-    oper = lib().orc_hk_sor_queue(n, _ptr(indptr), _ptr(indices), _ptr(degree), int(s), tau, eps, omega, int(local),
-                                  _ptr(x), _ptr(r), _ptr(est))
+    fn = lib().orc_hk_sor_sync if sync else lib().orc_hk_sor_queue
+    oper = fn(n, _ptr(indptr), _ptr(indices), _ptr(degree), int(s), tau, eps, omega, int(local), _ptr(x), _ptr(r),
+              _ptr(est))
     return int(est[0]), x, r, float(oper)
 
 

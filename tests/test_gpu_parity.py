@@ -153,6 +153,37 @@ def test_hk_level_push_matches_reference(golden_graphs):
         np.testing.assert_allclose(res["r"][0], c["o"]["r"], rtol=1e-9, atol=1e-15)
 
 
+@pytest.mark.parametrize("omega", [0.8, 1.3, 1.6])
+@pytest.mark.parametrize("local", [True, False])
+def test_hk_relaxed_level_push_matches_oracle(golden_graphs, omega, local):
+    """HK with relaxation omega != 1: the level-synchronous oracle (which is the reference's
+    own result for the global sweeps) gives the same opers and solution."""
+    seen = set()
+    for c in G.cases("hk_sor_queue"):
+        p = c["p"]
+        key = (c["graph"], int(p["s"]), float(p["tau"]), float(p["eps"]))
+        if key in seen:
+            continue
+        seen.add(key)
+        d, Gd = golden_graphs[c["graph"]]
+        n = len(d["indptr"]) - 1
+        deg = np.diff(d["indptr"]).astype(np.float64)
+        _, xo, _, oo = O.hk_sor_queue(n, d["indptr"], d["indices"], deg, int(p["s"]), p["tau"], p["eps"], omega, local,
+                                      sync=True)
+        res = api.solve(Gd, L.HK, L.HK_LOCAL if local else L.HK_GLOBAL, [int(p["s"])], [p["eps"]], prec="fp64",
+                        tau=p["tau"], omega=omega)
+        assert res["oper"][0] == pytest.approx(oo, rel=OPER_RTOL), c["id"]
+        assert rel_l1(res["x"][0], xo) < 1e-11, c["id"]
+
+
+def test_hk_omega_outside_the_convergent_range_is_rejected(golden_graphs):
+    d, Gd = next(iter(golden_graphs.values()))
+    for omega in (2.0, -0.5):
+        with pytest.raises(L.GDEError) as ei:
+            api.solve(Gd, L.HK, L.HK_LOCAL, [0], [1e-5], prec="fp64", tau=3.0, omega=omega)
+        assert ei.value.status == L.GDE_EINVAL
+
+
 def test_hk_taylor_matches_reference(golden_graphs):
     for c in G.cases("hk_taylor_approx"):
         p = c["p"]

@@ -91,6 +91,44 @@ def test_hk_sor_queue(c):
     _close(r, c["o"]["r"])
 
 
+@pytest.mark.parametrize("c", G.cases("hk_sor_queue"), ids=lambda c: c["id"])
+def test_hk_sync_form_is_the_reference_where_order_cannot_matter(c):
+    """The level-synchronous HK form (the GPU's) equals the reference's queue for omega = 1
+    and for the global sweeps at any omega; only the local form with omega != 1 differs
+    (its re-enqueue test reads the next level's queue marks)."""
+    ip, ix, d = _g(c["graph"])
+    p = c["p"]
+    n = len(ip) - 1
+    for omega in ((p["omega"],) if p["omega"] == 1.0 else (0.8, p["omega"])):
+        for local in ((True, False) if omega == 1.0 else (False,)):
+            e1, x1, _, o1 = O.hk_sor_queue(n, ip, ix, d, p["s"], p["tau"], p["eps"], omega, local)
+            e2, x2, _, o2 = O.hk_sor_queue(n, ip, ix, d, p["s"], p["tau"], p["eps"], omega, local, sync=True)
+            assert e1 == e2 and o1 == o2
+            np.testing.assert_allclose(x2, x1, rtol=1e-12, atol=1e-16)
+
+
+@pytest.mark.parametrize("c", [c for c in G.cases("hk_sor_queue") if c["p"]["omega"] != 1.0 and c["p"]["local"]],
+                         ids=lambda c: c["id"])
+def test_hk_sync_local_relaxation_keeps_the_heat_kernel_mass(c):
+    """Relaxing each node to its threshold keeps sum(x) near 1 (the heat kernel is
+    column-stochastic) and x near expm; the reference's local queue with omega != 1 leaves
+    part of each (1 - omega) r unpushed."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spla
+    ip, ix, d = _g(c["graph"])
+    p = c["p"]
+    n = len(ip) - 1
+    _, x, _, _ = O.hk_sor_queue(n, ip, ix, d, p["s"], p["tau"], p["eps"], p["omega"], True, sync=True)
+    A = sp.csr_matrix((np.ones(len(ix)), ix, ip), shape=(n, n))
+    Lap = (A @ sp.diags(1.0 / np.asarray(d, np.float64))) - sp.identity(n)
+    e = np.zeros(n)
+    e[p["s"]] = 1.0
+    truth = spla.expm_multiply(p["tau"] * Lap.tocsc(), e)
+    assert abs(x.sum() - 1.0) < 1e-2
+    assert np.abs(x - truth).sum() < 1e-2
+    assert np.abs(c["o"]["x"] - truth).sum() >= np.abs(x - truth).sum() - 1e-12
+
+
 @pytest.mark.parametrize("c", G.cases("hk_taylor_approx"), ids=lambda c: c["id"])
 def test_hk_taylor(c):
     ip, ix, d = _g(c["graph"])
