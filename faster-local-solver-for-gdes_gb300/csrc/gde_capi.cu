@@ -1565,6 +1565,19 @@ int gde_internal_graph_refresh_nodes(gde_ctx* ctx, gde_graph* G, const int64_t* 
     return GDE_OK;
 }
 
+// A padded graph's rows moved to a new layout (gde_graph_repad): the graph
+// takes ownership of row_ptr and col; degrees and node tables are unchanged.
+void gde_internal_graph_relayout(gde_graph* G, int64_t* row_ptr, int32_t* col, int64_t cap, const int64_t* h_indptr) {
+    cudaFree(G->row_ptr);
+    cudaFree(G->col);
+    G->row_ptr = row_ptr;
+    G->col = col;
+    G->g.row_ptr = row_ptr;
+    G->g.col = col;
+    G->g.cap = cap;
+    G->h_indptr.assign(h_indptr, h_indptr + G->g.n + 1);
+}
+
 int gde_internal_graph_host(gde_graph* G, const int64_t** indptr, const int64_t** len, int64_t* n) {
     *indptr = G->h_indptr.data();
     *len = G->h_len.data();

@@ -48,6 +48,7 @@ const double* gde_internal_npush(gde_graph* G);
 const double* gde_internal_degd(gde_graph* G);
 bool gde_internal_relabeled(gde_graph* G);
 int gde_internal_ign_tables(gde_ctx* ctx, gde_graph* G, double beta);
+void gde_internal_graph_relayout(gde_graph* G, int64_t* row_ptr, int32_t* col, int64_t cap, const int64_t* h_indptr);
 
 namespace {
 
@@ -930,6 +931,71 @@ DeviceEdit device_insert(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t
     R.repair_nbr = total;
     return R;
 }
+
+// One warp per row: the live entries to the new place, the slack filled
+// with the sentinel n.
+__global__ void repad_rows_kernel(const int64_t* old_ptr, const int32_t* old_col, const int32_t* row_len,
+                                  const int64_t* new_ptr, int32_t* new_col, int64_t n) {
+    const int lane = threadIdx.x & 31;
+    const int64_t nw = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t u = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5; u < n; u += nw) {
+        const int64_t src = old_ptr[u], dst = new_ptr[u], c = new_ptr[u + 1] - dst;
+        const int len = row_len[u];
+        for (int64_t i = lane; i < c; i += 32) new_col[dst + i] = i < len ? old_col[src + i] : (int32_t)n;
+    }
+}
+
+}  // namespace
+
+extern "C" int gde_graph_repad(gde_ctx* ctx, gde_graph* G, int64_t min_slack, int64_t* indptr_out,
+                               int32_t* indices_out, int64_t* cap_out) {
+    if (!ctx || !G || !cap_out || min_slack < 0) return gde_internal_fail(ctx, GDE_EINVAL, "bad repad arguments");
+    if (gde_internal_relabeled(G))
+        return gde_internal_fail(ctx, GDE_EINVAL, "repad needs a padded CSR graph (upload with row_len)");
+    const int64_t* indptr;
+    const int64_t* hlen;
+    int64_t n;
+    gde_internal_graph_host(G, &indptr, &hlen, &n);
+    std::vector<int64_t> ptr((size_t)n + 1, 0);
+    for (int64_t u = 0; u < n; u++)
+        ptr[(size_t)u + 1] = ptr[(size_t)u] + std::max(indptr[u + 1] - indptr[u], hlen[u] + min_slack);
+    const int64_t cap = ptr[(size_t)n];
+    *cap_out = cap;
+    if (!indices_out) return GDE_OK;
+    if (!indptr_out) return gde_internal_fail(ctx, GDE_EINVAL, "repad: indptr_out is NULL");
+    cudaStream_t st = gde_internal_stream(ctx);
+    int64_t* d_ptr = nullptr;
+    int32_t* d_col = nullptr;
+    if (cudaMalloc(&d_ptr, (size_t)(n + 3) * sizeof(int64_t)) != cudaSuccess ||
+        cudaMalloc(&d_col, (size_t)std::max<int64_t>(cap, 1) * sizeof(int32_t)) != cudaSuccess) {
+        cudaFree(d_ptr);
+        cudaFree(d_col);
+        cudaGetLastError();
+        return gde_internal_fail(ctx, GDE_ENOMEM, "repad: device memory exhausted");
+    }
+    bool ok = cudaMemsetAsync(d_ptr, 0, (size_t)(n + 3) * sizeof(int64_t), st) == cudaSuccess &&
+              cudaMemcpyAsync(d_ptr, ptr.data(), (size_t)(n + 1) * sizeof(int64_t), cudaMemcpyHostToDevice, st) ==
+                  cudaSuccess;
+    if (ok && n > 0) {
+        const int blocks = (int)std::min<int64_t>(8192, (n * 32 + kEdT - 1) / kEdT);
+        repad_rows_kernel<<<blocks, kEdT, 0, st>>>(G->row_ptr, G->col, G->row_len, d_ptr, d_col, n);
+        ok = cudaGetLastError() == cudaSuccess;
+    }
+    if (ok && cap > 0)
+        ok = cudaMemcpyAsync(indices_out, d_col, (size_t)cap * sizeof(int32_t), cudaMemcpyDeviceToHost, st) ==
+             cudaSuccess;
+    if (ok) ok = cudaStreamSynchronize(st) == cudaSuccess;
+    if (!ok) {
+        cudaFree(d_ptr);
+        cudaFree(d_col);
+        return gde_internal_fail(ctx, GDE_ECUDA, "repad: copy of the rows");
+    }
+    std::copy(ptr.begin(), ptr.end(), indptr_out);
+    gde_internal_graph_relayout(G, d_ptr, d_col, cap, ptr.data());
+    return GDE_OK;
+}
+
+namespace {
 
 }  // namespace
 

@@ -60,6 +60,7 @@ SIGNATURES = {
     "gde_serve": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _p, _p, _p, _int, _int, _i64, _p, _p, _p,
                          ctypes.POINTER(Stats)]),
     "gde_hk_estimate_n": (_i64, [_dbl, _dbl]),
+    "gde_graph_repad": (_int, [_p, _p, _i64, _p, _p, _p]),
     "gde_feature_push": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _i64, _dbl, _p, _i64, _p,
                                 ctypes.POINTER(Stats)]),
     "gde_feature_update": (_int, [_p, _p, _p, _p, _p, _p, _i64, _int, ctypes.POINTER(Params), _i64, _p, _p, _p,

@@ -341,6 +341,22 @@ def feature_update(graph: Graph, kind: int, h_indices: np.ndarray, h_degree: np.
     return {"oper": oper, "stats": st.as_dict()}
 
 
+def repad(graph: Graph, min_slack: int) -> tuple[np.ndarray, np.ndarray]:
+    """Re-lay a padded graph with at least ``min_slack`` free slots per row, on the device.
+
+    Returns the new host ``(indptr, indices)``; the caller's degree array stays valid.
+    """
+    lib = L.load()
+    cap = ctypes.c_int64()
+    L.check(graph.ctx.ptr, lib.gde_graph_repad(graph.ctx.ptr, graph.ptr, int(min_slack), None, None,
+                                                ctypes.byref(cap)), "gde_graph_repad")
+    indptr = np.empty(graph.n + 1, dtype=np.int64)
+    indices = np.empty(max(cap.value, 1), dtype=np.int32)[:cap.value]
+    L.check(graph.ctx.ptr, lib.gde_graph_repad(graph.ctx.ptr, graph.ptr, int(min_slack), _ptr(indptr), _ptr(indices),
+                                                ctypes.byref(cap)), "gde_graph_repad")
+    return indptr, indices
+
+
 def plain_ppr_local(graph: Graph, seed: int, alpha: float, eps: float, x_out=None, r_out=None):
     """The plain single-query baseline (structure of ppr_gd_local_gpu)."""
     lib = L.load()

@@ -255,6 +255,19 @@ int gde_feature_update(gde_ctx *ctx, gde_graph *g, int32_t *h_indices, int64_t *
                        const int32_t *vs, int64_t k, int only_insert, const gde_params *p, int64_t F, void *P,
                        void *R, const void *X, int64_t ld, double eps, double *oper_out, gde_stats *stats);
 
+/* Slack management for padded graphs (no counterpart in the reference, whose
+ * padded layout is fixed when data_process_GNN.py:93-171 builds it).  Re-lays
+ * the graph so every row has at least min_slack free slots after its live
+ * entries; rows that already have that much keep their capacity.  Two calls:
+ * with indices_out NULL it only writes the new capacity to *cap_out; then,
+ * with indptr_out[n + 1] and indices_out[*cap_out], it moves the rows on the
+ * device and writes the new host arrays (live entries first, slack filled
+ * with the sentinel n).  Degrees, tables and the node ids are unchanged; the
+ * caller's degree array stays valid.  A row without slack makes
+ * gde_feature_update return GDE_ECAPACITY; this is the way to grow it. */
+int gde_graph_repad(gde_ctx *ctx, gde_graph *g, int64_t min_slack, int64_t *indptr_out, int32_t *indices_out,
+                    int64_t *cap_out);
+
 /* ---- plain single-query baseline ----
  * The structure of ppr_gd_local_gpu (ppr_solver.py:82-146) on this GPU:
  * thread-per-row atomic kernel, O(n) passes and a host sync every round.

@@ -192,3 +192,73 @@ def test_instantgnn_mixed_batch_on_device(algo):
     np.testing.assert_allclose(res["oper"], oo, rtol=1e-12)
     np.testing.assert_allclose(P.cpu().numpy(), Po, rtol=1e-9, atol=1e-13)
     np.testing.assert_allclose(R.cpu().numpy(), Ro, rtol=1e-9, atol=1e-13)
+
+
+def _repad_numpy(ip, ix, dg, min_slack):
+    """The expected relayout: each row's live entries first, capacity max(old, degree + slack)."""
+    n = len(dg)
+    cap = np.maximum(np.diff(ip), dg + min_slack)
+    ip2 = np.zeros(n + 1, np.int64)
+    np.cumsum(cap, out=ip2[1:])
+    ix2 = np.full(ip2[-1], n, np.int32)
+    for u in range(n):
+        ix2[ip2[u]:ip2[u] + dg[u]] = ix[ip[u]:ip[u] + dg[u]]
+    return ip2, ix2
+
+
+def test_repad_grows_the_slack_of_full_rows_and_the_batch_then_runs_on_the_device():
+    """A batch that needs more slack than a row has: GDE_ECAPACITY on the tight layout;
+    after gde_graph_repad the same batch runs on the device and matches the oracle."""
+    import torch
+    g = graphs.chung_lu(2000, 2.2, 6.0, 100.0, seed=41)
+    n = g.n
+    ip, ix, dg = _padded(g, 0)
+    low = int(np.argmin(np.diff(g.indptr)))
+    rng = np.random.default_rng(3)
+    others = rng.choice(np.setdiff1d(np.arange(n), np.concatenate([[low], g.indices[g.indptr[low]:g.indptr[low + 1]]])),
+                        size=5, replace=False)
+    us = np.full(5, low, np.int32)
+    vs = others.astype(np.int32)
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    P = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    R = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    R[int(low), 0] = 0.1
+    ix_before, dg_before = ix.copy(), dg.copy()
+    with pytest.raises(L.GDEError) as ei:
+        api.feature_update(Gd, L.UPPR, ix, dg, us, vs, False, P, R, None, 1e-5, alpha=0.1, prec="fp64", tile_w=1)
+    assert ei.value.status == L.GDE_ECAPACITY
+    # no slack anywhere: the first insertion already failed, nothing changed
+    np.testing.assert_array_equal(ix, ix_before)
+    np.testing.assert_array_equal(dg, dg_before)
+    ip2, ix2 = api.repad(Gd, 8)
+    eip, eix = _repad_numpy(ip, ix, dg, 8)
+    np.testing.assert_array_equal(ip2, eip)
+    np.testing.assert_array_equal(ix2, eix)
+    # the same batch now runs on the device and matches the oracle's sequential pass
+    ix_o, dg_o = ix2.copy(), dg.copy()
+    Po = np.zeros((1, n))
+    Ro = np.ascontiguousarray(R.cpu().numpy().T)
+    oo = O.update_ppr(n, ip2, ix_o, dg_o, 0.1, 1e-5, 1.0, Po, Ro, us, vs, sync=True)
+    res = api.feature_update(Gd, L.UPPR, ix2, dg, us, vs, False, P, R, None, 1e-5, alpha=0.1, prec="fp64", tile_w=1)
+    assert res["stats"]["edit_path"] == EDIT_DEVICE_DATAFLOW
+    np.testing.assert_array_equal(ix2, ix_o)
+    np.testing.assert_array_equal(dg, dg_o)
+    np.testing.assert_allclose(res["oper"], oo, rtol=1e-12)
+    np.testing.assert_allclose(P.cpu().numpy().T, Po, rtol=1e-9, atol=1e-13)
+    np.testing.assert_allclose(R.cpu().numpy().T, Ro, rtol=1e-9, atol=1e-13)
+
+
+def test_repad_keeps_every_solve_the_same():
+    g = graphs.chung_lu(2000, 2.2, 6.0, 100.0, seed=42)
+    ip, ix, dg = _padded(g, 1)
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    seeds = graphs.uniform_seeds(g, 4, seed=1)
+    a = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, 1e-7, prec="fp64", alpha=0.15, tile_w=1)
+    ip2, ix2 = api.repad(Gd, 3)
+    assert ip2[-1] == ip[-1] + 2 * g.n
+    b = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, 1e-7, prec="fp64", alpha=0.15, tile_w=1)
+    np.testing.assert_array_equal(a["oper"], b["oper"])
+    np.testing.assert_allclose(a["x"], b["x"], rtol=1e-12, atol=1e-16)
+    with pytest.raises(L.GDEError) as ei:
+        api.repad(api.Graph(g.indptr, g.indices), 2)  # a static (relabelled) graph has no padded layout
+    assert ei.value.status == L.GDE_EINVAL
