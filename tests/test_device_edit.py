@@ -262,3 +262,53 @@ def test_repad_keeps_every_solve_the_same():
     with pytest.raises(L.GDEError) as ei:
         api.repad(api.Graph(g.indptr, g.indices), 2)  # a static (relabelled) graph has no padded layout
     assert ei.value.status == L.GDE_EINVAL
+
+
+def _tiny_padded(n, edges, slack):
+    a = np.array([e[0] for e in edges] + [e[1] for e in edges], np.int64)
+    b = np.array([e[1] for e in edges] + [e[0] for e in edges], np.int64)
+    order = np.lexsort((b, a))
+    a, b = a[order], b[order]
+    deg = np.bincount(a, minlength=n).astype(np.int64)
+    ip = np.zeros(n + 1, np.int64)
+    np.cumsum(deg + slack, out=ip[1:])
+    ix = np.full(ip[-1], n, np.int32)
+    fill = ip[:-1].copy()
+    for x, y in zip(a, b):
+        ix[fill[x]] = y
+        fill[x] += 1
+    return ip, ix, deg
+
+
+@pytest.mark.parametrize("case", ["leaf_guard", "toggle", "swap_with_last", "star_hub"])
+def test_device_edit_rules_on_tiny_graphs(case):
+    """updetaGraph's rules one by one (InstantGNN.py:147-179), on the device path: the degree-1
+    guard keeps an edge, a pair toggles delete / insert / delete, a deletion moves the row's last
+    entry into the hole, and a hub's row takes a long chain of edits in batch order."""
+    import torch
+    if case == "leaf_guard":       # path 0-1-2-3: (0,1) has a leaf end, (1,2) does not
+        n, edges, us, vs = 4, [(0, 1), (1, 2), (2, 3)], [0, 1, 2], [1, 2, 1]
+    elif case == "toggle":
+        n, edges, us, vs = 5, [(0, 1), (1, 2), (2, 3), (3, 4), (4, 0)], [0, 0, 2, 0, 2], [2, 2, 0, 2, 4]
+    elif case == "swap_with_last":
+        n, edges, us, vs = 6, [(0, 1), (0, 2), (0, 3), (0, 4), (1, 2), (2, 3), (3, 4), (4, 5), (5, 1)], \
+            [0, 0, 3, 0], [1, 3, 2, 5]
+    else:                          # star: centre 0 with 12 leaves, plus a ring on the leaves
+        n = 13
+        edges = [(0, i) for i in range(1, 13)] + [(i, i % 12 + 1) for i in range(1, 13)]
+        rng = np.random.default_rng(5)
+        pairs = [(0, int(v)) for v in rng.integers(1, 13, size=40)]
+        us = [p[0] if i % 2 else p[1] for i, p in enumerate(pairs)]
+        vs = [p[1] if i % 2 else p[0] for i, p in enumerate(pairs)]
+    ip, ix, dg = _tiny_padded(n, edges, 6)
+    us = np.asarray(us, np.int32)
+    vs = np.asarray(vs, np.int32)
+    ix_o, dg_o = ix.copy(), dg.copy()
+    O.update_graph(n, ip, ix_o, dg_o, us, vs, False)
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    P = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    R = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    res = api.feature_update(Gd, L.UPPR, ix, dg, us, vs, False, P, R, None, 1e-3, alpha=0.2, prec="fp64", tile_w=1)
+    assert res["stats"]["edit_path"] == EDIT_DEVICE_DATAFLOW
+    np.testing.assert_array_equal(ix, ix_o)
+    np.testing.assert_array_equal(dg, dg_o)
