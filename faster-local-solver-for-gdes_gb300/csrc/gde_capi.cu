@@ -191,6 +191,18 @@ int alloc_tiles(gde_ctx* ctx, gde_graph* G, int ntiles, int W, int prec64, bool 
         ctx->stamp.assign(ctx->ws["mark"].bytes / 4 / std::max<int64_t>(n, 1) + 1, 0);
     }
     if ((int)ctx->stamp.size() < ntiles) ctx->stamp.resize(ntiles, 0);
+    {
+        // A tile's marks live at mark + t * n, so a graph of another size maps
+        // tile t onto marks another tile wrote.  Every tile therefore starts
+        // past the largest stamp any tile has used (marks are compared for
+        // equality); near the int range the marks are reset instead.
+        int base = *std::max_element(ctx->stamp.begin(), ctx->stamp.end());
+        if (base > (1 << 30)) {
+            CK(cudaMemsetAsync(a.mark, 0xff, ctx->ws["mark"].bytes, ctx->stream));
+            base = 0;
+        }
+        std::fill(ctx->stamp.begin(), ctx->stamp.end(), base);
+    }
     tw.elem = es;
     a.tp = (TileParams*)wsget(ctx, "tp", (size_t)ntiles * sizeof(TileParams));
     a.ts = (TileState*)wsget(ctx, "ts", (size_t)ntiles * sizeof(TileState));
@@ -825,6 +837,7 @@ int gde_serve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
     gde_params pp = *p;
     pp.prec = katz_compute_prec(ctx, G, p);
     p = &pp;
+    if (stats) stats->prec = p->prec;
     return solve_served(ctx, G, p, nq, seeds, eps, arrival_ms, x_out, r_out, out64, out_mem, ld_out, oper_out,
                         rounds_out, lat_ms_out, stats);
 }
@@ -1030,6 +1043,7 @@ int gde_solve(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const
     gde_params pp = *p;
     pp.prec = katz_compute_prec(ctx, G, p);
     p = &pp;
+    if (stats) stats->prec = p->prec;
     const int prec64 = (p->prec == GDE_FP64);
 
     // PPR / Katz local GD with one column per tile runs as a served queue:

@@ -36,7 +36,7 @@ class Stats(ctypes.Structure):
                 ("union_vol", _dbl), ("col_vol", _dbl), ("union_nodes", ctypes.c_uint64),
                 ("col_nodes", ctypes.c_uint64), ("tiles", _int), ("tile_w", _int),
                 ("check_ms", _dbl), ("prep_ms", _dbl), ("scatter_ms", _dbl), ("edit_path", _int),
-                ("edit_ms", _dbl)]
+                ("edit_ms", _dbl), ("prec", _int)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -93,6 +93,8 @@ typedef struct {
     double scatter_ms;
     int edit_path;              /* gde_feature_update: how the edge batch was applied (GDE_EDIT_*) */
     double edit_ms;             /* gde_feature_update: host time from the call to the push (edit + repair) */
+    int prec;                   /* gde_solve / gde_serve: the precision computed in (GDE_FP32 / GDE_FP64);
+                                   Katz near its convergence radius is promoted to FP64 */
 } gde_stats;
 
 /* gde_stats.edit_path */

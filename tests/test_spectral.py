@@ -57,8 +57,13 @@ def test_bounds_drive_katz_cheby():
 
 @pytest.mark.gpu
 def test_katz_near_its_radius_computes_in_fp64():
-    """An FP32 Katz request with alpha * lambda_max >= 0.9 is computed in FP64: its operation
-    counts equal the FP64 solve's exactly (FP32 residuals would flip thresholds)."""
+    """An FP32 Katz request with alpha * lambda_max >= 0.9 is computed in FP64 (gde_stats.prec),
+    and then follows the FP64 solve's trajectory: the same operation counts and solutions.
+
+    Near the radius a trajectory is near-critical: a threshold test that an FP64 rounding of the
+    atomics' order flips can change the rest of the run, so one of the seeds may diverge between
+    two FP64 runs; the others must agree exactly.
+    """
     from gde import _lib as L
     from gde import api, graphs
     g = graphs.chung_lu(3000, 2.1, 8.0, 300.0, seed=12)
@@ -69,12 +74,17 @@ def test_katz_near_its_radius_computes_in_fp64():
     for tile_w in (1, 4):
         r32 = api.solve(Gd, L.KATZ, L.LOCAL_GD, seeds, 1e-6, prec="fp32", alpha=alpha, tile_w=tile_w)
         r64 = api.solve(Gd, L.KATZ, L.LOCAL_GD, seeds, 1e-6, prec="fp64", alpha=alpha, tile_w=tile_w)
-        np.testing.assert_allclose(r32["oper"], r64["oper"], rtol=1e-12)
+        assert r32["stats"]["prec"] == L.FP64 and r64["stats"]["prec"] == L.FP64
         assert r32["x"].dtype == np.float32  # the rows keep the requested format
-        for i in range(len(seeds)):
+        same = r32["oper"] == r64["oper"]
+        assert same.sum() >= len(seeds) - 1, (r32["oper"], r64["oper"])
+        for i in np.nonzero(same)[0]:
             ref = r64["x"][i]
             assert np.abs(r32["x"][i].astype(np.float64) - ref).sum() <= 1e-6 * np.abs(ref).sum()
     # a fresh graph object (no cached estimate) decides the same way, through its own Lanczos run
     G2 = api.Graph(g.indptr, g.indices)
     r = api.solve(G2, L.KATZ, L.LOCAL_GD, seeds, 1e-6, prec="fp32", alpha=alpha, tile_w=1)
-    np.testing.assert_allclose(r["oper"], r64["oper"], rtol=1e-12)
+    assert r["stats"]["prec"] == L.FP64
+    # far from the radius an FP32 request stays in FP32
+    r = api.solve(Gd, L.KATZ, L.LOCAL_GD, seeds, 1e-6, prec="fp32", alpha=0.5 / lam, tile_w=1)
+    assert r["stats"]["prec"] == L.FP32
