@@ -34,5 +34,6 @@ def test_alternating_graph_sizes_keep_exact_operation_counts():
             res = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, eps, prec="fp64", alpha=0.15, tile_w=W)
         deg = g.degree.astype(np.float64)
         for q, s in enumerate(seeds):
-            _, _, oo = O.ppr_gd(g.n, g.indptr, g.indices, deg, int(s), 0.15, eps, True)
+            xo, _, oo = O.ppr_gd(g.n, g.indptr, g.indices, deg, int(s), 0.15, eps, True)
             assert res["oper"][q] == pytest.approx(oo, rel=1e-12), (step, i, W, q)
+            assert np.abs(res["x"][q] - xo).sum() <= 1e-10 * np.abs(xo).sum(), (step, i, W, q)
