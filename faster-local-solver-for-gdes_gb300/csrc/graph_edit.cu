@@ -498,6 +498,9 @@ __global__ void mix_edit_kernel(const int64_t* row_ptr, int32_t* col, int32_t* r
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int e = warp; e < k; e += nwarps) {
         const MixOp op = ops[e];
+        // row starts and ends never change during the batch: load them before the wait
+        const int64_t ru = row_ptr[op.u], ru_end = row_ptr[op.u + 1];
+        const int64_t rv = row_ptr[op.v], rv_end = row_ptr[op.v + 1];
         int go = 1;
         if (lane == 0) {
             int64_t polls = 0;
@@ -516,7 +519,6 @@ __global__ void mix_edit_kernel(const int64_t* row_ptr, int32_t* col, int32_t* r
         }
         if (!__shfl_sync(0xffffffffu, go, 0)) return;
         __threadfence();  // the predecessors' writes before this edge's reads
-        const int64_t ru = row_ptr[op.u], rv = row_ptr[op.v];
         const int du = __ldcg(&row_len[op.u]), dv = __ldcg(&row_len[op.v]);
         // first position of v in u's row (InstantGNN.py:153-155)
         const int found = warp_find_first(col, ru, du, op.v, lane);
@@ -533,7 +535,7 @@ __global__ void mix_edit_kernel(const int64_t* row_ptr, int32_t* col, int32_t* r
                 }
                 oc = MIX_DELETE;
             }
-        } else if (ru + du >= row_ptr[op.u + 1] || rv + dv >= row_ptr[op.v + 1]) {
+        } else if (ru + du >= ru_end || rv + dv >= rv_end) {
             // no slack left for the append: nothing is written, the batch stops
             if (lane == 0) atomicExch(state, 1);
             return;
