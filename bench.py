@@ -54,7 +54,7 @@ def parse():
     ap.add_argument("--tile-w", type=int, default=1, help="1 = served slots (continuous batching)")
     ap.add_argument("--slots", type=int, default=32, help="concurrent queries of the served engine")
     ap.add_argument("--e2e-steps", type=int, default=2)
-    ap.add_argument("--plain-queries", type=int, default=4)
+    ap.add_argument("--plain-queries", type=int, default=32)
     ap.add_argument("--cpu-queries", type=int, default=0, help="CPU-baseline sample (0 = 2 per host thread)")
     ap.add_argument("--no-baselines", action="store_true")
     ap.add_argument("--tuning", default="", help="k=v,... engine tuning overrides")
@@ -90,12 +90,13 @@ class ClockSampler:
     def __init__(self, device: int):
         self.device = device
         self.proc = None
-        self.path = os.path.join(ROOT, "gpurun_out", f"clocks_{os.getpid()}.csv")
+        self.path = None
 
     def __enter__(self):
         try:
-            os.makedirs(os.path.dirname(self.path), exist_ok=True)
-            self.fh = open(self.path, "w")
+            import tempfile
+            self.fh = tempfile.NamedTemporaryFile("w+", prefix="gde_clocks_", suffix=".csv", delete=False)
+            self.path = self.fh.name
             self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
                                           "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.fh,
                                          stderr=subprocess.DEVNULL)
@@ -113,11 +114,14 @@ class ClockSampler:
             self.fh.close()
 
     def summary(self) -> dict:
-        if self.proc is None or not os.path.exists(self.path):
+        if self.proc is None or not self.path or not os.path.exists(self.path):
             return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
         sm, smax, reasons = [], [], set()
         names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
-        for line in open(self.path):
+        with open(self.path) as fh:
+            lines = fh.readlines()
+        os.unlink(self.path)
+        for line in lines:
             f = [x.strip() for x in line.split(",")]
             if len(f) < 9:
                 continue
@@ -230,6 +234,14 @@ def accuracy_vs_truth(G, g, seeds, x_oracle, tuning):
             "max_r_over_d": max(r["max_r_over_d"] for r in rows), "stop_rule": EPS * ALPHA}
 
 
+def c2_config(g, Q, args, world):
+    """The headline workload, named the same in both arms (the reference arm times a sample of it)."""
+    return {"workload": WORKLOAD, "n": g.n, "nnz": g.nnz, "queries_per_step": Q, "alpha": ALPHA, "eps": EPS,
+            "tile_w": args.tile_w, "slots": args.slots,
+            "precision": "fp32 residual, kahan fp32 x, fp64 threshold",
+            "l2": "512 MB buffer written between timed steps", "parallelism": f"replicas x{world}"}
+
+
 def run_reference(args):
     rank, world, _ = dist_env()
     if rank != 0:
@@ -255,10 +267,11 @@ def run_reference(args):
         "metric": METRIC, "value": qps, "unit": "queries/s", "impl": "reference", "n_gpus": 0,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t_total / args.steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": "ppr_local_gd_fp64_cpu_port_chung_lu_2.36M", "queries_per_step": per_step,
-                   "alpha": ALPHA, "eps": EPS, "n": g.n, "nnz": g.nnz},
+        "config": c2_config(g, args.batch, args, 1),
+        "sample_queries_per_step": per_step,
         "cpu_baseline": {"value": qps, "unit": "queries/s", "cores": threads, "kind": "port",
-                         "sample": f"{per_step} queries per step, one per OpenMP thread"},
+                         "sample": f"{per_step} of the workload's queries per step (ppr_gd local FP64, the C port "
+                                   f"of the reference), one per OpenMP thread"},
         "e2e": {"value": qps, "unit": "queries/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
@@ -379,9 +392,7 @@ def run_ours(args):
         "metric": METRIC, "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "n": g.n, "nnz": g.nnz, "queries_per_step": Q, "alpha": ALPHA, "eps": EPS,
-                   "tile_w": args.tile_w, "precision": "fp32 residual, kahan fp32 x, fp64 threshold",
-                   "l2": "512 MB buffer written between timed steps", "parallelism": f"replicas x{world}"},
+        "config": c2_config(g, Q, args, world),
         "p50_ms": float(np.percentile(lat_sorted, 50)) if lat else None,
         "p99_ms": float(np.percentile(lat_sorted, 99)) if lat else None,
         "mean_oper": float(np.mean(opers)) if opers else None,

@@ -211,6 +211,7 @@ int alloc_tiles(gde_ctx* ctx, gde_graph* G, int ntiles, int W, int prec64, bool 
     a.stats = ctx->dstats;
     a.trace = ctx->trace;
     a.trace_iters = ctx->trace ? ctx->trace_iters : 0;
+    a.spin_limit = (unsigned long long)std::max<int64_t>(ctx->wait_limit, 0);
     a.bar = ctx->bar;
     a.err = ctx->derr;
     return GDE_OK;
@@ -259,7 +260,17 @@ int run_engine(gde_ctx* ctx, PushArgs& a, int prec64, int W, gde_stats* st, doub
         st->prep_ms += (double)ctx->hstats->prep_ns * 1e-6;
         st->scatter_ms += (double)ctx->hstats->scatter_ns * 1e-6;
     }
-    if (herr != 0) return fail(ctx, herr, "a device-side wait ran out of iterations (grid barrier)");
+    if (herr != 0) {
+        // The launch stopped part-way: its marks may carry stamps the next
+        // launch would reuse, so every mark starts over (stamps from 0).
+        auto it = ctx->ws.find("mark");
+        if (it != ctx->ws.end() && it->second.p) {
+            CK(cudaMemsetAsync(it->second.p, 0xff, it->second.bytes, ctx->stream));
+            CK(cudaStreamSynchronize(ctx->stream));
+        }
+        std::fill(ctx->stamp.begin(), ctx->stamp.end(), 0);
+        return fail(ctx, herr, "a device-side wait ran out of iterations (grid barrier)");
+    }
     return GDE_OK;
 }
 
@@ -798,6 +809,12 @@ int gde_ctx_trace(gde_ctx* ctx, int iters) {
     }
     CK(cudaMemsetAsync(ctx->trace, 0, bytes, ctx->stream));
     ctx->trace_iters = iters;
+    return GDE_OK;
+}
+
+int gde_ctx_set_wait_limit(gde_ctx* ctx, int64_t polls) {
+    if (!ctx || polls < 0) return fail(ctx, GDE_EINVAL, "bad wait limit");
+    ctx->wait_limit = polls;
     return GDE_OK;
 }
 
@@ -1616,6 +1633,20 @@ const DevGraph* gde_internal_devgraph(gde_graph* G) { return &G->g; }
 int32_t gde_internal_node_in(gde_graph* G, int64_t u) { return G->node_in(u); }
 double gde_internal_host_degree(gde_graph* G, int32_t u) { return G->h_deg[u]; }
 void gde_internal_fill_tuning(const gde_params* p, PushArgs* a) { fill_tuning(p, *a); }
+// katz_compute_prec's rule with nothing that allocates: the degree bound,
+// then a cached spectral estimate; when neither clears FP32, FP64 (the
+// Lanczos estimate gde_solve would compute needs device memory).
+int gde_internal_katz_prec_noalloc(gde_graph* G, const gde_params* p) {
+    if (p->kind != KIND_KATZ || p->prec == GDE_FP64) return p->prec;
+    if (G->dmax < 0.0) {
+        double m = 0.0;
+        for (double d : G->h_deg) m = std::max(m, d);
+        G->dmax = m;
+    }
+    if (p->alpha * G->dmax < kKatzFp64Ratio) return p->prec;
+    if (std::isnan(G->lam_max_est)) return GDE_FP64;
+    return (p->alpha * G->lam_max_est >= kKatzFp64Ratio) ? GDE_FP64 : p->prec;
+}
 int gde_internal_ign_tables(gde_ctx* ctx, gde_graph* G, double beta) {
     if (G->nfac && G->ign_beta == beta) return GDE_OK;
     return upload_ign_tables(ctx, G, beta);

@@ -244,6 +244,7 @@ struct PushArgs {
     ServeQueue queue;
     unsigned long long* trace; // [trace_iters][grid][kTracePoints] %globaltimer stamps (nullptr: off)
     int trace_iters;
+    unsigned long long spin_limit;  // grid-barrier polls before GDE_EHANG (0: the default, ~seconds)
 };
 
 // Phase boundaries stamped per block and launch iteration when tracing is on.

@@ -17,7 +17,9 @@ constexpr unsigned long long kSpinLimit = 1ull << 26;  // ~ seconds of polling
 __device__ __forceinline__ unsigned ld_volatile(const unsigned* p) { return *(volatile const unsigned*)p; }
 __device__ __forceinline__ int ld_volatile_i(const int* p) { return *(volatile const int*)p; }
 
-__device__ __forceinline__ bool grid_barrier(GridBarrier* bar, int* err) {
+// `limit` polls (0: kSpinLimit) before a waiting block gives up.
+__device__ __forceinline__ bool grid_barrier(GridBarrier* bar, int* err, unsigned long long limit = 0) {
+    if (limit == 0) limit = kSpinLimit;
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -33,7 +35,7 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier* bar, int* err) {
             unsigned long long spins = 0;
             while (ld_volatile(&bar->gen) == gen) {
                 if (ld_volatile_i(err) != 0) { ok = 0; break; }
-                if (++spins > kSpinLimit) { atomicCAS(err, 0, GDE_EHANG); ok = 0; break; }
+                if (++spins > limit) { atomicCAS(err, 0, GDE_EHANG); ok = 0; break; }
                 __nanosleep(100);
             }
         }

@@ -38,6 +38,9 @@ struct gde_ctx {
     unsigned long long* trace = nullptr;
     int trace_iters = 0;
     int trace_grid = 0;
+    // bounded device waits: polls before a wait gives up (0: the defaults);
+    // set by gde_ctx_set_wait_limit to exercise the GDE_EHANG paths
+    int64_t wait_limit = 0;
 };
 
 struct gde_graph {

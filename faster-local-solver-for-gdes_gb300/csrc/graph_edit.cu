@@ -7,12 +7,18 @@
 // GPU (InstantGNN.py:303-318 for InstantGNN, ppr_solver.py:776-792 for the
 // beta = 0 PPR update); (3) push from the repaired nodes with the engine.
 //
-// Insert-only batches without self-loops are applied on the device
-// (device_insert below): which edges are inserted and where every new entry
-// lands are decided in parallel with exactly the sequential semantics, and
-// the caller's host arrays receive the same values afterwards.  Deletions
-// keep a short sequential pass on the host (O(sum of scanned row lengths)),
-// whose effect on the device graph is uploaded as (position, value) entries
+// Batches run on the device: insert-only batches (device_insert) decide in
+// parallel which edges are inserted and where every new entry lands, with
+// exactly the sequential semantics; batches with deletions
+// (device_mixed_edit) run as a dataflow over the edges in which each edge
+// waits (bounded) on the previous edge of each endpoint.  The caller's host
+// arrays receive the same values afterwards.  Three cases keep a sequential
+// pass on the host, on purpose: a batch with a self-loop (the reference
+// writes both endpoints' appends into one slot and counts two degrees, a
+// quirk not worth a device path), a graph whose degree array is not its row
+// length, and a batch that fills a row (the host pass then reproduces the
+// reference's partial edit before GDE_ECAPACITY is returned).  The host
+// pass's effect on the device graph is uploaded as (position, value) entries
 // plus the new degree tables.
 #include <cuda_runtime.h>
 
@@ -637,7 +643,7 @@ struct DeviceEdit {
 };
 
 DeviceEdit device_mixed_edit(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree, const int32_t* us,
-                             const int32_t* vs, int64_t k, int kind, double beta) {
+                             const int32_t* vs, int64_t k, int kind, double beta, uint8_t* outcome) {
     DeviceEdit M;
     const int64_t n = G->g.n;
     const int64_t* indptr;
@@ -699,6 +705,7 @@ DeviceEdit device_mixed_edit(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int
     int ki = (int)k;
     // a wait is bounded by the whole batch running in sequence (>= 1 us a poll)
     int64_t poll_limit = std::max<int64_t>((int64_t)1 << 22, 64 * k);
+    if (ctx->wait_limit > 0) poll_limit = ctx->wait_limit;
     int* err = ctx->derr;
     void* args[] = {(void*)&row_ptr, (void*)&col,    (void*)&rl,     (void*)&d_ops,   (void*)&ki,
                     (void*)&d_done,  (void*)&d_out,  (void*)&d_icnt, (void*)&d_dcnt,  (void*)&d_rank,
@@ -708,6 +715,7 @@ DeviceEdit device_mixed_edit(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int
     int herr = 0, hfull = 0;
     ck(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st), "edit status");
     ck(cudaMemcpyAsync(&hfull, d_state, 4, cudaMemcpyDeviceToHost, st), "edit status");
+    if (outcome) ck(cudaMemcpyAsync(outcome, d_out, (size_t)k, cudaMemcpyDeviceToHost, st), "edit outcomes");
     ck(cudaStreamSynchronize(st), "edit kernel");
     if (M.status != GDE_OK) return M;
     if (herr != 0 || hfull != 0) {
@@ -820,7 +828,7 @@ DeviceEdit device_mixed_edit(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int
 }
 
 DeviceEdit device_insert(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree, const int32_t* us,
-                           const int32_t* vs, int64_t k, int kind, double beta) {
+                           const int32_t* vs, int64_t k, int kind, double beta, uint8_t* outcome) {
     DeviceEdit R;
     const int64_t n = G->g.n;
     cudaStream_t st = gde_internal_stream(ctx);
@@ -913,11 +921,15 @@ DeviceEdit device_insert(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t
     std::vector<int64_t> hpos(total);
     std::vector<int32_t> hval(total);
     std::vector<int> hcnt(n);
+    if (outcome) DI_CK(cudaMemcpyAsync(outcome, d_state, (size_t)k, cudaMemcpyDeviceToHost, st));
     DI_CK(cudaMemcpyAsync(hpos.data(), d_pos, (size_t)total * 8, cudaMemcpyDeviceToHost, st));
     DI_CK(cudaMemcpyAsync(hval.data(), d_nbr, (size_t)total * 4, cudaMemcpyDeviceToHost, st));
     DI_CK(cudaMemcpyAsync(hcnt.data(), d_cnt, n * 4, cudaMemcpyDeviceToHost, st));
     DI_CK(cudaStreamSynchronize(st));
 #undef DI_CK
+    // insert states: 2 inserted; 0 present already and 1 a repeat, both skipped
+    if (outcome)
+        for (int64_t e = 0; e < k; e++) outcome[e] = outcome[e] == 2 ? MIX_INSERT : MIX_NOOP;
     for (int i = 0; i < total; i++) h_indices[hpos[i]] = hval[i];
     for (int64_t w = 0; w < n; w++) {
         if (!hcnt[w]) continue;
@@ -1001,10 +1013,12 @@ namespace {
 
 }  // namespace
 
-extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree,
-                                  const int32_t* us, const int32_t* vs, int64_t k, int only_insert,
-                                  const gde_params* p, int64_t F, void* Pm, void* Rm, const void* Xm, int64_t ld,
-                                  double eps, double* oper_out, gde_stats* stats) {
+// The edge batch, then (unless edit_only) the repair and the push.
+// outcome (host, may be null): per edge MIX_NOOP / MIX_INSERT / MIX_DELETE.
+static int feature_update_impl(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree,
+                               const int32_t* us, const int32_t* vs, int64_t k, int only_insert,
+                               const gde_params* p, int64_t F, void* Pm, void* Rm, const void* Xm, int64_t ld,
+                               double eps, double* oper_out, gde_stats* stats, uint8_t* outcome, bool edit_only) {
     const auto t_entry = std::chrono::steady_clock::now();
     auto since_entry = [&]() {
         return std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t_entry).count();
@@ -1013,7 +1027,8 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
         return gde_internal_fail(ctx, GDE_EINVAL, "bad update arguments");
     const int kind = p->kind;
     if (kind != KIND_IGN && kind != KIND_UPPR) return gde_internal_fail(ctx, GDE_EINVAL, "kind must be IGN or UPPR");
-    if (kind == KIND_IGN && !Xm) return gde_internal_fail(ctx, GDE_EINVAL, "InstantGNN repair needs X");
+    if (kind == KIND_IGN && !Xm && !edit_only) return gde_internal_fail(ctx, GDE_EINVAL, "InstantGNN repair needs X");
+    if (outcome && k > 0) memset(outcome, MIX_NOOP, (size_t)k);
     if (gde_internal_relabeled(G))
         return gde_internal_fail(ctx, GDE_EINVAL, "edge updates need a padded CSR graph (upload with row_len)");
     const int64_t* indptr;
@@ -1039,12 +1054,20 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
             if (rc0 == GDE_OK) rc0 = ensure_power_tables(ctx, G, p->beta);
             if (rc0 != GDE_OK) return rc0;
         }
-        DeviceEdit D = only_insert ? device_insert(ctx, G, h_indices, h_degree, us, vs, k, kind, p->beta)
-                                   : device_mixed_edit(ctx, G, h_indices, h_degree, us, vs, k, kind, p->beta);
+        DeviceEdit D = only_insert ? device_insert(ctx, G, h_indices, h_degree, us, vs, k, kind, p->beta, outcome)
+                                   : device_mixed_edit(ctx, G, h_indices, h_degree, us, vs, k, kind, p->beta, outcome);
         if (D.status != GDE_OK) return D.status;
         // InstantGNN tables built for an earlier call are not updated by this
         // kind's edit: the next InstantGNN call rebuilds them
         if (kind != KIND_IGN) G->ign_beta = NAN;
+        if (!D.fallback && edit_only) {
+            if (stats) {
+                memset(stats, 0, sizeof(*stats));
+                stats->edit_path = only_insert ? GDE_EDIT_DEVICE_INSERT : GDE_EDIT_DEVICE_DATAFLOW;
+                stats->edit_ms = since_entry();
+            }
+            return GDE_OK;
+        }
         if (!D.fallback) {
             cudaStream_t st = gde_internal_stream(ctx);
             const int prec64 = (p->prec == GDE_FP64);
@@ -1114,6 +1137,7 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
                 h_degree[v] -= 1;
                 del.add(u, v);
                 del.add(v, u);
+                if (outcome) outcome[e] = MIX_DELETE;
                 break;
             }
         }
@@ -1132,6 +1156,7 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
             h_degree[v] += 1;
             ins.add(u, v);
             ins.add(v, u);
+            if (outcome) outcome[e] = MIX_INSERT;
         }
     }
     // A slot can be written more than once (swap-with-last deletions); the
@@ -1153,6 +1178,14 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
     if (status != GDE_OK)
         return gde_internal_fail(ctx, status, status == GDE_ECAPACITY ? "padded row has no slack for an insertion"
                                                                       : "edge endpoint out of range");
+    if (edit_only) {
+        if (stats) {
+            memset(stats, 0, sizeof(*stats));
+            stats->edit_path = GDE_EDIT_HOST;
+            stats->edit_ms = since_entry();
+        }
+        return GDE_OK;
+    }
     // ---- (2) repair at the touched nodes ----
     std::vector<RepairKey> keys;
     std::vector<int32_t> nbr;
@@ -1234,5 +1267,98 @@ extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices
         stats->edit_path = GDE_EDIT_HOST;
         stats->edit_ms = edit_ms;
     }
+    return GDE_OK;
+}
+
+extern "C" int gde_feature_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree,
+                                  const int32_t* us, const int32_t* vs, int64_t k, int only_insert,
+                                  const gde_params* p, int64_t F, void* Pm, void* Rm, const void* Xm, int64_t ld,
+                                  double eps, double* oper_out, gde_stats* stats) {
+    return feature_update_impl(ctx, G, h_indices, h_degree, us, vs, k, only_insert, p, F, Pm, Rm, Xm, ld, eps,
+                               oper_out, stats, nullptr, false);
+}
+
+extern "C" int gde_graph_update(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree, const int32_t* us,
+                                const int32_t* vs, int64_t k, int only_insert, uint8_t* outcome, gde_stats* stats) {
+    gde_params p;
+    memset(&p, 0, sizeof p);
+    p.kind = KIND_UPPR;  // no feature tables to keep up to date
+    p.prec = GDE_FP64;
+    return feature_update_impl(ctx, G, h_indices, h_degree, us, vs, k, only_insert, &p, 0, nullptr, nullptr, nullptr,
+                               0, 0.0, nullptr, stats, outcome, true);
+}
+
+extern "C" int gde_feature_repair(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t F, void* Pm, void* Rm,
+                                  const void* Xm, int64_t ld, int64_t nkeys, const int32_t* keys,
+                                  const int64_t* old_degree, const int64_t* nbr_off, const int32_t* nbr) {
+    if (!ctx || !G || !p || F < 0 || nkeys < 0 || (nkeys > 0 && (!keys || !old_degree || !nbr_off)))
+        return gde_internal_fail(ctx, GDE_EINVAL, "bad repair arguments");
+    const int kind = p->kind;
+    if (kind != KIND_IGN && kind != KIND_UPPR) return gde_internal_fail(ctx, GDE_EINVAL, "kind must be IGN or UPPR");
+    if (kind == KIND_IGN && !Xm) return gde_internal_fail(ctx, GDE_EINVAL, "InstantGNN repair needs X");
+    if (nkeys == 0 || F == 0) return GDE_OK;
+    if (nkeys >= ((int64_t)1 << 31) || nbr_off[2 * nkeys] >= ((int64_t)1 << 31))
+        return gde_internal_fail(ctx, GDE_EINVAL, "repair lists too long");
+    const int64_t* indptr;
+    const int64_t* hlen;
+    int64_t n;
+    gde_internal_graph_host(G, &indptr, &hlen, &n);
+    if (kind == KIND_IGN) {
+        int rc0 = gde_internal_ign_tables(ctx, G, p->beta);
+        if (rc0 != GDE_OK) return rc0;
+    }
+    // factors in the reference's operation order (InstantGNN.py:303-314,
+    // ppr_solver.py:776-792), degrees after the batch from the resident graph
+    std::vector<RepairKey> rk((size_t)nkeys);
+    for (int64_t i = 0; i < nkeys; i++) {
+        const int32_t u = keys[i];
+        if (u < 0 || u >= n || !(old_degree[i] > 0)) return gde_internal_fail(ctx, GDE_EINVAL, "bad repair key");
+        RepairKey& K = rk[(size_t)i];
+        memset(&K, 0, sizeof K);
+        K.u = u;
+        const double d = (double)hlen[u], od = (double)old_degree[i];
+        if (kind == KIND_IGN) {
+            const double b = p->beta;
+            K.a1 = std::pow(d / od, 1 - b);
+            K.a2 = std::pow(od, 1 - b);
+            K.a3 = std::pow(d, 1 - b);
+            K.b1 = std::pow(od, b);
+            K.b2 = std::pow(d, b);
+        } else {
+            K.a1 = d;
+            K.a2 = od;
+        }
+        K.ins_beg = (int32_t)nbr_off[2 * i];
+        K.ins_end = (int32_t)nbr_off[2 * i + 1];
+        K.del_beg = K.ins_end;
+        K.del_end = (int32_t)nbr_off[2 * i + 2];
+    }
+    const int64_t total = nbr_off[2 * nkeys];
+    for (int64_t j = 0; j < total; j++)
+        if (nbr[j] < 0 || nbr[j] >= n) return gde_internal_fail(ctx, GDE_EINVAL, "repair neighbour out of range");
+    cudaStream_t st = gde_internal_stream(ctx);
+    RepairKey* d_keys = (RepairKey*)gde_internal_wsget(ctx, "repair_keys", rk.size() * sizeof(RepairKey));
+    int32_t* d_nbr = (int32_t*)gde_internal_wsget(ctx, "repair_nbr", (size_t)std::max<int64_t>(total, 1) * 4);
+    if (!d_keys || !d_nbr) return gde_internal_fail(ctx, GDE_ENOMEM, "repair tables");
+    if (cudaMemcpyAsync(d_keys, rk.data(), rk.size() * sizeof(RepairKey), cudaMemcpyHostToDevice, st) != cudaSuccess ||
+        (total > 0 && cudaMemcpyAsync(d_nbr, nbr, (size_t)total * 4, cudaMemcpyHostToDevice, st) != cudaSuccess))
+        return gde_internal_fail(ctx, GDE_ECUDA, "repair upload");
+    const int blocks = (int)((nkeys * F + 255) / 256);
+    if (p->prec == GDE_FP64) {
+        repair_pass1<double><<<blocks, 256, 0, st>>>(d_keys, (int)nkeys, (double*)Pm, (double*)Rm, ld, F, kind,
+                                                      p->alpha);
+        repair_pass2<double><<<blocks, 256, 0, st>>>(d_keys, (int)nkeys, d_nbr, (const double*)Pm, (double*)Rm,
+                                                      (const double*)Xm, ld, F, kind, p->alpha,
+                                                      gde_internal_npush(G), gde_internal_degd(G));
+    } else {
+        repair_pass1<float><<<blocks, 256, 0, st>>>(d_keys, (int)nkeys, (float*)Pm, (float*)Rm, ld, F, kind,
+                                                     p->alpha);
+        repair_pass2<float><<<blocks, 256, 0, st>>>(d_keys, (int)nkeys, d_nbr, (const float*)Pm, (float*)Rm,
+                                                     (const float*)Xm, ld, F, kind, p->alpha, gde_internal_npush(G),
+                                                     gde_internal_degd(G));
+    }
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return gde_internal_fail(ctx, GDE_ECUDA, cudaGetErrorString(e));
     return GDE_OK;
 }

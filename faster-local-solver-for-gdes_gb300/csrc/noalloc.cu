@@ -22,9 +22,21 @@
 //  * Every call on a device shares the one array.  Calls whose GPU work
 //    overlaps (other streams, other contexts on the same device, other host
 //    threads) race on it and corrupt each other's results: serialise them.
-//  * The first call on each device looks the array up
-//    (cudaGetSymbolAddress, with that device current) and caches its
-//    address.  Make that first call before any stream capture begins.
+//  * The array's name in host code is a host-side stand-in, not a device
+//    address.  Every call looks the device address up with
+//    cudaGetSymbolAddress, with the context's device current, and passes it
+//    to the kernels; the first call on a device also loads the module there,
+//    so make that first call before any stream capture begins.  (Looking the
+//    address up on every call, rather than caching it, stays correct after
+//    the host application resets the device and the module reloads.)
+//  * Every device that loads the library holds the 64 MiB array until the
+//    process exits, whether or not this entry point is ever called.
+//  * Katz keeps gde_solve's precision rule: near its convergence radius
+//    (alpha * lambda_max >= 0.9) an FP32 request computes in FP64.  The
+//    largest degree settles most calls; otherwise a cached spectral estimate
+//    of the graph decides (gde_katz_spectral_bounds, or an earlier gde_solve
+//    of such a query, computes one).  With no estimate cached the call
+//    computes in FP64, since the estimate itself needs device memory.
 //  * Outputs are device pointers (x_out / r_out: n entries in caller node
 //    order, FP64 when out64 else FP32); the small per-call records are copied
 //    with cudaMemcpyAsync from / to host stack memory, and the call returns
@@ -35,7 +47,6 @@
 #include <cmath>
 #include <cstdio>
 #include <cstring>
-#include <mutex>
 #include <string>
 
 #include "gde_common.cuh"
@@ -52,32 +63,24 @@ const DevGraph* gde_internal_devgraph(gde_graph* G);
 int32_t gde_internal_node_in(gde_graph* G, int64_t u);
 double gde_internal_host_degree(gde_graph* G, int32_t u);
 void gde_internal_fill_tuning(const gde_params* p, PushArgs* a);
+int gde_internal_katz_prec_noalloc(gde_graph* G, const gde_params* p);
 
 namespace {
 
 constexpr size_t kNoAllocScratchBytes = (size_t)64 << 20;  // 64 MiB
 constexpr size_t kAlign = 256;
-constexpr int kMaxDevices = 64;
 
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-std::mutex g_setup_mu;
-void* g_scratch_ptr[kMaxDevices] = {};
-
-// Address of the array on `device` (current).  Looked up once per device.
-int scratch_for_device(gde_ctx* ctx, int device, unsigned char** out) {
-    if (device < 0 || device >= kMaxDevices) return gde_internal_fail(ctx, GDE_EINVAL, "device ordinal out of range");
-    std::lock_guard<std::mutex> lk(g_setup_mu);
-    if (!g_scratch_ptr[device]) {
-        void* p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            std::string m = std::string("cudaGetSymbolAddress of the fixed scratch array: ") + cudaGetErrorString(e);
-            return gde_internal_fail(ctx, GDE_ECUDA, m.c_str());
-        }
-        g_scratch_ptr[device] = p;
+// Device address of the array on the current device.
+int scratch_address(gde_ctx* ctx, unsigned char** out) {
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        std::string m = std::string("cudaGetSymbolAddress of the fixed scratch array: ") + cudaGetErrorString(e);
+        return gde_internal_fail(ctx, GDE_ECUDA, m.c_str());
     }
-    *out = (unsigned char*)g_scratch_ptr[device];
+    *out = (unsigned char*)p;
     return GDE_OK;
 }
 
@@ -116,7 +119,7 @@ extern "C" int gde_solve_noalloc(gde_ctx* ctx, gde_graph* G, const gde_params* p
     const int32_t s_in = gde_internal_node_in(G, seed);
     if (kind == KIND_PPR && !(eps * gde_internal_host_degree(G, s_in) <= 1.))
         return gde_internal_fail(ctx, GDE_EINVAL, "eps * degree[s_node] > 1 (ppr_solver.py:213)");
-    const int prec64 = (p->prec == GDE_FP64);
+    const int prec64 = (gde_internal_katz_prec_noalloc(G, p) == GDE_FP64);
     const size_t es = prec64 ? 8 : 4;
 
     PushArgs a{};
@@ -144,7 +147,7 @@ extern "C" int gde_solve_noalloc(gde_ctx* ctx, gde_graph* G, const gde_params* p
     const int device = gde_internal_device(ctx);
     NA_CK(cudaSetDevice(device));
     unsigned char* base = nullptr;
-    int rc = scratch_for_device(ctx, device, &base);
+    int rc = scratch_address(ctx, &base);
     if (rc != GDE_OK) return rc;
     cudaStream_t st = gde_internal_stream(ctx);
 
@@ -171,6 +174,7 @@ extern "C" int gde_solve_noalloc(gde_ctx* ctx, gde_graph* G, const gde_params* p
     a.stats = (LaunchStats*)(base + oSt);
     a.serve = 0;
     a.round_budget = a.max_rounds + 1;
+    a.spin_limit = 0;
 
     // ---- what must start at zero (or at the "untouched" mark -1) ----
     NA_CK(cudaMemsetAsync(a.R, 0, n * es, st));

@@ -1673,7 +1673,7 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
                 if (m != M_GLOBAL_GD && m != M_GLOBAL_CHEBY) continue;
                 check_phase<T, W>(a, t, it, s_cnt);
             }
-            if (!grid_barrier(a.bar, a.err)) return;
+            if (!grid_barrier(a.bar, a.err, a.spin_limit)) return;
             if (timer) {
                 unsigned long long t1 = globaltimer_ns();
                 a.stats->check_ns += t1 - t0;
@@ -1706,7 +1706,7 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
             }
         }
         trace_point(a, it, TP_PREP_DONE);
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, a.spin_limit)) return;
         trace_point(a, it, TP_PREP_BAR);
         if (timer) {
             unsigned long long t1 = globaltimer_ns();
@@ -1821,7 +1821,7 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
             }
         }
         trace_point(a, it, TP_SCAT_ENTER);
-        if (!grid_barrier(a.bar, a.err)) return;
+        if (!grid_barrier(a.bar, a.err, a.spin_limit)) return;
         trace_point(a, it, TP_SCAT_BAR);
         if (timer) a.stats->scatter_ns += globaltimer_ns() - t0;
     }

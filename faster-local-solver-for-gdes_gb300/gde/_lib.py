@@ -61,6 +61,8 @@ SIGNATURES = {
                          ctypes.POINTER(Stats)]),
     "gde_hk_estimate_n": (_i64, [_dbl, _dbl]),
     "gde_graph_repad": (_int, [_p, _p, _i64, _p, _p, _p]),
+    "gde_graph_update": (_int, [_p, _p, _p, _p, _p, _p, _i64, _int, _p, ctypes.POINTER(Stats)]),
+    "gde_feature_repair": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _p, _i64, _i64, _p, _p, _p, _p]),
     "gde_feature_push": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _p, _p, _i64, _dbl, _p, _i64, _p,
                                 ctypes.POINTER(Stats)]),
     "gde_feature_update": (_int, [_p, _p, _p, _p, _p, _p, _i64, _int, ctypes.POINTER(Params), _i64, _p, _p, _p,
@@ -74,6 +76,7 @@ SIGNATURES = {
     "gde_katz_spectral_bounds": (_int, [_p, _p, _dbl, _int, _dbl, _p, _p, _p, _p]),
     "gde_ctx_trace": (_int, [_p, _int]),
     "gde_ctx_trace_read": (_int, [_p, _p, _i64, _p, _p, _p]),
+    "gde_ctx_set_wait_limit": (_int, [_p, _i64]),
     "gde_solve_noalloc": (_int, [_p, _p, ctypes.POINTER(Params), _i32, _dbl, _p, _p, _int, _p, _p]),
 }
 

@@ -278,6 +278,12 @@ def ctx_stream(ctx: Context | None = None) -> int:
     return int(L.load().gde_ctx_stream(c.ptr) or 0)
 
 
+def set_wait_limit(polls: int, ctx: Context | None = None) -> None:
+    """Polls before a bounded device wait gives up with GDE_EHANG (0: the library's defaults)."""
+    c = ctx or Context.get(0)
+    L.check(c.ptr, L.load().gde_ctx_set_wait_limit(c.ptr, int(polls)), "gde_ctx_set_wait_limit")
+
+
 def trace(iters: int, ctx: Context | None = None) -> None:
     """Record per-block phase stamps for the first ``iters`` iterations of later push launches (0 = off)."""
     c = ctx or Context.get(0)
@@ -339,6 +345,41 @@ def feature_update(graph: Graph, kind: int, h_indices: np.ndarray, h_degree: np.
                                     eps, _ptr(oper), ctypes.byref(st))
     L.check(graph.ctx.ptr, status, "gde_feature_update")
     return {"oper": oper, "stats": st.as_dict()}
+
+
+def graph_update(graph: Graph, h_indices: np.ndarray, h_degree: np.ndarray, us, vs, only_insert: bool) -> dict:
+    """The edge batch alone on the padded CSR (updetaGraph semantics); host arrays mutated in place.
+
+    Returns dict(outcome, stats): outcome[i] = 0 no change, 1 inserted, 2 deleted.
+    """
+    lib = L.load()
+    assert h_indices.dtype == np.int32 and h_degree.dtype == np.int64
+    assert h_indices.flags.c_contiguous and h_degree.flags.c_contiguous
+    us = np.ascontiguousarray(us, dtype=np.int32)
+    vs = np.ascontiguousarray(vs, dtype=np.int32)
+    outcome = np.zeros(us.shape[0], dtype=np.uint8)
+    st = L.Stats()
+    status = lib.gde_graph_update(graph.ctx.ptr, graph.ptr, _ptr(h_indices), _ptr(h_degree), _ptr(us), _ptr(vs),
+                                  us.shape[0], int(only_insert), _ptr(outcome), ctypes.byref(st))
+    L.check(graph.ctx.ptr, status, "gde_graph_update")
+    return {"outcome": outcome, "stats": st.as_dict()}
+
+
+def feature_repair(graph: Graph, kind: int, P, R, X, keys, old_degree, nbr_off, nbr, *, alpha: float,
+                   beta: float = 0.0, prec: str = "fp64") -> None:
+    """Repair device matrices P, R ([n, F]) at the keys after an edge batch (instantGNNUpdateBatch / update_ppr)."""
+    lib = L.load()
+    F = int(P.shape[1])
+    ld = int(P.stride(0))
+    keys = np.ascontiguousarray(keys, dtype=np.int32)
+    old_degree = np.ascontiguousarray(old_degree, dtype=np.int64)
+    nbr_off = np.ascontiguousarray(nbr_off, dtype=np.int64)
+    nbr = np.ascontiguousarray(nbr, dtype=np.int32)
+    p = make_params(kind, L.LOCAL_GD, prec, 0, alpha=alpha, beta=beta)
+    status = lib.gde_feature_repair(graph.ctx.ptr, graph.ptr, ctypes.byref(p), F, _ptr(P), _ptr(R), _ptr(X), ld,
+                                    keys.shape[0], _ptr(keys), _ptr(old_degree), _ptr(nbr_off),
+                                    _ptr(nbr) if nbr.size else None)
+    L.check(graph.ctx.ptr, status, "gde_feature_repair")
 
 
 def repad(graph: Graph, min_slack: int) -> tuple[np.ndarray, np.ndarray]:

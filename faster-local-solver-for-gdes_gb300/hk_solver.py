@@ -19,7 +19,8 @@ from gde import _lib as L
 from gde import api
 from gde.dropin import Timer, graph_for
 
-__all__ = ["estimate_coefficient", "estimate_n", "hk_taylor_approx", "hk_sor_queue", "solve_a_graph_all"]
+__all__ = ["estimate_coefficient", "estimate_n", "hk_taylor_approx", "hk_sor_queue", "solve_a_graph_all",
+           "solve_a_graph_pk"]
 
 
 def estimate_coefficient(t, k):
@@ -68,19 +69,36 @@ def hk_sor_queue(n, indptr, indices, degree, s_node, tau, eps, omega, local):
     return est_n, r["x"][0], r["r"][0], float(r["oper"][0]), [], t.dt, t.dt
 
 
-def solve_a_graph_all(n, indptr, indices, degree, tau, eps, omega, graph_name, s_nodes):
-    """(hk_solver.py:303-366): local and global SOR with ``omega``, then the omega = 1 ("ahk") pair.
+def _batch(n, indptr, indices, degree, s_nodes, tau, eps, omega, local, device_x=False):
+    g = graph_for(indptr, indices, degree)
+    assert g.n == n, "n must equal len(indptr) - 1"
+    seeds = np.ascontiguousarray(np.asarray(s_nodes).ravel(), dtype=np.int32)
+    with Timer() as t:
+        r = api.solve(g, L.HK, L.HK_LOCAL if local else L.HK_GLOBAL, seeds, eps, prec="fp64", tau=tau,
+                      omega=float(omega), want_x=device_x, want_r=False, device_out=device_x)
+    return r, np.full(len(seeds), t.dt / max(len(seeds), 1))
 
-    The Taylor and relax entries stay zero, as the reference leaves them.
+
+def solve_a_graph_all(n, indptr, indices, degree, tau, eps, omega, graph_name, s_nodes):
+    """(hk_solver.py:303-366): local and global SOR with ``omega``, then the omega = 1 ("ahk") pair, each
+    over all seeds in one batched call.  The Taylor and relax entries stay zero, as the reference leaves them.
     """
     test_num = len(s_nodes)
     z = lambda: np.zeros(test_num, dtype=np.int64)  # noqa: E731
     zt = lambda: np.zeros(test_num)  # noqa: E731
     out = []
     for om, local in ((omega, True), (omega, False), (1.0, True), (1.0, False)):
-        o, t = z(), zt()
-        for ii in range(test_num):
-            res = hk_sor_queue(n, indptr, indices, degree, int(s_nodes[ii]), tau, eps, om, local)
-            o[ii], t[ii] = res[3], res[6]
-        out += [o, t]
+        r, t = _batch(n, indptr, indices, degree, s_nodes, tau, eps, om, local)
+        out += [np.rint(r["oper"]).astype(np.int64), t]
     return (s_nodes, *out, z(), zt(), z(), zt())
+
+
+def solve_a_graph_pk(n, indptr, indices, degree, tau, eps, omega, graph_name, s_nodes):
+    """Global level push (omega = 1) over s_nodes with each solution's participation ratio
+    pk = (sum (n x)^2)^2 / sum (n x)^4 (hk_solver.py:369-393) -> (opers, algo_times, pk, est_ns)."""
+    r, t = _batch(n, indptr, indices, degree, s_nodes, tau, eps, 1.0, False, device_x=True)
+    xn = r["x"].double() * n
+    sq = xn * xn
+    pk = ((sq.sum(1) ** 2) / (sq * sq).sum(1)).cpu().numpy()
+    est = np.full(len(s_nodes), float(estimate_n(tau, .5 * eps)))
+    return np.asarray(r["oper"], dtype=np.float64), t, pk, est

@@ -98,7 +98,8 @@ typedef struct {
 } gde_stats;
 
 /* gde_stats.edit_path */
-#define GDE_EDIT_HOST 0             /* sequential host pass (self-loops, no slack to spare, relabelled) */
+#define GDE_EDIT_HOST 0             /* sequential host pass (a self-loop, a degree array that is not the row
+                                       length, or a row without slack for an insertion) */
 #define GDE_EDIT_DEVICE_INSERT 1    /* insert-only batch on the device */
 #define GDE_EDIT_DEVICE_DATAFLOW 2  /* batch with deletions on the device, as a dataflow over the edges */
 
@@ -122,6 +123,17 @@ int gde_ctx_sync(gde_ctx *ctx);
  * the shape; call it with out == NULL to get the shape only. */
 int gde_ctx_trace(gde_ctx *ctx, int iters);
 int gde_ctx_trace_read(gde_ctx *ctx, uint64_t *out, int64_t cap, int *iters, int *grid, int *points);
+
+/* ---- bounded device waits (failure detection; no counterpart in the reference) ----
+ * Every device-side wait of the library is bounded: the push kernel's grid
+ * barrier and the edit dataflow's predecessor waits give up after a number of
+ * polls, record GDE_EHANG and return, so a wait that cannot end leaves a
+ * usable context and an error status instead of a hung GPU.  The defaults are
+ * seconds of polling.  gde_ctx_set_wait_limit(ctx, polls) sets the limit of
+ * every later wait on this context (0 restores the defaults); a limit of one
+ * or two polls makes the waits run out, which is how the GDE_EHANG paths are
+ * tested. */
+int gde_ctx_set_wait_limit(gde_ctx *ctx, int64_t polls);
 
 /* ---- graph ----
  * Uploads a CSR graph.  Row u's neighbours are indices[indptr[u] ..
@@ -256,6 +268,35 @@ int gde_feature_push(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t F,
 int gde_feature_update(gde_ctx *ctx, gde_graph *g, int32_t *h_indices, int64_t *h_degree, const int32_t *us,
                        const int32_t *vs, int64_t k, int only_insert, const gde_params *p, int64_t F, void *P,
                        void *R, const void *X, int64_t ld, double eps, double *oper_out, gde_stats *stats);
+
+/* ---- padded-CSR edge batch alone (updetaGraph / updeta_graph) ----
+ * Applies the batch (us[i], vs[i]) exactly as updetaGraph (InstantGNN.py:137-180)
+ * and updeta_graph (ppr_solver.py:723-766) do -- the edit gde_feature_update
+ * starts with, on the device, without a repair or push -- mutating the
+ * caller's host arrays h_indices / h_degree and the resident graph.
+ * outcome (host, may be NULL): k bytes, per edge 0 = no change, 1 = inserted,
+ * 2 = deleted, from which the caller rebuilds the reference's
+ * insert_neighbor / delete_neighbor maps in batch order.  A row without
+ * slack stops the batch (GDE_ECAPACITY) after the edges before it, as the
+ * sequential pass would.  stats (may be NULL) gets edit_path and edit_ms. */
+int gde_graph_update(gde_ctx *ctx, gde_graph *g, int32_t *h_indices, int64_t *h_degree, const int32_t *us,
+                     const int32_t *vs, int64_t k, int only_insert, uint8_t *outcome, gde_stats *stats);
+
+/* ---- repair of P, R after an edge batch (the first half of instantGNNUpdateBatch / update_ppr) ----
+ * For each key u = keys[i] (a node with insertions), with its degree
+ * old_degree[i] before the batch and its degree now from the resident
+ * (edited) graph: rescales P[u], R[u] and adds the neighbour terms of its
+ * inserted neighbours nbr[nbr_off[2i] .. nbr_off[2i+1]) minus those of its
+ * deleted neighbours nbr[nbr_off[2i+1] .. nbr_off[2i+2]), for every column,
+ * in the reference's arithmetic: kind GDE_IGN (InstantGNN.py:303-314, needs
+ * X; pass no deleted neighbours when the reference's algo contains
+ * 'insert') or GDE_UPPR (ppr_solver.py:776-792).  P, R, X: device n x F
+ * matrices with row stride ld (FP64 if p->prec == GDE_FP64, else FP32).
+ * keys, old_degree, nbr_off (2 nkeys + 1 entries), nbr: host arrays.  The push
+ * from the repaired nodes is gde_feature_push with cand = keys. */
+int gde_feature_repair(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t F, void *P, void *R, const void *X,
+                       int64_t ld, int64_t nkeys, const int32_t *keys, const int64_t *old_degree,
+                       const int64_t *nbr_off, const int32_t *nbr);
 
 /* Slack management for padded graphs (no counterpart in the reference, whose
  * padded layout is fixed when data_process_GNN.py:93-171 builds it).  Re-lays

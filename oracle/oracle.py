@@ -253,12 +253,14 @@ def ign_update(n, indptr, indices, degree, alpha, eps, omega, P, R, X, us, vs, b
     F = R.shape[1]
     X = np.ascontiguousarray(X, dtype=np.float64)
     opers = np.zeros(F, np.int64)
-    for f in range(F):
+
+    def column(f):
         opers[f] = lib().orc_ign_update_column(n, _ptr(indptr), _ptr(indices), _ptr(degree), _ptr(old_degree),
                                                P.ctypes.data + 8 * f, R.ctypes.data + 8 * f, X.ctypes.data + 8 * f, F,
                                                alpha, eps, omega, int("sor" in algo), int("insert" in algo), beta,
                                                _ptr(ik), _ptr(io), _ptr(inb), len(ik), _ptr(dk), _ptr(do), _ptr(dnb),
                                                len(dk), mode, _ptr(col), int(col.max()) + 1)
+    _columns(F, column)
     return maps, opers
 
 
@@ -297,10 +299,12 @@ def ign_sync(n, indptr, indices, degree, alpha, eps, beta, P, R, cand0=None, max
         cand0 = np.ones(n, np.uint8)
     cand0 = np.ascontiguousarray(cand0, dtype=np.uint8)
     opers = np.zeros(F, np.int64)
-    for f in range(F):
+
+    def column(f):
         opers[f] = lib().orc_ign_sync_column(n, _ptr(indptr), _ptr(indices), _ptr(degree), alpha,
                                              alpha if x_gain is None else x_gain, _ptr(eps_vec), beta,
                                              P.ctypes.data + 8 * f, R.ctypes.data + 8 * f, F, _ptr(cand0), max_rounds)
+    _columns(F, column)
     return opers
 
 
@@ -320,6 +324,18 @@ def ign_sor_color(n, indptr, indices, degree, alpha, eps, beta, omega, P, R, col
                                                   R.ctypes.data + 8 * f, F, _ptr(cand0), _ptr(colors),
                                                   int(colors.max()) + 1, 0)
     return opers
+
+
+def _columns(F: int, fn) -> None:
+    """fn(f) for every column f, on host threads (each column's C call touches only its own column of P, R;
+    ctypes releases the GIL around the call)."""
+    if F <= 1:
+        for f in range(F):
+            fn(f)
+        return
+    from concurrent.futures import ThreadPoolExecutor
+    with ThreadPoolExecutor(max_workers=min(F, os.cpu_count() or 1)) as ex:
+        list(ex.map(fn, range(F)))
 
 
 def threads() -> int:

@@ -90,6 +90,36 @@ def test_noalloc_matches_gde_solve_twice(cl, name, kind, method, alpha, eps, pre
             assert abs(o - oe) <= 1e-3 * oe, (name, call, o, oe)
 
 
+def test_noalloc_katz_near_its_radius_keeps_the_fp64_rule(cl):
+    """An FP32 Katz query with alpha * lambda_max >= 0.9 computes in FP64 in both entry points.
+
+    The largest degree cannot clear it here, so on a graph without a spectral
+    estimate the allocation-free call computes in FP64 (its operation counts
+    are the FP64 solve's); once the estimate is cached, gde_solve and the
+    allocation-free call take the same precision and agree to the FP64 bar,
+    twice in a row.
+    """
+    g, _ = cl
+    fresh = api.Graph(g.indptr, g.indices)      # no spectral estimate cached yet
+    lam = api.katz_spectral_bounds(api.Graph(g.indptr, g.indices), 0.1)["lam_max"]
+    alpha = 0.95 / lam
+    assert alpha * float(g.degree.max()) >= 0.9
+    seeds = graphs.uniform_seeds(g, 2, seed=12)
+    _, _, o64, _ = existing(fresh, L.KATZ, L.LOCAL_GD, int(seeds[0]), 1e-6, "fp64", alpha)
+    _, _, o, _ = noalloc(fresh, L.KATZ, L.LOCAL_GD, int(seeds[0]), 1e-6, "fp32", alpha)
+    assert o == pytest.approx(o64, rel=OPER_RTOL)
+    api.katz_spectral_bounds(fresh, alpha)      # caches the estimate gde_solve would compute
+    for call in range(2):
+        s = int(seeds[call])
+        xe, re_, oe, ke = existing(fresh, L.KATZ, L.LOCAL_GD, s, 1e-6, "fp32", alpha)
+        x, r, o, k = noalloc(fresh, L.KATZ, L.LOCAL_GD, s, 1e-6, "fp32", alpha)
+        assert o == pytest.approx(oe, rel=OPER_RTOL), (call, o, oe)
+        assert k == ke
+        # both computed in FP64 and rounded to FP32 rows
+        assert rel_l1(x, xe.astype(np.float64)) < 1e-6, call
+    fresh.free()
+
+
 def test_noalloc_rejects_graph_above_the_fixed_scratch():
     n = 2_000_000                    # ~90 MB of FP32 workspace > the 64 MiB array
     u = np.arange(n - 1, dtype=np.int64)
