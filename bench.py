@@ -68,6 +68,9 @@ def parse():
     ap.add_argument("--mlp", action="store_true",
                     help="c5: train the MLP classifier on the device-resident features after the initial push and "
                          "after the last snapshot (outside the timed region)")
+    ap.add_argument("--online", action="store_true",
+                    help="c4: submit the queries in real time to the online server (gde_server_*) instead of "
+                         "handing the whole arrival schedule to one served launch")
     ap.add_argument("--rates", default="250,500,1000,2000,0",
                     help="c4: Poisson arrival rates in queries/s to sweep (0 = all queries at once)")
     return ap.parse_args()
@@ -513,6 +516,19 @@ def run_c3(args):
     if not args.no_baselines and rank == 0:
         from oracle import oracle as O
         threads = O.threads()
+        # the last timed step's rows (still in x_dev) against the FP64 oracle: 64 of its 1,024 queries
+        sd, ep = batch(100 + args.steps - 1)
+        pick = np.arange(0, Q, Q // 64)
+        oo, xo = O.ppr_gd_many(g.n, g.indptr, g.indices, g.degree.astype(np.float64), sd[pick], ALPHA, ep[pick],
+                               keep_x=True, nthreads=threads)
+        xg = x_dev[torch.from_numpy(pick).to(x_dev.device)].double().cpu().numpy()
+        l1 = np.abs(xg - xo).sum(1)
+        od = np.abs(outs[-1]["oper"][pick] - oo) / np.maximum(oo, 1)
+        out["accuracy"] = {"vs": "FP64 oracle (C port of ppr_gd local)", "queries": int(pick.size),
+                           "l1_max": float(l1.max()), "l1_mean": float(l1.mean()),
+                           "rel_l1_max": float((l1 / np.abs(xo).sum(1)).max()),
+                           "oper_rel_diff_max": float(od.max()), "oper_abs_diff_max": float(
+                               np.abs(outs[-1]["oper"][pick] - oo).max())}
         sd, ep = batch(300)
         nq = max(args.cpu_queries, 2 * threads)
         t0 = time.perf_counter()
@@ -522,6 +538,62 @@ def run_c3(args):
                                "sample": f"{nq} of the step's queries (ppr_gd local FP64), {dt:.1f} s"}
     if rank == 0:
         print(json.dumps(out), flush=True)
+
+
+def mixed_oracle(g, kind, seed, eps, alpha, tau):
+    """FP64 oracle row of one mixed query, as the reference returns it -> (x, oper)."""
+    from gde import _lib as L
+    from oracle import oracle as O
+    deg = g.degree.astype(np.float64)
+    if kind == L.PPR:
+        x, _, o = O.ppr_gd(g.n, g.indptr, g.indices, deg, int(seed), alpha, eps, True)
+    elif kind == L.KATZ:
+        x, _, o = O.katz_gd(g.n, g.indptr, g.indices, deg, int(seed), alpha, eps, True)
+    else:
+        _, x, _, o = O.hk_sor_queue(g.n, g.indptr, g.indices, deg, int(seed), tau, eps, 1.0, True)
+    return x, float(o)
+
+
+def mixed_accuracy(g, rows, opers, kinds, seeds, eps, alphas, tau, per_kind: int = 3, eps_min: float = 1e-6):
+    """FP32 rows of a mixed queue against the FP64 oracle, `per_kind` queries of each kind with eps >= eps_min
+    (the oracle is sequential; smaller eps is what the GPU is for), in parallel on the host's threads."""
+    from concurrent.futures import ThreadPoolExecutor
+    from gde import _lib as L
+    pick = []
+    for k in (L.PPR, L.KATZ, L.HK):
+        idx = np.flatnonzero((kinds == k) & (eps >= eps_min))[:per_kind]
+        pick += [int(i) for i in idx]
+    with ThreadPoolExecutor(max_workers=os.cpu_count() or 1) as ex:
+        orc = list(ex.map(lambda i: mixed_oracle(g, int(kinds[i]), seeds[i], float(eps[i]), float(alphas[i]), tau),
+                          pick))
+    per = {}
+    for i, (xo, oo) in zip(pick, orc):
+        x = np.asarray(rows[i], dtype=np.float64)
+        name = {int(L.PPR): "ppr", int(L.KATZ): "katz", int(L.HK): "hk"}[int(kinds[i])]
+        d = per.setdefault(name, {"queries": 0, "l1_max": 0.0, "rel_l1_max": 0.0, "oper_rel_diff_max": 0.0})
+        d["queries"] += 1
+        l1 = float(np.abs(x - xo).sum())
+        d["l1_max"] = max(d["l1_max"], l1)
+        d["rel_l1_max"] = max(d["rel_l1_max"], l1 / max(float(np.abs(xo).sum()), 1e-300))
+        d["oper_rel_diff_max"] = max(d["oper_rel_diff_max"], abs(float(opers[i]) - oo) / max(oo, 1.0))
+    return {"vs": "FP64 oracle (C ports of ppr_gd, katz_gd, hk_sor_queue local)", "eps_min": eps_min, "per_kind": per}
+
+
+def mixed_cpu_baseline(g, kinds, seeds, eps, alphas, tau, budget_s: float = 15.0):
+    """The oracle's C ports on the host's threads over the mix (eps as drawn), until about budget_s of work."""
+    from concurrent.futures import ThreadPoolExecutor
+    threads = os.cpu_count() or 1
+    done = 0
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        while done < len(kinds) and time.perf_counter() - t0 < budget_s:
+            k = min(threads, len(kinds) - done)
+            list(ex.map(lambda i: mixed_oracle(g, int(kinds[i]), seeds[i], float(eps[i]), float(alphas[i]), tau),
+                        range(done, done + k)))
+            done += k
+    dt = time.perf_counter() - t0
+    return {"value": done / dt, "unit": "queries/s", "cores": threads, "kind": "port",
+            "sample": f"{done} queries of the mix (eps as drawn, FP64 C ports, one per thread), {dt:.1f} s"}
 
 
 def run_c4(args):
@@ -554,14 +626,23 @@ def run_c4(args):
         arr = None if rate <= 0 else np.cumsum(rng.exponential(1e3 / rate, Q))
         return kinds, seeds, eps, alphas, arr
 
-    def step(k, rate):
+    config = {"workload": "served_mix_ppr_katz_hk_fp32_rmat22", "n": g.n, "nnz": g.nnz, "queries_per_step": Q,
+              "ppr_alpha": ALPHA, "katz_alpha": "0.5 / d_max", "hk_tau": tau, "eps": "log-uniform [1e-8, 1e-5]",
+              "hbm_budget_bytes": budget, "requested_slots": args.slots, "graph_generation_s": gen_s}
+    if args.online:
+        run_c4_online(args, g, G, x_dev, queries, config, tau, budget)
+        return
+
+    def step(k, rate, x_out=None, device_out=True):
         kinds, seeds, eps, alphas, arr = queries(k, rate)
         return api.serve_mixed(G, kinds, seeds, eps, alphas=alphas, tau=tau, arrival_ms=arr, hbm_budget_bytes=budget,
-                               prec="fp32", x_out=x_dev, device_out=True, slots=args.slots)
+                               prec="fp32", x_out=x_dev if x_out is None else x_out, device_out=device_out,
+                               slots=args.slots)
 
     for w in range(args.warmup):
         step(10 + w, 0)
     rows = []
+    sat = None
     with ClockSampler(local) as clk:
         for rate in [float(r) for r in args.rates.split(",")]:
             times, outs = _timed_steps(stream, flush, args.steps, lambda k: step(100 + k, rate))
@@ -569,19 +650,117 @@ def run_c4(args):
             rows.append({"rate_qps": rate if rate > 0 else None, "queries_per_s": Q * len(times) / (sum(times) / 1e3),
                          "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
                          "slots": int(outs[0]["stats"]["tiles"]), "ms_per_step": sum(times) / len(times)})
+            if rate <= 0:
+                sat = (times, outs, 100 + len(times) - 1)
     best = max(rows, key=lambda r: r["queries_per_s"])
     out = {
         "metric": "served mixed queries/s + p50/p99 ms (60% PPR, 25% Katz, 15% heat kernel), R-MAT scale 22",
         "value": best["queries_per_s"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": best["ms_per_step"], "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
-        "config": {"workload": "served_mix_ppr_katz_hk_fp32_rmat22", "n": g.n, "nnz": g.nnz, "queries_per_step": Q,
-                   "ppr_alpha": ALPHA, "katz_alpha": "0.5 / d_max", "hk_tau": tau, "eps": "log-uniform [1e-8, 1e-5]",
-                   "hbm_budget_bytes": budget, "requested_slots": args.slots, "graph_generation_s": gen_s,
-                   "l2": "512 MB buffer written between timed steps"},
+        "config": dict(config, l2="512 MB buffer written between timed steps"),
         "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "rate_sweep": rows,
         "gpu_launches": args.steps * len(rows), "clocks": clk.summary(),
     }
+    if sat is not None:
+        # roofline of the push kernel over the saturation steps (all queries arrive at once)
+        times, outs, last = sat
+        agg = {k: sum(o["stats"][k] for o in outs) for k in ("union_vol", "col_vol", "col_nodes", "kernel_ms")}
+        achieved = algorithmic_bytes(agg) / (agg["kernel_ms"] / 1e3) / 1e9
+        peak, peak_kind = measured_peak()
+        out["roofline"] = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                           "peak_kind": peak_kind, "traffic": None, "kernel": "push_kernel<float,1>",
+                           "kernel_ms_per_launch": agg["kernel_ms"] / len(outs),
+                           "algorithmic_bytes_per_launch": algorithmic_bytes(agg) / len(outs)}
+        # e2e: the same saturation step into pinned host rows (host seeds, eps, kinds)
+        x_host = torch.empty((Q, g.n), dtype=torch.float32).pin_memory()
+        e2e, _ = _timed_steps(stream, flush, max(1, args.e2e_steps), lambda k: step(300 + k, 0, x_host, False))
+        out["e2e"] = {"value": Q * len(e2e) / (sum(e2e) / 1e3), "unit": "queries/s",
+                      "h2d_bytes_per_step": Q * (4 + 4 + 8 + 8), "d2h_bytes_per_step": Q * g.n * 4}
+        if not args.no_baselines:
+            kinds, seeds, eps, alphas, _ = queries(last, 0)
+            xr = x_dev.cpu().numpy()
+            out["accuracy"] = mixed_accuracy(g, xr, outs[-1]["oper"], kinds, seeds, eps, alphas, tau)
+            out["cpu_baseline"] = mixed_cpu_baseline(g, kinds, seeds, eps, alphas, tau)
+    print(json.dumps(out), flush=True)
+
+
+def run_c4_online(args, g, G, x_dev, queries, config, tau, budget):
+    """The C4 mix through the online server: a host loop submits each query at its Poisson arrival time while
+    the server's persistent launch runs, and watches the completion records.  Latency is measured on the host,
+    from a query's scheduled arrival to the moment its completed record is seen; throughput is queries over the
+    time from the first arrival to the last completion."""
+    from gde import _lib as L
+    from gde import api
+    Q = args.batch
+    srv = api.Server(G, prec="fp32", slots=args.slots, tau=tau, ring_capacity=max(4096, 2 * Q),
+                     hbm_budget_bytes=budget, idle_ms=50.0)
+
+    def run(k, rate):
+        kinds, seeds, eps, alphas, arr = queries(k, rate)
+        arr = np.zeros(Q) if arr is None else arr
+        tickets = np.full(Q, -1, np.int64)
+        fin = np.full(Q, np.nan)
+        opers = np.zeros(Q)
+        nxt = 0
+        t0 = time.perf_counter()
+        while True:
+            now = (time.perf_counter() - t0) * 1e3
+            while nxt < Q and arr[nxt] <= now:
+                tickets[nxt] = srv.submit(int(kinds[nxt]), int(seeds[nxt]), float(eps[nxt]), float(alphas[nxt]),
+                                          x_dev[nxt])
+                nxt += 1
+            idx = np.flatnonzero((tickets >= 0) & np.isnan(fin))
+            if idx.size:
+                r = srv.poll_many(tickets[idx])
+                hit = r["done"] == 1
+                if hit.any():
+                    fin[idx[hit]] = (time.perf_counter() - t0) * 1e3
+                    opers[idx[hit]] = r["oper"][hit]
+            if nxt == Q and not np.isnan(fin).any():
+                break
+        lat = fin - arr
+        span = (fin.max() - arr.min()) / 1e3
+        return {"rate_qps": rate if rate > 0 else None, "queries_per_s": Q / span,
+                "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99))}, \
+            (kinds, seeds, eps, alphas, opers)
+
+    for w in range(args.warmup):
+        run(10 + w, 0)
+    rows = []
+    last = None
+    with ClockSampler(G.ctx.device) as clk:
+        for rate in [float(r) for r in args.rates.split(",")]:
+            for k in range(args.steps):
+                row, q = run(100 + k, rate)
+                rows.append(row)
+                if rate <= 0:
+                    last = q
+    info = srv.info()
+    srv.stop()
+    sat = [r for r in rows if r["rate_qps"] is None]
+    best = max(sat or rows, key=lambda r: r["queries_per_s"])
+    sweep = {}
+    for r in rows:
+        key = r["rate_qps"] or 0
+        d = sweep.setdefault(key, {"rate_qps": r["rate_qps"], "queries_per_s": [], "p50_ms": [], "p99_ms": []})
+        for f in ("queries_per_s", "p50_ms", "p99_ms"):
+            d[f].append(r[f])
+    sweep = [{k: (float(np.median(v)) if isinstance(v, list) else v) for k, v in d.items()} for d in sweep.values()]
+    out = {
+        "metric": "online served mixed queries/s + p50/p99 ms (60% PPR, 25% Katz, 15% heat kernel), R-MAT scale 22",
+        "value": best["queries_per_s"], "unit": "queries/s", "n_gpus": 1, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": 1e3 * Q / best["queries_per_s"], "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": dict(config, workload="online_served_mix_ppr_katz_hk_fp32_rmat22", submission="host loop, "
+                       "real-time Poisson arrivals into the server's pinned ring", slots=info["slots"]),
+        "p50_ms": best["p50_ms"], "p99_ms": best["p99_ms"], "rate_sweep": sweep,
+        "server": info, "gpu_launches": int(info["launches"]), "clocks": clk.summary(),
+        "latency": "host-observed: scheduled arrival to completion record seen",
+    }
+    if last is not None and not args.no_baselines:
+        kinds, seeds, eps, alphas, opers = last
+        out["accuracy"] = mixed_accuracy(g, x_dev.cpu().numpy(), opers, kinds, seeds, eps, alphas, tau)
     print(json.dumps(out), flush=True)
 
 
@@ -630,7 +809,7 @@ def run_c5(args):
             us = np.concatenate([dyn.Us[s - 1], us])[perm]
             vs = np.concatenate([dyn.Vs[s - 1], vs])[perm]
         batches.append((np.ascontiguousarray(us, dtype=np.int32), np.ascontiguousarray(vs, dtype=np.int32)))
-    times, outs = [], []
+    times, outs, snapP = [], [], []
     with ClockSampler(local) as clk:
         for s in range(snaps):
             torch.cuda.synchronize()
@@ -642,6 +821,7 @@ def run_c5(args):
             e1.record(stream)
             e1.synchronize()
             times.append(e0.elapsed_time(e1))
+            snapP.append(Pd[:, :C5_CHECK_COLS].double().cpu().numpy())  # after the timed region
     total_ms = sum(times)
     agg = {k: sum(o["stats"][k] for o in outs) for k in ("union_vol", "col_vol", "col_nodes", "kernel_ms")}
     achieved = algorithmic_bytes(agg) / (max(agg["kernel_ms"], 1e-9) / 1e3) / 1e9
@@ -669,7 +849,73 @@ def run_c5(args):
     if args.mlp:
         mlp["final"] = consumer.train_eval(Pd, labels, split)
         out["mlp"] = mlp
+    # e2e: the whole sequence again through the public API, each snapshot's P read back to pinned host memory
+    # inside the timed region (the edge batch goes in from host arrays)
+    indices2, degree2 = dyn.indices.copy(), dyn.degree.copy()
+    G2 = api.Graph(dyn.indptr, indices2, row_len=degree2, degree=degree2.astype(np.float64), ctx=G.ctx)
+    P2, R2 = torch.zeros_like(Xd), Xd.clone()
+    api.feature_push(G2, L.IGN, P2, R2, eps, alpha=ALPHA, beta=beta, prec="fp32", tile_w=tw)
+    P_host = torch.empty((n, F), dtype=torch.float32).pin_memory()
+    torch.cuda.synchronize()
+    e2e = []
+    for s in range(snaps):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        api.feature_update(G2, L.IGN, indices2, degree2, batches[s][0], batches[s][1], not mixed, P2, R2, Xd, eps,
+                           alpha=ALPHA, beta=beta, prec="fp32", tile_w=tw)
+        with torch.cuda.stream(stream):
+            P_host.copy_(P2, non_blocking=True)
+        e1.record(stream)
+        e1.synchronize()
+        e2e.append(e0.elapsed_time(e1))
+    out["e2e"] = {"value": snaps / (sum(e2e) / 1e3), "unit": "snapshots/s",
+                  "h2d_bytes_per_step": int(2 * 4 * batches[0][0].shape[0]), "d2h_bytes_per_step": int(n * F * 4)}
+    G2.free()
+    if not args.no_baselines:
+        out.update(c5_oracle_check(dyn, X, batches, mixed, snapP, outs, beta, eps))
     print(json.dumps(out), flush=True)
+
+
+C5_CHECK_COLS = 4
+
+
+def c5_oracle_check(dyn, X, batches, mixed, snapP, outs, beta, eps):
+    """accuracy: C5_CHECK_COLS FP32 columns after every snapshot against the FP64 oracle's synchronous update
+    (the GPU's order); cpu_baseline: the oracle's port of the reference's FIFO update (instantGNNUpdateBatch,
+    InstantGNN.py:298-329), one column per host thread on one snapshot, scaled to 128 columns."""
+    from oracle import oracle as O
+    n = dyn.n
+    ip = dyn.indptr.astype(np.int64)
+    threads = os.cpu_count() or 1
+    Fs = max(C5_CHECK_COLS, min(threads, 16))
+    ix, dg = dyn.indices.copy(), dyn.degree.copy()
+    Xs = X[:, :Fs].astype(np.float64)
+    Po, Ro = np.zeros((n, Fs)), Xs.copy()
+    O.ign_sync(n, ip, ix, dg, ALPHA, eps, beta, Po, Ro)
+    # CPU baseline: the reference's FIFO update of snapshot 0 on Fs columns in parallel
+    ixb, dgb, Pb, Rb = ix.copy(), dg.copy(), Po.copy(), Ro.copy()
+    t0 = time.perf_counter()
+    O.ign_update(n, ip, ixb, dgb, ALPHA, eps, 1.0, Pb, Rb, Xs, batches[0][0], batches[0][1], beta,
+                 "fwd" + ("" if mixed else "-insert"), sync=False)
+    dt = time.perf_counter() - t0
+    cpu = {"value": 1.0 / (dt * 128 / Fs), "unit": "snapshots/s", "cores": threads, "kind": "port",
+           "sample": f"snapshot 0 on {Fs} of 128 columns in parallel (one per thread), {dt:.2f} s, "
+                     f"scaled by 128/{Fs}"}
+    # accuracy: the first C5_CHECK_COLS columns through every snapshot
+    k = C5_CHECK_COLS
+    Pa, Ra, Xa = Po[:, :k].copy(), Ro[:, :k].copy(), Xs[:, :k].copy()
+    per = []
+    for s, (us, vs) in enumerate(batches):
+        _, oo = O.ign_update(n, ip, ix, dg, ALPHA, eps, 1.0, Pa, Ra, Xa, us, vs, beta,
+                             "fwd" + ("" if mixed else "-insert"), sync=True)
+        rel = np.abs(snapP[s] - Pa).sum(0) / np.abs(Pa).sum(0)
+        od = np.abs(outs[s]["oper"][:k] - oo) / np.maximum(oo, 1)
+        per.append({"snapshot": s, "rel_l1_max": float(rel.max()), "oper_rel_diff_max": float(od.max())})
+    acc = {"vs": "FP64 oracle, synchronous update push (C port of instantGNNUpdateBatch's repair)",
+           "columns": k, "snapshots": len(per), "rel_l1_max": max(p["rel_l1_max"] for p in per),
+           "oper_rel_diff_max": max(p["oper_rel_diff_max"] for p in per), "per_snapshot": per}
+    return {"accuracy": acc, "cpu_baseline": cpu}
 
 
 def main():

@@ -1370,10 +1370,11 @@ static int feature_push_impl(gde_ctx* ctx, gde_graph* G, const gde_params* p, in
         int rc = alloc_tiles(ctx, G, nt, W, prec64, false, false, false, false, tw);
         if (rc != GDE_OK) return rc;
         PushArgs& a = tw.a;
-        // an incremental update (candidates given on the device) visits only
-        // touched nodes: degree edits may have lowered untouched thresholds,
-        // and the reference never re-examines those nodes
-        a.allow_dense = cand_on_device ? 0 : 1;
+        // a push that starts from a candidate list (an incremental update, a
+        // reference queue) visits only touched nodes: degree edits may have
+        // lowered untouched thresholds, and the reference never re-examines
+        // those nodes; only the initial scan of every node may go dense
+        a.allow_dense = cand ? 0 : 1;
         rc = alloc_large(ctx, G, nt, tw);
         if (rc != GDE_OK) return rc;
         const size_t es = prec64 ? 8 : 4;

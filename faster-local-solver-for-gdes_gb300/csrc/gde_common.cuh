@@ -115,6 +115,46 @@ enum SlotState : int {
     SLOT_DONE = 1,    // finished (batch solves: results extracted after the launch)
     SLOT_IDLE = 2,    // served solves: result extracted and slot cleared, awaiting a query
     SLOT_EMPTY = 3,   // served solves: no query left for this slot
+    SLOT_DRAIN = 4,   // online server: result written; the slot's vectors are cleared this round
+};
+
+// ---------------------------------------------------------------------------
+// Online server (gde_server_*): requests arrive in a ring in pinned host
+// memory that the device reads while the persistent launch runs.
+// ---------------------------------------------------------------------------
+struct OnlineReq {            // one submitted query, written by the host before it publishes `tail`
+    int32_t kind;             // KIND_PPR / KIND_KATZ / KIND_HK
+    int32_t seed;             // internal node id
+    int32_t seed_caller;      // caller node id (Katz x[s] -= 1 in caller order)
+    int32_t n_levels;         // HK: Taylor length N
+    int32_t psi_off;          // HK: offset of its psi table
+    int32_t out64;            // x_out holds doubles (else floats)
+    double theta;             // threshold scale
+    double r0;                // initial residual at the seed
+    double alpha;             // PPR / Katz alpha
+    void* x_out;              // device-addressable row of n entries, caller order (nullptr: none)
+    long long ticket;
+};
+
+struct OnlineDone {           // completion record, device-written; the host reads done_ticket last
+    double oper;
+    int32_t rounds;
+    int32_t status;           // GDE_OK
+    unsigned long long admit_ns, finish_ns;
+    long long done_ticket;    // == ticket once the record and the row are complete
+};
+
+struct OnlineSlot {           // the query a slot holds (copied out of the ring at admission)
+    long long ticket;
+    void* x_out;
+    int32_t out64;
+    int32_t seed_caller;
+    int32_t kind;
+    int32_t rounds;
+    int32_t status;           // GDE_OK, or GDE_EITERCAP when max_rounds stopped it
+    int32_t pad;
+    double oper;
+    unsigned long long admit_ns, finish_ns;
 };
 
 struct TileState {            // device-updated
@@ -154,6 +194,20 @@ struct ServeQueue {
     int* rounds;                  // [nq]
     unsigned long long* start_ns; // [nq] admission time
     unsigned long long* finish_ns;// [nq] finish time
+    // online server (online != 0): queries come from a ring the host fills
+    // while the launch runs, instead of the arrays above
+    int online;
+    int cap;                      // ring entries
+    const OnlineReq* req;         // [cap] pinned host ring
+    OnlineDone* done;             // [cap] pinned host completion records (ticket % cap)
+    const long long* tail;        // host-written: tickets submitted so far
+    long long* head;              // device-written (host-visible): tickets admitted so far
+    const int* stop;              // host-written stop flag
+    int* quit;                    // device: every block leaves at the next round start when set
+    unsigned long long* last_ns;  // device: %globaltimer of the last round with work
+    unsigned long long idle_ns;   // the launch ends after this long with nothing to do
+    OnlineSlot* slot;             // [slots]
+    const int32_t* perm;          // caller id -> internal id (nullptr: identity)
 };
 
 struct ColState {             // one per column slot

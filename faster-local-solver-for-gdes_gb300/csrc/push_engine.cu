@@ -364,7 +364,9 @@ struct RoundSh {
     int any_check;                              // some live tile needs a CHECK phase
     int any_idle;                               // served solves: some slot awaits a query
     int tiles[kMaxLaunchTiles];                 // live tile ids (ascending)
-    unsigned char idle[kMaxLaunchTiles];        // slot was idle at the round start
+    unsigned char idle[kMaxLaunchTiles];        // 1: slot idle at the round start; 2: draining (online)
+    short drain[kMaxLaunchTiles];               // online slots to clear this round (SLOT_DRAIN)
+    int ndrain;
     long long off[4][kMaxLaunchTiles + 1];      // exclusive prefix sums of the current phase's spaces
     int level[kMaxLaunchTiles];                 // per live tile: rounds since its start
     unsigned char flags[kMaxLaunchTiles];       // per live tile scatter flags (SF_*)
@@ -1481,7 +1483,16 @@ __device__ void finish_round(const PushArgs& a, int t, int level, bool dense_nex
         // level: that level pushes into x during SCATTER, so x is read out by
         // the next round's retire
         if (ts.front_cnt[par] == 0 || (hk_end && !a.serve)) {
-            if (a.serve) {
+            if (a.serve && a.queue.online) {
+                // online slot: its row is gathered by every block in this
+                // SCATTER; next round clears the slot and publishes the result
+                const ColState& cs = a.cs[(int64_t)t * W];
+                OnlineSlot& os = a.queue.slot[t];
+                os.oper = cs.oper;
+                os.rounds = cs.rounds;
+                os.finish_ns = globaltimer_ns();
+                ts.done = SLOT_DRAIN;
+            } else if (a.serve) {
                 // served slot: the query's result is extracted and the slot
                 // cleared by every block in this SCATTER; admit next round
                 const ColState& cs = a.cs[(int64_t)t * W];
@@ -1612,6 +1623,144 @@ __device__ void retire_range(const PushArgs& a, int t, long long beg, long long 
     }
 }
 
+// ---------------------------------------------------------------------------
+// Online server: the request ring and completion records live in pinned host
+// memory.  The host publishes a request by a release store of `tail` after
+// writing the entry; the device reads `tail` with an acquire load at system
+// scope, then the entry.  A completion record is filled, then published by a
+// release store of done_ticket.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ long long ld_acquire_sys(const long long* p) {
+    long long v;
+    asm volatile("ld.acquire.sys.b64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
+    return v;
+}
+__device__ __forceinline__ void st_release_sys(long long* p, long long v) {
+    asm volatile("st.release.sys.b64 [%0], %1;" ::"l"(p), "l"(v) : "memory");
+}
+__device__ __forceinline__ int ld_relaxed_sys_i(const int* p) {
+    int v;
+    asm volatile("ld.relaxed.sys.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+// Block 0, thread 0: the next submitted query into idle slot t, if any.
+template <typename T, int W>
+__device__ bool admit_online(const PushArgs& a, int t, int it) {
+    const ServeQueue& q = a.queue;
+    const long long head = *q.head;  // only this thread writes it
+    if (head >= ld_acquire_sys(q.tail)) return false;
+    const volatile OnlineReq* rq = q.req + (head % q.cap);
+    const int k = rq->kind;
+    const int seed = rq->seed;
+    OnlineSlot& os = q.slot[t];
+    os.ticket = rq->ticket;
+    os.x_out = rq->x_out;
+    os.out64 = rq->out64;
+    os.seed_caller = rq->seed_caller;
+    os.kind = k;
+    os.rounds = 0;
+    os.status = GDE_OK;
+    os.oper = 0.0;
+    os.finish_ns = 0;
+    TileState& ts = a.ts[t];
+    TileParams& tp = a.tp[t];
+    tp.kind = k;
+    tp.method = (k == KIND_HK) ? M_HK_LOCAL : M_LOCAL_GD;
+    tp.alpha = (k == KIND_HK) ? 0.0 : rq->alpha;
+    tp.tau = q.tau;
+    tp.n_levels = (k == KIND_HK) ? rq->n_levels : 0;
+    tp.psi_tab = (k == KIND_HK) ? q.psi + rq->psi_off : nullptr;
+    const double theta = rq->theta, r0 = rq->r0;
+    *q.head = head + 1;
+    __threadfence_system();
+    // stamps keep growing within the slot: skip past the last query's
+    ts.stamp = ts.stamp + max(it - ts.t0, 0) + 2;
+    for (int i = 0; i < 3; ++i) ts.cand_cnt[i] = 0;
+    for (int i = 0; i < 2; ++i) {
+        ts.front_cnt[i] = ts.small_cnt[i] = ts.med_cnt[i] = ts.large_cnt[i] = 0;
+        ts.dense_next[i] = 0;
+        ts.union_vol[i] = 0.0;
+    }
+    const int64_t n = a.g.n;
+    a.cand[((int64_t)t * 2 + 0) * n] = seed;  // level-0 candidates: the seed
+    ts.cand_cnt[0] = 1;
+    ts.t0 = it + 1;
+    ts.qid = t;
+    ColState& cs = a.cs[(int64_t)t * W];
+    cs.theta = theta;
+    cs.oper = 0.0;
+    cs.fsum = 0;
+    cs.live = 1;
+    cs.rounds = 0;
+    cs.round_active[0] = cs.round_active[1] = 0;
+    cs.check_cnt[0] = cs.check_cnt[1] = 0;
+    cs.seed = seed;
+    cs.finish_ns = 0;
+    slab_ptr<T>(a.R, a, t)[(int64_t)seed * a.ld] = (T)r0;
+    os.admit_ns = globaltimer_ns();
+    __threadfence();
+    ts.done = SLOT_LIVE;
+    return true;
+}
+
+// A finished online query's row, caller ids [beg, end): gathered through
+// the node permutation into the caller's row, x - c for a Kahan slab, with
+// the Katz x[s] -= 1 and the heat kernel's x / e^tau.  Read-only on the
+// slot: its vectors are cleared next round, after every block's gather.
+template <typename T, int W>
+__device__ void gather_online_range(const PushArgs& a, int t, long long beg, long long end) {
+    const ServeQueue& q = a.queue;
+    const OnlineSlot& os = q.slot[t];
+    if (!os.x_out) return;
+    const T* X = xslab_ptr<T>(a.X, a, t);
+    const float* XC = a.kahan ? xslab_ptr<float>(a.XC, a, t) : nullptr;
+    const int64_t xld = x_ld(a);
+    const double seed_add = (os.kind == KIND_KATZ) ? -1.0 : 0.0;  // katz_solver.py:243
+    const double xdiv = (os.kind == KIND_HK) ? q.hk_scale : 1.0;    // hk_solver.py:295
+    for (long long u = beg + threadIdx.x; u < end; u += kThreads) {
+        const int64_t v = q.perm ? q.perm[u] : u;
+        double x = (double)X[v * xld];
+        if (XC) x -= (double)XC[v * xld];
+        if (u == os.seed_caller) x += seed_add;
+        if (xdiv != 1.0) x /= xdiv;
+        if (os.out64) reinterpret_cast<double*>(os.x_out)[u] = x;
+        else reinterpret_cast<float*>(os.x_out)[u] = (float)x;
+    }
+    __threadfence_system();
+}
+
+// A drained online slot's vectors back to zero, internal nodes [beg, end).
+template <typename T, int W>
+__device__ void clear_slot_range(const PushArgs& a, int t, long long beg, long long end) {
+    T* X = xslab_ptr<T>(a.X, a, t);
+    T* R = slab_ptr<T>(a.R, a, t);
+    T* R2 = a.R2 ? slab_ptr<T>(a.R2, a, t) : nullptr;
+    float* XC = a.kahan ? xslab_ptr<float>(a.XC, a, t) : nullptr;
+    const int64_t xld = x_ld(a);
+    for (long long v = beg + threadIdx.x; v < end; v += kThreads) {
+        R[v * a.ld] = T(0);
+        X[v * xld] = T(0);
+        if (XC) XC[v * xld] = 0.f;
+        if (R2) R2[v * a.ld] = T(0);
+    }
+}
+
+// Block 0, thread 0: a drained slot's completion record (its row was
+// gathered, by every block, in the previous round).
+__device__ void publish_online(const PushArgs& a, int t) {
+    const ServeQueue& q = a.queue;
+    const OnlineSlot& os = q.slot[t];
+    OnlineDone* d = q.done + (os.ticket % q.cap);
+    d->oper = os.oper;
+    d->rounds = os.rounds;
+    d->status = os.status;
+    d->admit_ns = os.admit_ns;
+    d->finish_ns = os.finish_ns;
+    __threadfence_system();
+    st_release_sys(&d->done_ticket, os.ticket);
+}
+
 // Opt-in per-block phase timeline (thread 0, first trace_iters iterations).
 __device__ __forceinline__ void trace_point(const PushArgs& a, int it, int k) {
     if (a.trace && it < a.trace_iters && threadIdx.x == 0)
@@ -1633,17 +1782,31 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
         ps.acc_col_vol = 0.0; ps.acc_union_vol = 0.0;
     }
     int it = 0;
+    const bool online = a.serve && a.queue.online;
+    if (online && blockIdx.x == 0 && threadIdx.x == 0) *a.queue.last_ns = globaltimer_ns();
     for (; it < a.round_budget; ++it) {
+        // online server: block 0 decided to stop (stop flag, or idle) last round
+        if (online && ld_volatile_i(a.queue.quit) != 0) break;
         trace_point(a, it, TP_ITER);
         // ---- live tiles of this round (identical in every block) ----
-        if (threadIdx.x == 0) { rs.any_check = 0; rs.any_idle = 0; }
+        if (threadIdx.x == 0) { rs.any_check = 0; rs.any_idle = 0; rs.ndrain = 0; }
         __syncthreads();
         for (int t = threadIdx.x; t < a.ntiles; t += kThreads) {
             const TileState& ts = a.ts[t];
             const bool live = ts.done == SLOT_LIVE && it >= ts.t0 && (it - ts.t0) < a.max_rounds;
             s_vals[t] = live ? 1 : 0;
-            rs.idle[t] = (ts.done == SLOT_IDLE) ? 1 : 0;
+            rs.idle[t] = (ts.done == SLOT_IDLE) ? 1 : (ts.done == SLOT_DRAIN ? 2 : 0);
             if (ts.done == SLOT_IDLE) rs.any_idle = 1;
+        }
+        if (online) {
+            // drained slots in ascending order: the same list in every block
+            __syncthreads();
+            if (threadIdx.x == 0) {
+                int nd = 0;
+                for (int t = 0; t < a.ntiles; ++t)
+                    if (rs.idle[t] == 2) rs.drain[nd++] = (short)t;
+                rs.ndrain = nd;
+            }
         }
         __syncthreads();
         block_exclusive_scan(s_vals, a.ntiles, rs.off[0], rs.scan_tmp);
@@ -1660,7 +1823,7 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
         if (threadIdx.x == 0) rs.ntl = (int)rs.off[0][a.ntiles];
         __syncthreads();
         const int ntl = rs.ntl;
-        if (ntl == 0 && !rs.any_idle) break;
+        if (ntl == 0 && !rs.any_idle && rs.ndrain == 0) break;
         const bool timer = (blockIdx.x == 0 && threadIdx.x == 0);
         unsigned long long t0 = timer ? globaltimer_ns() : 0ull;
         // ---- CHECK (global GD / Chebyshev tiles) ----
@@ -1768,7 +1931,18 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
                     const long long b = max(lo, rs.off[3][k]) - rs.off[3][k];
                     const long long e = min(hi, rs.off[3][k + 1]) - rs.off[3][k];
                     if (b >= e) continue;
-                    retire_range<T, W>(a, rs.tiles[k], b, e);
+                    if (online) gather_online_range<T, W>(a, rs.tiles[k], b, e);
+                    else retire_range<T, W>(a, rs.tiles[k], b, e);
+                }
+            }
+            // online slots drained last round: every block an equal share of their nodes
+            if (online && rs.ndrain > 0) {
+                block_share((long long)rs.ndrain * n, lo, hi);
+                for (long long x = lo; x < hi;) {
+                    const long long k = x / n;
+                    const long long e = min(hi, (k + 1) * n);
+                    clear_slot_range<T, W>(a, rs.drain[k], x - k * n, e - k * n);
+                    x = e;
                 }
             }
         }
@@ -1806,9 +1980,20 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
             if (ts.front_cnt[lv & 1] == 0) continue;
             hk_drop<T, W>(a, t, lv, ts.dense_next[lv & 1] != 0, ts.cand_cnt[lv % 3]);
         }
-        if (blockIdx.x == 0 && a.serve && rs.any_idle) {
+        bool admitted = false;
+        if (blockIdx.x == 0 && online) {
+            if (threadIdx.x == 0) {
+                for (int k = 0; k < rs.ndrain; ++k) {
+                    publish_online(a, rs.drain[k]);
+                    a.ts[rs.drain[k]].done = SLOT_IDLE;  // admitted from the next round on
+                }
+                if (rs.any_idle)
+                    for (int t = 0; t < a.ntiles; ++t)
+                        if (rs.idle[t] == 1 && admit_online<T, W>(a, t, it)) admitted = true;
+            }
+        } else if (blockIdx.x == 0 && a.serve && rs.any_idle) {
             for (int t = 0; t < a.ntiles; ++t)
-                if (rs.idle[t]) admit_query<T, W>(a, t, it);
+                if (rs.idle[t] == 1) admit_query<T, W>(a, t, it);
         }
         if (blockIdx.x == 0) {
             finish_columns_all<W>(a, rs, ntl);
@@ -1818,6 +2003,29 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
                 const int lv = rs.level[k];
                 const bool dnext = dense_next_round(a, a.tp[t], a.ts[t], lv & 1);
                 finish_round<W>(a, t, lv, dnext);
+            }
+            if (online && threadIdx.x == 0) {
+                // a slot that reaches max_rounds ends with GDE_EITERCAP (its row is not written)
+                for (int k = 0; k < ntl; ++k) {
+                    const int t = rs.tiles[k];
+                    TileState& ts = a.ts[t];
+                    if (ts.done == SLOT_LIVE && it + 1 - ts.t0 >= a.max_rounds) {
+                        OnlineSlot& os = a.queue.slot[t];
+                        os.oper = a.cs[(int64_t)t * W].oper;
+                        os.rounds = a.cs[(int64_t)t * W].rounds;
+                        os.finish_ns = globaltimer_ns();
+                        os.status = GDE_EITERCAP;
+                        ts.done = SLOT_DRAIN;
+                    }
+                }
+                // leave on the stop flag, or after idle_ns with nothing live,
+                // draining or admitted (every slot is then idle: a later
+                // launch picks the ring up where this one left it)
+                const unsigned long long now = globaltimer_ns();
+                const bool busy = ntl > 0 || rs.ndrain > 0 || admitted;
+                if (busy) *a.queue.last_ns = now;
+                if (ld_relaxed_sys_i(a.queue.stop) != 0 || (!busy && now - *a.queue.last_ns > a.queue.idle_ns))
+                    *a.queue.quit = 1;
             }
         }
         trace_point(a, it, TP_SCAT_ENTER);

@@ -19,7 +19,7 @@ BUILD = os.path.join(PKG_DIR, "build")
 LIB = os.path.join(BUILD, "libgde.so")
 
 SOURCES = ["push_engine.cu", "aux_kernels.cu", "plain.cu", "graph_edit.cu", "gde_capi.cu", "noalloc.cu", "spectral.cu", "sor_engine.cu",
-           "probe.cu"]
+           "probe.cu", "server.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2", "--expt-relaxed-constexpr",
          "-I", INCLUDE, "-I", CSRC]

@@ -77,6 +77,14 @@ SIGNATURES = {
     "gde_ctx_trace": (_int, [_p, _int]),
     "gde_ctx_trace_read": (_int, [_p, _p, _i64, _p, _p, _p]),
     "gde_ctx_set_wait_limit": (_int, [_p, _i64]),
+    "gde_server_start": (_int, [_p, _p, ctypes.POINTER(Params), _i64, _dbl, _dbl, ctypes.POINTER(_p)]),
+    "gde_server_submit": (_int, [_p, _int, _i32, _dbl, _dbl, _p, _int, ctypes.POINTER(_i64)]),
+    "gde_server_poll": (_int, [_p, _i64, ctypes.POINTER(_int), ctypes.POINTER(_dbl), ctypes.POINTER(_i32),
+                               ctypes.POINTER(_dbl)]),
+    "gde_server_poll_many": (_int, [_p, _p, _i64, _p, _p, _p, _p]),
+    "gde_server_info": (_int, [_p, ctypes.POINTER(_int), ctypes.POINTER(_i64), ctypes.POINTER(_dbl),
+                               ctypes.POINTER(_i64)]),
+    "gde_server_stop": (_int, [_p, _int, ctypes.POINTER(_i64)]),
     "gde_solve_noalloc": (_int, [_p, _p, ctypes.POINTER(Params), _i32, _dbl, _p, _p, _int, _p, _p]),
 }
 

@@ -222,6 +222,87 @@ def serve_mixed(graph: Graph, kinds, seeds, eps, *, alphas=None, tau: float = 0.
     return {"x": x_out if want_x else None, "oper": oper, "rounds": rounds, "latency_ms": lat, "stats": st.as_dict()}
 
 
+class Server:
+    """Online serving (``gde_server_*``): queries submitted while one persistent launch runs.
+
+    ``submit`` returns a ticket; ``poll(ticket)`` returns None until the
+    query's row is written, then dict(oper, rounds, device_ms).  Rows go into
+    the caller's buffer: a device tensor or a pinned host tensor of n entries
+    (float32, or float64 with out64).  ``stop(drain=True)`` waits for every
+    submitted query, then ends the kernel and frees the server.
+    """
+
+    def __init__(self, graph: Graph, *, prec: str = "fp32", slots: int = 0, tau: float = 0.0,
+                 ring_capacity: int = 4096, hbm_budget_bytes: float = 0.0, idle_ms: float = 5.0,
+                 tuning: dict | None = None):
+        lib = L.load()
+        t = dict(tuning or {})
+        if slots:
+            t["slots"] = slots
+        p = make_params(L.PPR, L.LOCAL_GD, prec, 1, 0.0, tau, tuning=t)
+        h = ctypes.c_void_p()
+        st = lib.gde_server_start(graph.ctx.ptr, graph.ptr, ctypes.byref(p), int(ring_capacity),
+                                  float(hbm_budget_bytes), float(idle_ms), ctypes.byref(h))
+        L.check(graph.ctx.ptr, st, "gde_server_start")
+        self.ptr = h.value
+        self.graph = graph
+        self.ctx = graph.ctx
+        self._rows = {}  # ticket -> caller buffer (kept alive until the query finishes)
+
+    def submit(self, kind: int, seed: int, eps: float, alpha: float = 0.0, x_out=None, out64: bool = False) -> int:
+        t = ctypes.c_int64()
+        st = L.load().gde_server_submit(self.ptr, int(kind), int(seed), float(eps), float(alpha), _ptr(x_out),
+                                        int(out64), ctypes.byref(t))
+        L.check(self.ctx.ptr, st, "gde_server_submit")
+        if x_out is not None:
+            self._rows[t.value] = x_out
+        return int(t.value)
+
+    def poll(self, ticket: int):
+        done, oper, rounds, dms = ctypes.c_int(), ctypes.c_double(), ctypes.c_int32(), ctypes.c_double()
+        st = L.load().gde_server_poll(self.ptr, int(ticket), ctypes.byref(done), ctypes.byref(oper),
+                                      ctypes.byref(rounds), ctypes.byref(dms))
+        L.check(self.ctx.ptr, st, "gde_server_poll")
+        if not done.value:
+            return None
+        self._rows.pop(int(ticket), None)
+        return {"oper": oper.value, "rounds": rounds.value, "device_ms": dms.value}
+
+    def poll_many(self, tickets: np.ndarray) -> dict:
+        """Vector poll: dict(done[k] int32, oper[k], rounds[k], device_ms[k]) for int64 tickets."""
+        tickets = np.ascontiguousarray(tickets, dtype=np.int64)
+        k = tickets.shape[0]
+        out = {"done": np.zeros(k, np.int32), "oper": np.zeros(k), "rounds": np.zeros(k, np.int32),
+               "device_ms": np.zeros(k)}
+        st = L.load().gde_server_poll_many(self.ptr, _ptr(tickets), k, _ptr(out["done"]), _ptr(out["oper"]),
+                                           _ptr(out["rounds"]), _ptr(out["device_ms"]))
+        L.check(self.ctx.ptr, st, "gde_server_poll_many")
+        return out
+
+    def info(self) -> dict:
+        s, la, km, sub = ctypes.c_int(), ctypes.c_int64(), ctypes.c_double(), ctypes.c_int64()
+        st = L.load().gde_server_info(self.ptr, ctypes.byref(s), ctypes.byref(la), ctypes.byref(km), ctypes.byref(sub))
+        return {"slots": s.value, "launches": la.value, "kernel_ms": km.value, "submitted": sub.value, "status": st}
+
+    def stop(self, drain: bool = True) -> int:
+        """End the server; returns the number of queries abandoned (0 with drain)."""
+        if self.ptr is None:
+            return 0
+        lost = ctypes.c_int64()
+        st = L.load().gde_server_stop(self.ptr, int(drain), ctypes.byref(lost))
+        self.ptr = None
+        self._rows.clear()
+        L.check(self.ctx.ptr, st, "gde_server_stop")
+        return int(lost.value)
+
+    def __del__(self):
+        if getattr(self, "ptr", None) is not None:
+            try:
+                self.stop(drain=False)
+            except Exception:
+                pass
+
+
 def sor(graph: Graph, kind: int, seeds, eps, *, omega: float, local: bool = True, alpha: float = 0.0,
         prec: str = "fp64", out64: bool | None = None, want_x: bool = True, want_r: bool = True,
         device_out: bool = False, max_sweeps: int = 0) -> dict:

@@ -204,6 +204,48 @@ int gde_serve_mixed(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t nq,
                     double hbm_budget_bytes, void *x_out, int out64, int out_mem, int64_t ld_out, double *oper_out,
                     int32_t *rounds_out, float *lat_ms_out, gde_stats *stats);
 
+/* ---- online serving: queries submitted while the kernel runs ----
+ * Replaces the reference's request loop over single-query solver calls
+ * (ppr_solver.py:149-164 over ppr_gd_local_gpu; katz_solver.py:149-164;
+ * hk_solver.py:206-295 per seed) with a request stream into one resident
+ * persistent launch.  gde_server_start allocates p->slots (default 32, at
+ * most 512; fewer if hbm_budget_bytes > 0 holds fewer) one-query slots at
+ * precision p->prec, a ring of ring_capacity requests in pinned host memory,
+ * and starts a host thread that keeps the push kernel running while there is
+ * work: the kernel admits each submitted query into a free slot at a round
+ * boundary, advances every live slot together, writes each finished query's
+ * solution row (as the reference returns it: Katz x[s] - 1, heat kernel
+ * x / e^tau) into the caller's row, and publishes a completion record.
+ * After idle_ms with nothing to do the kernel returns; the next submit
+ * launches it again.  Heat-kernel queries use the level push with
+ * N = estimate_n(p->tau, eps/2) (needs p->tau >= 1); p->tuning fields apply.
+ * While the kernel runs it holds every SM; other work on the device waits
+ * for it to go idle, and the graph must not be edited.
+ *   gde_server_submit: thread-safe, host only; kind GDE_PPR / GDE_KATZ /
+ *     GDE_HK, alpha for PPR / Katz; x_out: n entries in caller node order
+ *     (FP64 if out64, else FP32), device memory of the context's device or
+ *     pinned host memory (or NULL for no row).  *ticket identifies the query.
+ *     GDE_ENOMEM when ring_capacity submitted queries are not yet admitted.
+ *   gde_server_poll: non-blocking; *done = 1 once the row and the record are
+ *     complete, with the operation count, rounds and the device time from
+ *     admission to finish.  Records are kept per ticket % ring_capacity: poll
+ *     a ticket before ring_capacity later submissions (GDE_ENOTFOUND after).
+ *   gde_server_stop: drain != 0 waits for every submitted query first; then
+ *     the stop flag ends the kernel at its next round and the server is
+ *     freed.  *abandoned (may be NULL) = queries that never finished.
+ * Returns GDE_EHANG (through poll or stop) if a bounded device wait ran out. */
+int gde_server_start(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t ring_capacity,
+                     double hbm_budget_bytes, double idle_ms, gde_server **out);
+int gde_server_submit(gde_server *s, int kind, int32_t seed, double eps, double alpha, void *x_out, int out64,
+                      int64_t *ticket);
+int gde_server_poll(gde_server *s, int64_t ticket, int *done, double *oper, int32_t *rounds, double *device_ms);
+/* gde_server_poll over k tickets (host arrays; oper, rounds, device_ms may be NULL); returns the first error */
+int gde_server_poll_many(gde_server *s, const int64_t *tickets, int64_t k, int32_t *done, double *oper,
+                         int32_t *rounds, double *device_ms);
+/* slots in use, kernel launches so far, their device time, queries submitted */
+int gde_server_info(gde_server *s, int *slots, int64_t *launches, double *kernel_ms, int64_t *submitted);
+int gde_server_stop(gde_server *s, int drain, int64_t *abandoned);
+
 /* ---- LocalSOR / APPR (ppr_sor, katz_sor) in multicolour order ----
  * Relaxation res = omega r_u, x_u += res, r_u -= res, push (1-alpha) res / d_u
  * (Katz: alpha res) as in ppr_sor (ppr_solver.py:331-461) / katz_sor

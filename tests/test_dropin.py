@@ -72,8 +72,8 @@ def test_ppr_single_query_functions(mods, cl):
         x, r, oper, t = ppr.ppr_cheby(n, ip, ix, dg, s, ALPHA, eps, local)
         xc, _, oc = O.cheby(n, ip, ix, dg, s, ALPHA, eps, local, sync=True)
         assert oper == oc and np.abs(x - xc).sum() < 1e-10
-    xo, _, oo = O.ppr_gd(n, ip, ix, dg, s, ALPHA, eps, True)
-    for fn in (ppr.ppr_gd_local_gpu, ppr.ppr_gd_standard_gpu):
+    for fn, local in ((ppr.ppr_gd_local_gpu, True), (ppr.ppr_gd_standard_gpu, False)):
+        xo, _, oo = O.ppr_gd(n, ip, ix, dg, s, ALPHA, eps, local)
         x, r, oper, t = fn(n, ip, ix, dg, s, ALPHA, eps)
         assert x.dtype == np.float32 and np.abs(x.astype(np.float64) - xo).sum() < 1e-4
     col = colors_of(ip, ix, dg)
@@ -186,9 +186,9 @@ def test_katz_functions(mods, cl):
         x, r, oper, _ = katz.katz_gd(n, ip, ix, dg, s, alpha, eps, local)
         xo, ro, oo = O.katz_gd(n, ip, ix, dg, s, alpha, eps, local)
         assert oper == oo and np.abs(x - xo).sum() < 1e-11
-    for fn in (katz.katz_gd_local_gpu, katz.katz_gd_standard_gpu):
+    for fn, local in ((katz.katz_gd_local_gpu, True), (katz.katz_gd_standard_gpu, False)):
         x, _, _, _ = fn(n, ip, ix, dg, s, alpha, eps)
-        assert np.abs(x.astype(np.float64) - O.katz_gd(n, ip, ix, dg, s, alpha, eps, True)[0]).sum() < 1e-4
+        assert np.abs(x.astype(np.float64) - O.katz_gd(n, ip, ix, dg, s, alpha, eps, local)[0]).sum() < 1e-4
     l_max, mu_min, lam_max, lam_min = katz.katz_spectral_bounds(n, ip, ix, dg, alpha)
     assert lam_min < 0 < lam_max <= dg.max()
     x, _, oper, _ = katz.katz_cheby(n, ip, ix, dg, s, alpha, l_max, mu_min, eps, True)
