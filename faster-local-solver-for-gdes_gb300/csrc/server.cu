@@ -175,6 +175,7 @@ struct gde_server {
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
         cudaEventRecord(e0, stream);
+        launches++;  // launches started (gde_server_info)
         cudaError_t e = engine_launch(a, prec64, 1, grid, stream);
         cudaEventRecord(e1, stream);
         int herr = 0;
