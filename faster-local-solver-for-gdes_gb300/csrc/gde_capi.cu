@@ -230,7 +230,7 @@ int alloc_large(gde_ctx* ctx, gde_graph* G, int ntiles, TileWs& tw) {
 int run_engine(gde_ctx* ctx, PushArgs& a, int prec64, int W, gde_stats* st, double* kernel_ms) {
     int grid = engine_max_grid(prec64, W, ctx->sms);
     if (grid <= 0) return fail(ctx, GDE_ECUDA, "push kernel does not fit on the device");
-    CK(cudaMemsetAsync(ctx->bar, 0, sizeof(GridBarrier), ctx->stream));
+    CK(cudaMemsetAsync(ctx->bar, 0, kMaxGroups * sizeof(GridBarrier), ctx->stream));
     CK(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->stream));
     CK(cudaMemsetAsync(ctx->dstats, 0, sizeof(LaunchStats), ctx->stream));
     if (ctx->trace) {
@@ -410,6 +410,8 @@ int build_static_records(gde_ctx* ctx, gde_graph* G, const int32_t* col) {
 // kinds / alphas (may be null): a mixed queue of PPR, Katz and heat-kernel
 // queries, each slot taking the kind of the query it admits.
 // budget_bytes > 0 caps the slot count so the slots' vectors fit in it.
+constexpr int kDefaultGroups = 1;  // served slot groups when gde_params.groups is 0
+
 int64_t served_slot_bytes(int64_t n, int64_t cap, int prec64, bool hk, const PushArgs& tun) {
     const int64_t es = prec64 ? 8 : 4;
     const int64_t large_cap = cap / std::max(tun.chunk, 1) + cap / std::max(tun.med_max, 1) + 64;
@@ -446,6 +448,8 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     PushArgs& a = tw.a;
     a.small_max = base.small_max; a.med_max = base.med_max; a.chunk = base.chunk;
     a.dense_div = base.dense_div; a.max_rounds = base.max_rounds; a.allow_dense = base.allow_dense;
+    // independent slot groups, each behind its own barrier (at most one per slot)
+    a.groups = std::max(1, std::min(std::min(p->groups > 0 ? p->groups : kDefaultGroups, S), kMaxGroups));
     rc = alloc_large(ctx, G, S, tw);
     if (rc != GDE_OK) return rc;
     const size_t es = prec64 ? 8 : 4;
@@ -752,7 +756,7 @@ int gde_ctx_create(int device, gde_ctx** out) {
     cudaDeviceGetAttribute(&ctx->sms, cudaDevAttrMultiProcessorCount, device);
     if (!coop) { delete ctx; return GDE_ECUDA; }
     if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess ||
-        cudaMalloc(&ctx->bar, sizeof(GridBarrier)) != cudaSuccess ||
+        cudaMalloc(&ctx->bar, kMaxGroups * sizeof(GridBarrier)) != cudaSuccess ||
         cudaMalloc(&ctx->derr, sizeof(int)) != cudaSuccess ||
         cudaMalloc(&ctx->dstats, sizeof(LaunchStats)) != cudaSuccess ||
         cudaMallocHost(&ctx->hstats, sizeof(LaunchStats)) != cudaSuccess ||

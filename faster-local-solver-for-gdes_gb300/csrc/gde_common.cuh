@@ -299,7 +299,14 @@ struct PushArgs {
     unsigned long long* trace; // [trace_iters][grid][kTracePoints] %globaltimer stamps (nullptr: off)
     int trace_iters;
     unsigned long long spin_limit;  // grid-barrier polls before GDE_EHANG (0: the default, ~seconds)
+    // Served solves: the grid splits into `groups` block groups (blocks
+    // [g B / G, (g+1) B / G)), each advancing the slots t with t % G == g
+    // behind its own barrier bar[g], so a straggler stalls only its group.
+    // 0 or 1: one group (every other launch).
+    int groups;
 };
+
+constexpr int kMaxGroups = 64;
 
 // Phase boundaries stamped per block and launch iteration when tracing is on.
 enum TracePoint : int {

@@ -17,9 +17,12 @@ constexpr unsigned long long kSpinLimit = 1ull << 26;  // ~ seconds of polling
 __device__ __forceinline__ unsigned ld_volatile(const unsigned* p) { return *(volatile const unsigned*)p; }
 __device__ __forceinline__ int ld_volatile_i(const int* p) { return *(volatile const int*)p; }
 
-// `limit` polls (0: kSpinLimit) before a waiting block gives up.
-__device__ __forceinline__ bool grid_barrier(GridBarrier* bar, int* err, unsigned long long limit = 0) {
+// `limit` polls (0: kSpinLimit) before a waiting block gives up; `members`
+// blocks meet at `bar` (0: the whole grid).
+__device__ __forceinline__ bool grid_barrier(GridBarrier* bar, int* err, unsigned long long limit = 0,
+                                             unsigned members = 0) {
     if (limit == 0) limit = kSpinLimit;
+    if (members == 0) members = gridDim.x;
     __shared__ int s_ok;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -27,7 +30,7 @@ __device__ __forceinline__ bool grid_barrier(GridBarrier* bar, int* err, unsigne
         unsigned gen = ld_volatile(&bar->gen);
         __threadfence();
         unsigned arrived = atomicAdd(&bar->count, 1u);
-        if (arrived == gridDim.x - 1) {
+        if (arrived == members - 1) {
             atomicExch(&bar->count, 0u);
             __threadfence();
             atomicAdd(&bar->gen, 1u);

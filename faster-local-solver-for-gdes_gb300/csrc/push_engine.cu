@@ -435,10 +435,27 @@ __device__ __forceinline__ int find_tile(const long long* off, int ntl, long lon
 }
 
 
-// This block's share [lo, hi) of a flattened space of `total` items.
-__device__ __forceinline__ void block_share(long long total, long long& lo, long long& hi) {
-    lo = total * (long long)blockIdx.x / gridDim.x;
-    hi = total * (long long)(blockIdx.x + 1) / gridDim.x;
+// The block group this block belongs to (served launches with a.groups > 1
+// split the grid; every other launch is one group): group g holds blocks
+// [ceil(g B / G), ceil((g+1) B / G)).
+struct GroupInfo {
+    int id;   // group index
+    int blk;  // this block's index within the group
+    int dim;  // blocks in the group
+};
+__device__ __forceinline__ GroupInfo group_of(const PushArgs& a) {
+    const int G = a.groups > 1 ? a.groups : 1;
+    const long long B = gridDim.x;
+    const int g = (int)((long long)blockIdx.x * G / B);
+    const int start = (int)(((long long)g * B + G - 1) / G);
+    const int end = (int)(((long long)(g + 1) * B + G - 1) / G);
+    return GroupInfo{g, (int)blockIdx.x - start, end - start};
+}
+
+// This block's share [lo, hi) of a flattened space of `total` items (its group's blocks split it).
+__device__ __forceinline__ void block_share(long long total, long long& lo, long long& hi, const GroupInfo& gi) {
+    lo = total * (long long)gi.blk / gi.dim;
+    hi = total * (long long)(gi.blk + 1) / gi.dim;
 }
 
 // ---------------------------------------------------------------------------
@@ -1419,16 +1436,16 @@ __device__ void scatter_small_flat(const PushArgs& a, int t, const ScatterCtx<T,
 // HK: drop this level's sub-threshold residuals (hk_solver.py:284); the
 // frontier's own entries were already moved into x.
 template <typename T, int W>
-__device__ void hk_drop(const PushArgs& a, int t, int level, bool dense, int cand_cnt) {
+__device__ void hk_drop(const PushArgs& a, int t, int level, bool dense, int cand_cnt, const GroupInfo& gi) {
     const int64_t n = a.g.n;
     T* Rcur = slab_ptr<T>((level & 1) ? a.R2 : a.R, a, t);
-    const int64_t stride = (int64_t)gridDim.x * kThreads;
+    const int64_t stride = (int64_t)gi.dim * kThreads;
     if (dense) {
-        for (int64_t u = (int64_t)blockIdx.x * kThreads + threadIdx.x; u < n; u += stride)
+        for (int64_t u = (int64_t)gi.blk * kThreads + threadIdx.x; u < n; u += stride)
             for (int c = 0; c < W; ++c) Rcur[u * a.ld + c] = T(0);
     } else {
         const int32_t* cand = a.cand + ((int64_t)t * 2 + (level & 1)) * n;
-        for (int64_t i = (int64_t)blockIdx.x * kThreads + threadIdx.x; i < cand_cnt; i += stride) {
+        for (int64_t i = (int64_t)gi.blk * kThreads + threadIdx.x; i < cand_cnt; i += stride) {
             const int u = cand[i];
             for (int c = 0; c < W; ++c) Rcur[(int64_t)u * a.ld + c] = T(0);
         }
@@ -1518,14 +1535,33 @@ __device__ void admit_query(const PushArgs& a, int t, int it) {
     if (threadIdx.x != 0) return;
     TileState& ts = a.ts[t];
     const ServeQueue& q = a.queue;
-    const int qid = *q.next;
-    if (qid >= q.nq) {
-        ts.done = SLOT_EMPTY;
-        return;
-    }
+    // the next query in order; group leaders take queries concurrently
     const unsigned long long now = globaltimer_ns();
-    if (q.arrival_ns && now < a.stats->start_ns + (unsigned long long)q.arrival_ns[qid]) return;
-    *q.next = qid + 1;
+    int qid = -1;
+    if (q.arrival_ns) {
+        // block 0 stamps the launch start; other groups may get here first
+        const unsigned long long st0 = *(volatile const unsigned long long*)&a.stats->start_ns;
+        if (st0 == 0) return;
+        for (int tries = 0; tries < 4096; ++tries) {
+            const int c = ld_volatile_i(q.next);
+            if (c >= q.nq) {
+                ts.done = SLOT_EMPTY;
+                return;
+            }
+            if (now < st0 + (unsigned long long)q.arrival_ns[c]) return;  // not arrived yet
+            if (atomicCAS(q.next, c, c + 1) == c) {
+                qid = c;
+                break;
+            }
+        }
+        if (qid < 0) return;  // another leader kept winning: try next round
+    } else {
+        qid = atomicAdd(q.next, 1);
+        if (qid >= q.nq) {
+            ts.done = SLOT_EMPTY;
+            return;
+        }
+    }
     const int64_t n = a.g.n;
     const int seed = q.seed[qid];
     // stamps must keep growing within the slot: skip past the last query's
@@ -1783,6 +1819,8 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
     }
     int it = 0;
     const bool online = a.serve && a.queue.online;
+    const GroupInfo gi = group_of(a);
+    const int G = a.groups > 1 ? a.groups : 1;
     if (online && blockIdx.x == 0 && threadIdx.x == 0) *a.queue.last_ns = globaltimer_ns();
     for (; it < a.round_budget; ++it) {
         // online server: block 0 decided to stop (stop flag, or idle) last round
@@ -1793,10 +1831,11 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
         __syncthreads();
         for (int t = threadIdx.x; t < a.ntiles; t += kThreads) {
             const TileState& ts = a.ts[t];
-            const bool live = ts.done == SLOT_LIVE && it >= ts.t0 && (it - ts.t0) < a.max_rounds;
+            const bool mine = (t % G) == gi.id;  // this group's slots
+            const bool live = mine && ts.done == SLOT_LIVE && it >= ts.t0 && (it - ts.t0) < a.max_rounds;
             s_vals[t] = live ? 1 : 0;
-            rs.idle[t] = (ts.done == SLOT_IDLE) ? 1 : (ts.done == SLOT_DRAIN ? 2 : 0);
-            if (ts.done == SLOT_IDLE) rs.any_idle = 1;
+            rs.idle[t] = !mine ? 0 : (ts.done == SLOT_IDLE) ? 1 : (ts.done == SLOT_DRAIN ? 2 : 0);
+            if (mine && ts.done == SLOT_IDLE) rs.any_idle = 1;
         }
         if (online) {
             // drained slots in ascending order: the same list in every block
@@ -1836,7 +1875,7 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
                 if (m != M_GLOBAL_GD && m != M_GLOBAL_CHEBY) continue;
                 check_phase<T, W>(a, t, it, s_cnt);
             }
-            if (!grid_barrier(a.bar, a.err, a.spin_limit)) return;
+            if (!grid_barrier(a.bar + gi.id, a.err, a.spin_limit, gi.dim)) return;
             if (timer) {
                 unsigned long long t1 = globaltimer_ns();
                 a.stats->check_ns += t1 - t0;
@@ -1844,7 +1883,7 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
             }
         }
         // ---- PREP: flattened candidates of all live tiles ----
-        if (blockIdx.x == 0) {
+        if (gi.blk == 0) {
             for (int k = 0; k < ntl; ++k) zero_next_counters<W>(a, rs.tiles[k], rs.level[k]);
         }
         for (int k = threadIdx.x; k < ntl; k += kThreads) {
@@ -1857,7 +1896,7 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
         trace_point(a, it, TP_PREP_WORK);
         {
             long long lo, hi;
-            block_share(rs.off[0][ntl], lo, hi);
+            block_share(rs.off[0][ntl], lo, hi, gi);
             if (lo < hi) {
                 for (int k = find_tile(rs.off[0], ntl, lo); k < ntl && rs.off[0][k] < hi; ++k) {
                     const long long b = max(lo, rs.off[0][k]) - rs.off[0][k];
@@ -1869,7 +1908,7 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
             }
         }
         trace_point(a, it, TP_PREP_DONE);
-        if (!grid_barrier(a.bar, a.err, a.spin_limit)) return;
+        if (!grid_barrier(a.bar + gi.id, a.err, a.spin_limit, gi.dim)) return;
         trace_point(a, it, TP_PREP_BAR);
         if (timer) {
             unsigned long long t1 = globaltimer_ns();
@@ -1925,7 +1964,7 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
             __syncthreads();
             block_exclusive_scan(s_vals, ntl, rs.off[3], rs.scan_tmp);
             long long lo, hi;
-            block_share(rs.off[3][ntl], lo, hi);
+            block_share(rs.off[3][ntl], lo, hi, gi);
             if (lo < hi) {
                 for (int k = find_tile(rs.off[3], ntl, lo); k < ntl && rs.off[3][k] < hi; ++k) {
                     const long long b = max(lo, rs.off[3][k]) - rs.off[3][k];
@@ -1937,7 +1976,7 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
             }
             // online slots drained last round: every block an equal share of their nodes
             if (online && rs.ndrain > 0) {
-                block_share((long long)rs.ndrain * n, lo, hi);
+                block_share((long long)rs.ndrain * n, lo, hi, gi);
                 for (long long x = lo; x < hi;) {
                     const long long k = x / n;
                     const long long e = min(hi, (k + 1) * n);
@@ -1951,7 +1990,7 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
         for (int sp = 2; sp >= 0; --sp) {
             const long long* off = rs.off[sp];
             long long lo, hi;
-            block_share(off[ntl], lo, hi);
+            block_share(off[ntl], lo, hi, gi);
             if (lo >= hi) continue;
             for (int k = find_tile(off, ntl, lo); k < ntl && off[k] < hi; ++k) {
                 const long long b = max(lo, off[k]) - off[k];
@@ -1978,10 +2017,10 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
             const int lv = rs.level[k];
             const TileState& ts = a.ts[t];
             if (ts.front_cnt[lv & 1] == 0) continue;
-            hk_drop<T, W>(a, t, lv, ts.dense_next[lv & 1] != 0, ts.cand_cnt[lv % 3]);
+            hk_drop<T, W>(a, t, lv, ts.dense_next[lv & 1] != 0, ts.cand_cnt[lv % 3], gi);
         }
         bool admitted = false;
-        if (blockIdx.x == 0 && online) {
+        if (gi.blk == 0 && online) {
             if (threadIdx.x == 0) {
                 for (int k = 0; k < rs.ndrain; ++k) {
                     publish_online(a, rs.drain[k]);
@@ -1991,11 +2030,11 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
                     for (int t = 0; t < a.ntiles; ++t)
                         if (rs.idle[t] == 1 && admit_online<T, W>(a, t, it)) admitted = true;
             }
-        } else if (blockIdx.x == 0 && a.serve && rs.any_idle) {
+        } else if (gi.blk == 0 && a.serve && rs.any_idle) {
             for (int t = 0; t < a.ntiles; ++t)
                 if (rs.idle[t] == 1) admit_query<T, W>(a, t, it);
         }
-        if (blockIdx.x == 0) {
+        if (gi.blk == 0) {
             finish_columns_all<W>(a, rs, ntl);
             __syncthreads();
             for (int k = threadIdx.x; k < ntl; k += kThreads) {
@@ -2029,13 +2068,13 @@ __global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN
             }
         }
         trace_point(a, it, TP_SCAT_ENTER);
-        if (!grid_barrier(a.bar, a.err, a.spin_limit)) return;
+        if (!grid_barrier(a.bar + gi.id, a.err, a.spin_limit, gi.dim)) return;
         trace_point(a, it, TP_SCAT_BAR);
         if (timer) a.stats->scatter_ns += globaltimer_ns() - t0;
     }
     // A tile still SLOT_LIVE after the launch stopped at max_rounds (the host
     // reports GDE_EITERCAP for it).
-    if (blockIdx.x == 0 && threadIdx.x == 0) a.stats->iters = (unsigned long long)it;
+    if (gi.blk == 0 && threadIdx.x == 0) atomicMax(&a.stats->iters, (unsigned long long)it);
     if (threadIdx.x == 0 && ps.acc_union_nodes) {
         atomicAdd(&a.stats->col_nodes, ps.acc_col_nodes);
         atomicAdd(&a.stats->col_vol, ps.acc_col_vol);

@@ -28,7 +28,7 @@ class Params(ctypes.Structure):
     _fields_ = [("kind", _int), ("method", _int), ("prec", _int), ("tile_w", _int),
                 ("alpha", _dbl), ("tau", _dbl), ("l_max", _dbl), ("mu_min", _dbl), ("beta", _dbl), ("omega", _dbl),
                 ("max_rounds", _int), ("small_max", _int), ("med_max", _int), ("chunk", _int), ("dense_div", _int),
-                ("slots", _int)]
+                ("slots", _int), ("groups", _int)]
 
 
 class Stats(ctypes.Structure):

@@ -95,6 +95,7 @@ def make_params(kind: int, method: int, prec: str = "fp64", tile_w: int = 0, alp
     p.chunk = int(t.get("chunk", 0))
     p.dense_div = int(t.get("dense_div", 0))
     p.slots = int(t.get("slots", 0))
+    p.groups = int(t.get("groups", 0))
     return p
 
 

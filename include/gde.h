@@ -75,6 +75,8 @@ typedef struct {
     int chunk;         /* edges per CTA chunk; 0 = default */
     int dense_div;     /* next round scans all nodes when vol(frontier) > n/dense_div; 0 = default */
     int slots;         /* served PPR/Katz local GD: concurrent queries (one residual vector each); 0 = default */
+    int groups;        /* served: the grid splits into this many block groups, each advancing its own slots
+                          (t % groups) behind its own barrier; 0 = default */
 } gde_params;
 
 typedef struct {

@@ -166,3 +166,27 @@ def test_served_rows_into_pinned_host_memory(cl):
     np.testing.assert_allclose(a["oper"], b["oper"], rtol=1e-3)
     for i in range(12):
         assert rel_l1(pinned[i].numpy(), b["x"][i].astype(np.float64)) < 1e-5, i
+
+
+@pytest.mark.parametrize("arrivals", [False, True])
+@pytest.mark.parametrize("groups", [2, 4])
+def test_slot_groups_give_the_same_results(cl, groups, arrivals):
+    """Slots split over block groups with their own barriers: every query still equals the query alone."""
+    g, Gd = cl
+    seeds, eps, arrival = mix(g, 40, 11)
+    served = api.serve(Gd, L.PPR, seeds, eps, arrival_ms=arrival if arrivals else None, prec="fp64", alpha=0.1,
+                       slots=8, tuning={"groups": groups})
+    one = api.serve(Gd, L.PPR, seeds, eps, prec="fp64", alpha=0.1, slots=8, tuning={"groups": 1})
+    np.testing.assert_allclose(served["oper"], one["oper"], rtol=1e-12)
+    np.testing.assert_array_equal(served["rounds"], one["rounds"])
+    for i in range(len(seeds)):
+        assert rel_l1(served["x"][i], one["x"][i]) < FP64_L1, i
+    mixed = api.serve_mixed(Gd, [L.PPR, L.KATZ, L.HK] * 8, seeds[:24], eps[:24],
+                            alphas=[0.1, 1.0 / (float(g.degree.max()) + 1.0), 0.0] * 8, tau=5.0, prec="fp64",
+                            slots=6, tuning={"groups": groups})
+    ref = api.serve_mixed(Gd, [L.PPR, L.KATZ, L.HK] * 8, seeds[:24], eps[:24],
+                          alphas=[0.1, 1.0 / (float(g.degree.max()) + 1.0), 0.0] * 8, tau=5.0, prec="fp64",
+                          slots=6, tuning={"groups": 1})
+    np.testing.assert_allclose(mixed["oper"], ref["oper"], rtol=1e-12)
+    for i in range(24):
+        assert rel_l1(mixed["x"][i], ref["x"][i]) < FP64_L1, i
