@@ -50,9 +50,11 @@ def parse():
     ap.add_argument("--steps", type=int, default=5)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--batch", type=int, default=512, help="queries per step")
+    ap.add_argument("--batch", type=int, default=1024, help="queries per step")
     ap.add_argument("--tile-w", type=int, default=1, help="1 = served slots (continuous batching)")
-    ap.add_argument("--slots", type=int, default=32, help="concurrent queries of the served engine")
+    ap.add_argument("--slots", type=int, default=64,
+                    help="concurrent queries of the served engine (each slot advances behind its own block "
+                         "group's barrier; --tuning groups=G to share groups)")
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--plain-queries", type=int, default=32)
     ap.add_argument("--cpu-queries", type=int, default=0, help="CPU-baseline sample (0 = 2 per host thread)")

@@ -306,7 +306,7 @@ struct PushArgs {
     int groups;
 };
 
-constexpr int kMaxGroups = 64;
+constexpr int kMaxGroups = 512;  // at most one per slot (kMaxLaunchTiles)
 
 // Phase boundaries stamped per block and launch iteration when tracing is on.
 enum TracePoint : int {

@@ -76,7 +76,7 @@ typedef struct {
     int dense_div;     /* next round scans all nodes when vol(frontier) > n/dense_div; 0 = default */
     int slots;         /* served PPR/Katz local GD: concurrent queries (one residual vector each); 0 = default */
     int groups;        /* served: the grid splits into this many block groups, each advancing its own slots
-                          (t % groups) behind its own barrier; 0 = default */
+                          (t % groups) behind its own barrier; 0 = default (one group per slot) */
 } gde_params;
 
 typedef struct {
