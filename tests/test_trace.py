@@ -15,14 +15,18 @@ pytestmark = pytest.mark.gpu
 TICK_NS = 2_000  # slack for %globaltimer granularity across SMs
 
 
-def test_trace_timeline_is_ordered_and_barriers_hold():
+@pytest.mark.parametrize("groups", [1, 8])
+def test_trace_timeline_is_ordered_and_barriers_hold(groups):
+    """One block group: the barrier holds over the whole grid.  Eight groups (one per served slot, the
+    default for 8 queries): it holds within each group, blocks [ceil(g B / 8), ceil((g+1) B / 8))."""
     g = graphs.chung_lu(3000, 2.1, 8.0, 300.0, seed=3)
     Gd = api.Graph(g.indptr, g.indices)
     seeds = graphs.uniform_seeds(g, 8, seed=5)
-    ref = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, 1e-6, prec="fp64", alpha=0.1)
+    tun = {"groups": groups}
+    ref = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, 1e-6, prec="fp64", alpha=0.1, tuning=tun)
     api.trace(6)
     try:
-        res = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, 1e-6, prec="fp64", alpha=0.1)
+        res = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, 1e-6, prec="fp64", alpha=0.1, tuning=tun)
         tr = api.trace_read()
     finally:
         api.trace(0)
@@ -37,11 +41,14 @@ def test_trace_timeline_is_ordered_and_barriers_hold():
     assert (np.diff(t, axis=2) >= 0).all()
     # iterations follow one another
     assert (t[1:, :, 0] >= t[:-1, :, 7]).all()
-    # barriers: every block leaves after the last block entered
-    for enter, leave in ((2, 3), (6, 7)):
-        last_in = t[:, :, enter].max(axis=1)
-        first_out = t[:, :, leave].min(axis=1)
-        assert (first_out + TICK_NS >= last_in).all()
+    # barriers: every block of a group leaves after the last block of the group entered
+    member = (np.arange(grid) * groups) // grid
+    for grp in range(groups):
+        tg = t[:, member == grp, :]
+        for enter, leave in ((2, 3), (6, 7)):
+            last_in = tg[:, :, enter].max(axis=1)
+            first_out = tg[:, :, leave].min(axis=1)
+            assert (first_out + TICK_NS >= last_in).all(), grp
     assert api.trace_read().size == 0
 
 
