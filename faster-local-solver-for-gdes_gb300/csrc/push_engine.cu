@@ -35,15 +35,23 @@ namespace {
 // trade a few spilled bytes for a fourth block per SM: their memory-latency-
 // bound phases gain more from the extra warps (served PPR +3 to +7%, the
 // 8-column InstantGNN push +4%) than the spills cost; 16- and 32-column and
-// FP64 kernels spill more and keep three.
+// FP64 kernels spill more and keep three.  The one-column FP32 kernel (the
+// served slots) runs five blocks per SM with two edges in flight per lane:
+// with a barrier per slot group, more resident warps each with fewer
+// outstanding atomics beat fewer warps with more (2,647 -> 2,740-2,800
+// queries/s on the 2.36M-node workload; four edges per lane at five or six
+// blocks, or one or two at seven blocks with their spills, measured slower).
 #ifndef GDE_MIN_BLOCKS
 #define GDE_MIN_BLOCKS 3
 #endif
 #ifndef GDE_MIN_BLOCKS_F32
 #define GDE_MIN_BLOCKS_F32 4
 #endif
+#ifndef GDE_MIN_BLOCKS_W1
+#define GDE_MIN_BLOCKS_W1 5
+#endif
 #ifndef GDE_EDGE_ILP
-#define GDE_EDGE_ILP 4
+#define GDE_EDGE_ILP 2
 #endif
 
 constexpr int kThreads = 256;
@@ -1804,7 +1812,9 @@ __device__ __forceinline__ void trace_point(const PushArgs& a, int it, int k) {
 }
 
 template <typename T, int W>
-__global__ void __launch_bounds__(kThreads, (W <= 8 && sizeof(T) == 4) ? GDE_MIN_BLOCKS_F32 : GDE_MIN_BLOCKS)
+__global__ void __launch_bounds__(kThreads, (W == 1 && sizeof(T) == 4)   ? GDE_MIN_BLOCKS_W1
+                                           : (W <= 8 && sizeof(T) == 4) ? GDE_MIN_BLOCKS_F32
+                                                                        : GDE_MIN_BLOCKS)
     push_kernel(PushArgs a) {
     __shared__ TileSh sh;
     __shared__ PrepSh ps;
