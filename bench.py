@@ -60,8 +60,10 @@ def parse():
     ap.add_argument("--cpu-queries", type=int, default=0, help="CPU-baseline sample (0 = 2 per host thread)")
     ap.add_argument("--no-baselines", action="store_true")
     ap.add_argument("--tuning", default="", help="k=v,... engine tuning overrides")
-    ap.add_argument("--workload", default="c2", choices=["c2", "c3", "c4", "c5"],
-                    help="c2: served PPR on the 2.36M graph (the headline); c3: 1,024 seeds per launch with "
+    ap.add_argument("--workload", default="c2", choices=["c1", "c2", "c2arms", "c3", "c4", "c5"],
+                    help="c1: FP64 local GD, 50 seeds on the 100k graph, checked against a global solve; "
+                         "c2arms: local GD and local Chebyshev in FP64 and FP32 on the 2.36M graph; "
+                         "c2: served PPR on the 2.36M graph (the headline); c3: 1,024 seeds per launch with "
                          "per-seed eps on the 100k graph; c4: served PPR/Katz/heat-kernel mix with Poisson "
                          "arrivals on R-MAT scale 22; c5: InstantGNN 128-column snapshot updates")
     ap.add_argument("--edit", default="insert", choices=["insert", "mixed"],
@@ -923,10 +925,166 @@ def c5_oracle_check(dyn, X, batches, mixed, snapP, outs, beta, eps):
     return {"accuracy": acc, "cpu_baseline": cpu}
 
 
+def run_c1(args):
+    """C1: PPR local GD in FP64 on the 100k-node Chung-Lu graph, 50 seeds at eps = 1e-6, checked against the
+    oracle (operation counts exactly) and, for two seeds, against an FP64 global solve."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from gde import _lib as L
+    from gde import api, graphs
+    from oracle import oracle as O
+    g = graphs.chung_lu_100k()
+    ctx = api.Context.get(local)
+    G = api.Graph(g.indptr, g.indices, ctx=ctx)
+    Q, alpha, eps = 50, 0.1, 1e-6
+    deg = g.degree.astype(np.float64)
+    stream = torch.cuda.ExternalStream(api.ctx_stream(ctx), device=f"cuda:{local}")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    x_dev = torch.empty((Q, g.n), dtype=torch.float64, device=f"cuda:{local}")
+    r_dev = torch.empty((Q, g.n), dtype=torch.float64, device=f"cuda:{local}")
+
+    def step(k, x_out=None, r_out=None, device_out=True):
+        seeds = graphs.uniform_seeds(g, Q, seed=1 + 1000 * k)
+        return api.solve(G, L.PPR, L.LOCAL_GD, seeds, eps, prec="fp64", alpha=alpha, tile_w=1,
+                         x_out=x_dev if x_out is None else x_out, r_out=r_dev if r_out is None else r_out,
+                         device_out=device_out)
+
+    for w in range(args.warmup):
+        step(10 + w)
+    with ClockSampler(local) as clk:
+        times, outs = _timed_steps(stream, flush, args.steps, lambda k: step(k))
+    value = Q * len(times) * world / (sum(times) / 1e3)
+    agg = {k: sum(o["stats"][k] for o in outs) for k in ("union_vol", "col_vol", "col_nodes", "kernel_ms")}
+    # FP64: 4 B col_idx + 16 B residual RMW per edge, 48 B per active node
+    achieved = (4 * agg["union_vol"] + 16 * agg["col_vol"] + 48 * agg["col_nodes"]) / (agg["kernel_ms"] / 1e3) / 1e9
+    peak, peak_kind = measured_peak()
+    x_host = torch.empty((Q, g.n), dtype=torch.float64).pin_memory()
+    e2e, _ = _timed_steps(stream, flush, max(1, args.e2e_steps), lambda k: step(200 + k, x_host, None, False))
+    out = {
+        "metric": "PPR local GD queries/s, FP64, eps = 1e-6, 50 seeds, Chung-Lu 100k",
+        "value": value, "unit": "queries/s", "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": sum(times) / len(times), "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "ppr_local_gd_fp64_50_seeds_chung_lu_100k", "n": g.n, "nnz": g.nnz,
+                   "queries_per_step": Q, "alpha": alpha, "eps": eps, "l2": "512 MB buffer written between steps"},
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_kind": peak_kind, "traffic": None},
+        "e2e": {"value": Q * len(e2e) / (sum(e2e) / 1e3), "unit": "queries/s", "h2d_bytes_per_step": Q * 12,
+                "d2h_bytes_per_step": Q * g.n * 8},
+        "gpu_launches": args.steps, "clocks": clk.summary(),
+    }
+    if not args.no_baselines:
+        seeds = graphs.uniform_seeds(g, Q, seed=1 + 1000 * (args.steps - 1))
+        threads = O.threads()
+        t0 = time.perf_counter()
+        oo, xo = O.ppr_gd_many(g.n, g.indptr, g.indices, deg, seeds, alpha, eps, keep_x=True, nthreads=threads)
+        dt = time.perf_counter() - t0
+        xg = x_dev.cpu().numpy()
+        rg = r_dev.cpu().numpy()
+        og = outs[-1]["oper"]
+        truth = []
+        for i in range(2):
+            t_ = O.global_solve_ppr(g.indptr, g.indices, deg, int(seeds[i]), alpha)
+            truth.append({"l1": float(np.abs(xg[i] - t_).sum()), "oracle_l1": float(np.abs(xo[i] - t_).sum()),
+                          "max_r_over_d": float(np.max(np.abs(rg[i]) / deg))})
+        out["accuracy"] = {"vs": "FP64 oracle (C port of ppr_gd local)", "queries": Q,
+                           "oper_mismatches": int(np.sum(np.rint(og).astype(np.int64) != oo)),
+                           "rel_l1_max": float((np.abs(xg - xo).sum(1) / np.abs(xo).sum(1)).max()),
+                           "truth": {"vs": "FP64 global solve to 1e-15 (scipy)", "rows": truth,
+                                     "stop_rule": eps * alpha}}
+        out["cpu_baseline"] = {"value": Q / dt, "unit": "queries/s", "cores": threads, "kind": "port",
+                               "sample": f"the step's 50 queries (ppr_gd local FP64, one per OpenMP thread), "
+                                         f"{dt:.2f} s"}
+    print(json.dumps(out), flush=True)
+
+
+def run_c2_arms(args):
+    """C2's four GPU arms on the 2.36M-node graph, 50 seeds at eps = 1e-7: local GD and local Chebyshev, each in
+    FP64 and in FP32 residuals, beside the plain single-query kernel and the CPU ports."""
+    import torch
+    rank, world, local = dist_env()
+    torch.cuda.set_device(local)
+    from gde import _lib as L
+    from gde import api, graphs
+    from oracle import oracle as O
+    g = graphs.chung_lu_wikitalk_shape()
+    ctx = api.Context.get(local)
+    G = api.Graph(g.indptr, g.indices, ctx=ctx)
+    Q = 50
+    deg = g.degree.astype(np.float64)
+    seeds = graphs.uniform_seeds(g, Q, seed=50)
+    stream = torch.cuda.ExternalStream(api.ctx_stream(ctx), device=f"cuda:{local}")
+    flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
+    arms = []
+    with ClockSampler(local) as clk:
+        for method, mname in ((L.LOCAL_GD, "local_gd"), (L.LOCAL_CHEBY, "local_cheby")):
+            for prec in ("fp64", "fp32"):
+                def fn(k, method=method, prec=prec):
+                    return api.solve(G, L.PPR, method, seeds, EPS, prec=prec, alpha=ALPHA, want_r=False,
+                                     device_out=True)
+                fn(0)
+                times, outs = _timed_steps(stream, flush, max(1, args.steps // 2), fn)
+                arms.append({"method": mname, "prec": prec, "queries_per_s": Q * len(times) / (sum(times) / 1e3),
+                             "ms_per_step": sum(times) / len(times), "mean_oper": float(outs[-1]["oper"].mean()),
+                             "x": outs[-1]["x"], "oper": outs[-1]["oper"]})
+    xs = torch.zeros(g.n, dtype=torch.float32, device=f"cuda:{local}")
+    api.plain_ppr_local(G, int(seeds[0]), ALPHA, EPS, x_out=xs)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for s in seeds[:16]:
+        api.plain_ppr_local(G, int(s), ALPHA, EPS, x_out=xs)
+    torch.cuda.synchronize()
+    plain = 16 / (time.perf_counter() - t0)
+    # FP64 oracle on 8 of the seeds: GD exactly, Chebyshev in the GPU's synchronous order
+    k = 8
+    threads = O.threads()
+    t0 = time.perf_counter()
+    oo, xo = O.ppr_gd_many(g.n, g.indptr, g.indices, deg, seeds[:k], ALPHA, EPS, keep_x=True, nthreads=threads)
+    gd_cpu = k / (time.perf_counter() - t0)
+    from concurrent.futures import ThreadPoolExecutor
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        che = list(ex.map(lambda s: O.cheby(g.n, g.indptr, g.indices, deg, int(s), ALPHA, EPS, True, sync=True),
+                          seeds[:k]))
+    ch_cpu = k / (time.perf_counter() - t0)
+    for a in arms:
+        x = a.pop("x")[:k].double().cpu().numpy()
+        oper = a.pop("oper")[:k]
+        if a["method"] == "local_gd":
+            ref_x, ref_o = xo, oo.astype(np.float64)
+        else:
+            ref_x = np.stack([c[0] for c in che])
+            ref_o = np.array([c[2] for c in che], np.float64)
+        l1 = np.abs(x - ref_x).sum(1)
+        a["accuracy"] = {"queries": k, "l1_max": float(l1.max()),
+                         "rel_l1_max": float((l1 / np.abs(ref_x).sum(1)).max()),
+                         "oper_rel_diff_max": float((np.abs(oper - ref_o) / ref_o).max())}
+    best = arms[1]  # FP32 local GD
+    out = {
+        "metric": "PPR local GD / local Chebyshev queries/s, FP64 and FP32, eps = 1e-7, 50 seeds, Chung-Lu 2.36M",
+        "value": best["queries_per_s"], "unit": "queries/s", "n_gpus": 1, "steps": max(1, args.steps // 2),
+        "warmup": 1, "ms_per_step": best["ms_per_step"], "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": {"workload": "ppr_local_gd_cheby_fp64_fp32_50_seeds_chung_lu_2.36M", "n": g.n, "nnz": g.nnz,
+                   "queries_per_step": Q, "alpha": ALPHA, "eps": EPS, "value_arm": "local_gd fp32"},
+        "arms": arms, "plain_gpu": {"value": plain, "unit": "queries/s", "sample": "16 queries"},
+        "cpu_baseline": {"value": gd_cpu, "unit": "queries/s", "cores": threads, "kind": "port",
+                         "sample": f"{k} of the seeds, ppr_gd local FP64, one per thread; local Chebyshev "
+                                   f"(synchronous order) {ch_cpu:.1f} q/s"},
+        "gpu_launches": 4 * max(1, args.steps // 2), "clocks": clk.summary(),
+    }
+    print(json.dumps(out), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "c1":
+        run_c1(args)
+    elif args.workload == "c2arms":
+        run_c2_arms(args)
     elif args.workload == "c3":
         run_c3(args)
     elif args.workload == "c4":

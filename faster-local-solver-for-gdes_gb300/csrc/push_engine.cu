@@ -50,6 +50,9 @@ namespace {
 #ifndef GDE_MIN_BLOCKS_W1
 #define GDE_MIN_BLOCKS_W1 5
 #endif
+#ifndef GDE_VEC_COLS
+#define GDE_VEC_COLS 0  // 1: 128-bit column-word loads for rows of 128 edges and more (W = 1)
+#endif
 #ifndef GDE_EDGE_ILP
 #define GDE_EDGE_ILP 2
 #endif
@@ -1259,6 +1262,57 @@ __device__ void scatter_warp_items_w1(const PushArgs& a, const PushItem* items, 
         T p[kEdgeILP];
 #pragma unroll
         for (int u = 0; u < kEdgeILP; ++u) p[u] = pv;
+#if GDE_VEC_COLS
+        // 128-bit column loads: the row's first 16-byte boundary, then each
+        // lane takes 4 consecutive column words with one load and pushes them
+        // kEdgeILP at a time
+        static_assert(4 % kEdgeILP == 0, "4 column words per lane split into kEdgeILP-edge steps");
+        if (a.g.col_deg && it.len >= 128) {
+            const int head = (int)((4 - (it.rp & 3)) & 3);
+            {
+                bool ok[kEdgeILP];
+                int v[kEdgeILP];
+                uint32_t dc[kEdgeILP];
+#pragma unroll
+                for (int u = 0; u < kEdgeILP; ++u) {
+                    ok[u] = (u == 0) && lane < head;
+                    v[u] = 0;
+                    dc[u] = 0;
+                    if (ok[u]) load_edge(a.g, it.rp + lane, v[u], dc[u]);
+                }
+                edges_w1<T>(a, c, ok, v, dc, p, theta, none, none);
+            }
+            const uint32_t* body = a.g.col_deg + it.rp + head;  // 16-byte aligned
+            const int nb = it.len - head;
+            const uint32_t mask = (1u << a.g.idx_bits) - 1u;
+            for (int b0 = 0; b0 < nb; b0 += 128) {
+                const int e = b0 + 4 * lane;
+                uint32_t w[4] = {0u, 0u, 0u, 0u};
+                if (e + 3 < nb) {
+                    const uint4 q = *reinterpret_cast<const uint4*>(body + e);
+                    w[0] = q.x; w[1] = q.y; w[2] = q.z; w[3] = q.w;
+                } else {
+#pragma unroll
+                    for (int i = 0; i < 4; ++i)
+                        if (e + i < nb) w[i] = body[e + i];
+                }
+#pragma unroll
+                for (int h = 0; h < 4; h += kEdgeILP) {
+                    bool ok[kEdgeILP];
+                    int v[kEdgeILP];
+                    uint32_t dc[kEdgeILP];
+#pragma unroll
+                    for (int u = 0; u < kEdgeILP; ++u) {
+                        ok[u] = e + h + u < nb;
+                        v[u] = (int)(w[h + u] & mask);
+                        dc[u] = w[h + u] >> a.g.idx_bits;
+                    }
+                    edges_w1<T>(a, c, ok, v, dc, p, theta, none, none);
+                }
+            }
+            continue;
+        }
+#endif
         for (int j0 = 0; j0 < it.len; j0 += 32 * kEdgeILP) {
             bool ok[kEdgeILP];
             int v[kEdgeILP];
