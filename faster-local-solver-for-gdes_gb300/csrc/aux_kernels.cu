@@ -33,7 +33,13 @@ __global__ void init_columns_kernel(PushArgs a, const InitCol* cols, int ncols, 
     const int stamp = a.ts[ic.tile].stamp;
     const int64_t so = (int64_t)ic.seed * a.ld + ic.col;
     if (lane == 0) {
-        R[so] = (T)ic.r0;
+        // served FP32 PPR / Katz local GD slots keep the hub prefix's residual in FP64
+        const TileParams& tp = a.tp[ic.tile];
+        const bool crosses = tp.method == M_LOCAL_GD && (tp.kind == KIND_PPR || tp.kind == KIND_KATZ);
+        if (sizeof(T) == 4 && a.RH && crosses && ic.seed < a.rh_cut)
+            a.RH[(int64_t)ic.tile * a.rh_cut + ic.seed] = ic.r0;
+        else
+            R[so] = (T)ic.r0;
         if (ic.x0 != 0.0) X[(int64_t)ic.seed * xld + ic.col] = (T)ic.x0;
         if (DX && ic.dx0 != 0.0) DX[so] = (T)ic.dx0;
     }

@@ -412,11 +412,15 @@ int build_static_records(gde_ctx* ctx, gde_graph* G, const int32_t* col) {
 // queries, each slot taking the kind of the query it admits.
 // budget_bytes > 0 caps the slot count so the slots' vectors fit in it.
 
+// Served FP32 slots keep the residual of at most this many highest-degree
+// nodes in FP64 (the graph's hub prefix: rows longer than kHubLen).
+constexpr int64_t kRhMax = 1 << 16;
+
 int64_t served_slot_bytes(int64_t n, int64_t cap, int prec64, bool hk, const PushArgs& tun) {
     const int64_t es = prec64 ? 8 : 4;
     const int64_t large_cap = cap / std::max(tun.chunk, 1) + cap / std::max(tun.med_max, 1) + 64;
-    return n * es * (3 + (hk ? 1 : 0)) + (prec64 ? 0 : n * 4) + n * 4 * 3 + n * (int64_t)sizeof(PushItem) +
-           large_cap * (int64_t)sizeof(PushItem);
+    return n * es * (3 + (hk ? 1 : 0)) + (prec64 ? 0 : n * 4 + kRhMax * 8) + n * 4 * 3 +
+           n * (int64_t)sizeof(PushItem) + large_cap * (int64_t)sizeof(PushItem);
 }
 
 int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, const int32_t* seeds,
@@ -479,8 +483,17 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
             }
         }
     }
+    // FP32 PPR / Katz slots: the residual of the highest-degree nodes in FP64
+    a.RH = nullptr;
+    a.rh_cut = 0;
+    if (!prec64 && G->g.hub_cut > 0) {
+        a.rh_cut = (int)std::min<int64_t>(G->g.hub_cut, kRhMax);
+        a.RH = (double*)wsget(ctx, "RH", (size_t)S * a.rh_cut * 8);
+        if (!a.RH) return fail(ctx, GDE_ENOMEM, "device memory exhausted (FP64 hub residuals)");
+    }
     CK(cudaEventRecord(ctx->ev[2], ctx->stream));
     CK(cudaMemsetAsync(a.R, 0, slab, ctx->stream));
+    if (a.RH) CK(cudaMemsetAsync(a.RH, 0, (size_t)S * a.rh_cut * 8, ctx->stream));
     if (a.xq) CK(cudaMemsetAsync(a.X, 0, (size_t)nq * (size_t)a.xtile * 4, ctx->stream));
     else CK(cudaMemsetAsync(a.X, 0, a.xld ? 2 * slab : slab, ctx->stream));  // interleaved: X and XC
     if (a.R2) CK(cudaMemsetAsync(a.R2, 0, slab, ctx->stream));

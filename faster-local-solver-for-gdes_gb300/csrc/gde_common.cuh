@@ -304,6 +304,13 @@ struct PushArgs {
     // behind its own barrier bar[g], so a straggler stalls only its group.
     // 0 or 1: one group (every other launch).
     int groups;
+    // Served one-column FP32 slots of PPR / Katz local GD: the residual of the
+    // highest-degree nodes (internal ids < rh_cut of a degree-sorted graph)
+    // accumulates in FP64, rh_cut entries per slot.  Those nodes take
+    // thousands of additions per round, and one threshold flip there moves
+    // about 2 theta d of l1.  nullptr: every residual entry is in R.
+    double* RH;
+    int rh_cut;
 };
 
 constexpr int kMaxGroups = 512;  // at most one per slot (kMaxLaunchTiles)

@@ -170,6 +170,11 @@ __device__ __forceinline__ T* xslab_ptr(void* base, const PushArgs& a, int t) {
     return reinterpret_cast<T*>(base) + s * (a.xld ? a.xtile : a.tile_stride);
 }
 
+// FP64 residual of the hub prefix of slot t (served FP32 crossing slots), or nullptr.
+__device__ __forceinline__ double* rh_ptr(const PushArgs& a, int t) {
+    return a.RH ? a.RH + (int64_t)t * a.rh_cut : nullptr;
+}
+
 // Per-tile data staged in shared memory at the start of each tile's phase.
 struct TileSh {
     TileParams tp;
@@ -569,6 +574,8 @@ __device__ void prep_w1_cross(const PushArgs& a, int t, const TileSh& sh, long l
     const float theta_f = (float)theta;
     const float alpha_f = (float)alpha, omalpha_f = (float)(1. - alpha);
     const int64_t ld = a.ld;
+    double* RH = (sizeof(T) == 4) ? rh_ptr(a, t) : nullptr;  // hub prefix in FP64
+    const int rh_cut = a.rh_cut;
     long long ideg = 0;  // sum of (integer) degrees of the pushed nodes
     for (long long base = beg + (long long)warp * 32 * kPrepILP; base < end;
          base += (long long)kWarps * 32 * kPrepILP) {
@@ -581,15 +588,21 @@ __device__ void prep_w1_cross(const PushArgs& a, int t, const TileSh& sh, long l
             u[q] = val[q] ? cand[i] : 0;
         }
         T r[kPrepILP], xv[kPrepILP];
+        double rd[kPrepILP];  // the FP64 residual of a hub-prefix node (RH), else unused
         float df[kPrepILP], xc[kPrepILP];
         int len[kPrepILP];
         long long rp[kPrepILP];
 #pragma unroll
         for (int q = 0; q < kPrepILP; ++q) {
-            r[q] = T(0); xv[q] = T(0); df[q] = 1.f; xc[q] = 0.f; len[q] = 0; rp[q] = 0;
+            r[q] = T(0); rd[q] = 0.0; xv[q] = T(0); df[q] = 1.f; xc[q] = 0.f; len[q] = 0; rp[q] = 0;
             if (val[q]) {
                 const int64_t off = (int64_t)u[q] * ld, xoff = (int64_t)u[q] * xld;
-                r[q] = R[off];
+                if (RH && u[q] < rh_cut) {
+                    rd[q] = RH[u[q]];
+                    r[q] = (T)rd[q];
+                } else {
+                    r[q] = R[off];
+                }
                 xv[q] = X[xoff];
                 if (XC) xc[q] = XC[xoff];
                 if (g.rec) {
@@ -611,10 +624,16 @@ __device__ void prep_w1_cross(const PushArgs& a, int t, const TileSh& sh, long l
             if (val[q]) {
                 const double du = g.degf_exact ? (double)df[q] : g.degd[u[q]];
                 if constexpr (sizeof(T) == 4) {
-                    // FP32 tile: exact threshold test mostly in FP32; push value in FP32
-                    if (g.degf_exact) act = ge_threshold(fabsf(r[q]), theta_f * df[q], theta, du);
-                    else act = fabs((double)r[q]) >= theta * du;
-                    if (act) push = katz ? alpha_f * r[q] : (omalpha_f * r[q]) / df[q];
+                    if (RH && u[q] < rh_cut) {
+                        // hub prefix: FP64 residual, FP64 test and push value
+                        act = fabs(rd[q]) >= theta * du;
+                        if (act) push = (T)(katz ? alpha * rd[q] : ((1. - alpha) * rd[q]) / du);
+                    } else {
+                        // FP32 tile: exact threshold test mostly in FP32; push value in FP32
+                        if (g.degf_exact) act = ge_threshold(fabsf(r[q]), theta_f * df[q], theta, du);
+                        else act = fabs((double)r[q]) >= theta * du;
+                        if (act) push = katz ? alpha_f * r[q] : (omalpha_f * r[q]) / df[q];
+                    }
                 } else {
                     const double rv = (double)r[q];
                     act = fabs(rv) >= theta * du;
@@ -623,7 +642,8 @@ __device__ void prep_w1_cross(const PushArgs& a, int t, const TileSh& sh, long l
                 }
                 if (act) {
                     const int64_t off = (int64_t)u[q] * ld, xoff = (int64_t)u[q] * xld;
-                    R[off] = T(0);
+                    if (RH && u[q] < rh_cut) RH[u[q]] = 0.0;
+                    else R[off] = T(0);
                     if (XC) {
                         // Kahan-compensated FP32 accumulation of the solution
                         const float y = (float)r[q] - xc[q];
@@ -986,6 +1006,8 @@ struct ScatterCtx {
     bool tgt_scale;
     bool cross;
     const ColState* cs;     // the tile's column states (thresholds for crossing)
+    double* rh;             // FP64 residual of the hub prefix (ids < rh_cut), or nullptr
+    int rh_cut;
 };
 
 template <typename T, int W>
@@ -1015,6 +1037,8 @@ __device__ __forceinline__ ScatterCtx<T, W> scatter_ctx(const PushArgs& a, int t
     c.tgt_scale = (flags & SF_TGTSCALE) != 0;
     c.cross = (flags & SF_CROSS) != 0;
     c.cs = a.cs + (int64_t)t * W;
+    c.rh = (sizeof(T) == 4 && W == 1 && c.cross) ? rh_ptr(a, t) : nullptr;
+    c.rh_cut = a.rh_cut;
     return c;
 }
 
@@ -1195,14 +1219,25 @@ __device__ __forceinline__ void edges_w1(const PushArgs& a, const ScatterCtx<T, 
             df[u] = 1.f;
             if (glob[u]) df[u] = (dcode[u] != g.deg_esc) ? (float)dcode[u] : g.degf[v[u]];
         }
+        bool hd[kEdgeILP];     // target in the FP64 hub prefix
+        double oldd[kEdgeILP];
 #pragma unroll
-        for (int u = 0; u < kEdgeILP; ++u)
-            old[u] = glob[u] ? atomicAdd(c.tgt + (int64_t)v[u] * c.tld, p[u]) : T(0);
+        for (int u = 0; u < kEdgeILP; ++u) {
+            hd[u] = c.rh && glob[u] && v[u] < c.rh_cut;
+            oldd[u] = 0.0;
+            old[u] = T(0);
+            if (hd[u]) oldd[u] = atomicAdd(c.rh + v[u], (double)p[u]);
+            else if (glob[u]) old[u] = atomicAdd(c.tgt + (int64_t)v[u] * c.tld, p[u]);
+        }
         bool cr[kEdgeILP];
 #pragma unroll
         for (int u = 0; u < kEdgeILP; ++u) {
             cr[u] = hub_cr[u];
-            if (glob[u]) {
+            if (hd[u]) {
+                const double dv = g.degf_exact ? (double)df[u] : g.degd[v[u]];
+                const double thr = theta * dv;
+                cr[u] = (oldd[u] < thr) && (oldd[u] + (double)p[u] >= thr);  // the value the atomic stored
+            } else if (glob[u]) {
                 const T s = old[u] + p[u];  // the value the atomic stored
                 if constexpr (sizeof(T) == 4) {
                     if (g.degf_exact) {
@@ -1346,6 +1381,7 @@ __device__ void scatter_flat_w1(const PushArgs& a, const PushItem* items, int st
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const double theta = c.cross ? c.cs[0].theta : 0.0;
     __shared__ T fagg[kWarps][32];
+    __shared__ double faggd[kWarps][32];  // hub-prefix targets: the warp's sum in FP64
     for (long long kb = beg + (long long)warp * GROUP; kb < end; kb += (long long)kWarps * GROUP) {
         const long long k = kb + lane;
         int len = 0;
@@ -1397,11 +1433,24 @@ __device__ void scatter_flat_w1(const PushArgs& a, const PushItem* items, int st
                     if (!__any_sync(kFull, hub)) continue;
                     const unsigned peers = __match_any_sync(kFull, hub ? v[u] : -1 - lane);
                     const int leader = __ffs(peers) - 1;
-                    if (hub && lane == leader) fagg[warp][lane] = T(0);
-                    __syncwarp();
-                    if (hub) atomicAdd(&fagg[warp][leader], p[u]);
-                    __syncwarp();
+                    const bool hd = hub && c.rh && v[u] < c.rh_cut;
                     if (hub && lane == leader) {
+                        fagg[warp][lane] = T(0);
+                        faggd[warp][lane] = 0.0;
+                    }
+                    __syncwarp();
+                    if (hd) atomicAdd(&faggd[warp][leader], (double)p[u]);
+                    else if (hub) atomicAdd(&fagg[warp][leader], p[u]);
+                    __syncwarp();
+                    if (hd && lane == leader) {
+                        // FP64 hub prefix: the combined add and the crossing test in FP64
+                        const double tot = faggd[warp][lane];
+                        const double old = atomicAdd(c.rh + v[u], tot);
+                        const double dv = (dc[u] != g.deg_esc) ? (double)dc[u]
+                                          : (g.degf_exact ? (double)g.degf[v[u]] : g.degd[v[u]]);
+                        const double thr = theta * dv;
+                        hub_cr[u] = (old < thr) && (old + tot >= thr);
+                    } else if (hub && lane == leader) {
                         const T tot = fagg[warp][lane];
                         T* addr = c.tgt + (int64_t)v[u] * c.tld;
                         if (c.cross) {
@@ -1659,7 +1708,8 @@ __device__ void admit_query(const PushArgs& a, int t, int it) {
     cs.check_cnt[0] = cs.check_cnt[1] = 0;
     cs.seed = seed;
     cs.finish_ns = 0;
-    slab_ptr<T>(a.R, a, t)[(int64_t)seed * a.ld] = (T)q.r0[qid];
+    if (sizeof(T) == 4 && a.RH && tile_crosses(a.tp[t]) && seed < a.rh_cut) rh_ptr(a, t)[seed] = q.r0[qid];
+    else slab_ptr<T>(a.R, a, t)[(int64_t)seed * a.ld] = (T)q.r0[qid];
     q.start_ns[qid] = now;
     __threadfence();
     ts.done = SLOT_LIVE;
@@ -1677,6 +1727,7 @@ __device__ void retire_range(const PushArgs& a, int t, long long beg, long long 
     T* R = slab_ptr<T>(a.R, a, t);
     T* R2 = a.R2 ? slab_ptr<T>(a.R2, a, t) : nullptr;
     float* XC = a.kahan ? xslab_ptr<float>(a.XC, a, t) : nullptr;
+    double* rh = (sizeof(T) == 4) ? rh_ptr(a, t) : nullptr;  // FP64 hub prefix
     const int64_t xld = x_ld(a);
     const int si = q.seed[qid];
     const int kind = q.kind ? q.kind[qid] : a.tp[t].kind;
@@ -1693,11 +1744,14 @@ __device__ void retire_range(const PushArgs& a, int t, long long beg, long long 
         // launch): only the slot's residual is extracted and cleared here
         for (long long v = beg + threadIdx.x; v < end; v += kThreads) {
             const int64_t o = v * a.ld;
+            const bool hv = rh && v < a.rh_cut;
             if (q.r_out) {
-                if (q.out64) reinterpret_cast<double*>(q.r_out)[orow + v] = (double)R[o];
-                else reinterpret_cast<float*>(q.r_out)[orow + v] = (float)R[o];
+                const double rv = hv ? rh[v] : (double)R[o];
+                if (q.out64) reinterpret_cast<double*>(q.r_out)[orow + v] = rv;
+                else reinterpret_cast<float*>(q.r_out)[orow + v] = (float)rv;
             }
             R[o] = T(0);
+            if (hv) rh[v] = 0.0;
             if (R2) R2[o] = T(0);
         }
         return;
@@ -1710,12 +1764,15 @@ __device__ void retire_range(const PushArgs& a, int t, long long beg, long long 
         if (xdiv != 1.0) x = x / xdiv;
         if (xo32) __stcs(xo32 + v, (float)x);
         if (xo64) __stcs(xo64 + v, x);
+        const bool hv = rh && v < a.rh_cut;
         if (q.r_out) {
-            if (q.out64) reinterpret_cast<double*>(q.r_out)[orow + v] = (double)R[o];
-            else reinterpret_cast<float*>(q.r_out)[orow + v] = (float)R[o];
+            const double rv = hv ? rh[v] : (double)R[o];
+            if (q.out64) reinterpret_cast<double*>(q.r_out)[orow + v] = rv;
+            else reinterpret_cast<float*>(q.r_out)[orow + v] = (float)rv;
         }
         X[xo] = T(0);
         R[o] = T(0);
+        if (hv) rh[v] = 0.0;
         if (R2) R2[o] = T(0);
         if (XC) XC[xo] = 0.f;
     }
@@ -1795,7 +1852,8 @@ __device__ bool admit_online(const PushArgs& a, int t, int it) {
     cs.check_cnt[0] = cs.check_cnt[1] = 0;
     cs.seed = seed;
     cs.finish_ns = 0;
-    slab_ptr<T>(a.R, a, t)[(int64_t)seed * a.ld] = (T)r0;
+    if (sizeof(T) == 4 && a.RH && tile_crosses(a.tp[t]) && seed < a.rh_cut) rh_ptr(a, t)[seed] = r0;
+    else slab_ptr<T>(a.R, a, t)[(int64_t)seed * a.ld] = (T)r0;
     os.admit_ns = globaltimer_ns();
     __threadfence();
     ts.done = SLOT_LIVE;
@@ -1835,9 +1893,11 @@ __device__ void clear_slot_range(const PushArgs& a, int t, long long beg, long l
     T* R = slab_ptr<T>(a.R, a, t);
     T* R2 = a.R2 ? slab_ptr<T>(a.R2, a, t) : nullptr;
     float* XC = a.kahan ? xslab_ptr<float>(a.XC, a, t) : nullptr;
+    double* rh = (sizeof(T) == 4) ? rh_ptr(a, t) : nullptr;
     const int64_t xld = x_ld(a);
     for (long long v = beg + threadIdx.x; v < end; v += kThreads) {
         R[v * a.ld] = T(0);
+        if (rh && v < a.rh_cut) rh[v] = 0.0;
         X[v * xld] = T(0);
         if (XC) XC[v * xld] = 0.f;
         if (R2) R2[v * a.ld] = T(0);

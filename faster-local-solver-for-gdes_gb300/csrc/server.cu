@@ -328,6 +328,19 @@ int gde_server_start(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t ri
     a.trace = nullptr;
     a.trace_iters = 0;
     a.spin_limit = (unsigned long long)std::max<int64_t>(ctx->wait_limit, 0);
+    // FP32 slots keep the residual of the highest-degree nodes in FP64
+    a.RH = nullptr;
+    a.rh_cut = 0;
+    if (!s->prec64 && G->g.hub_cut > 0) {
+        a.rh_cut = (int)std::min<int64_t>(G->g.hub_cut, (int64_t)1 << 16);
+        a.RH = (double*)s->dalloc((size_t)S * a.rh_cut * 8);
+        if (!a.RH) {
+            int rc = s->fail(GDE_ENOMEM, "device memory exhausted (FP64 hub residuals)");
+            s->free_all();
+            delete s;
+            return rc;
+        }
+    }
     a.serve = 1;
     a.round_budget = 0x7fffffff;
     // ---- heat-kernel psi tables for every Taylor length the server accepts ----
@@ -385,6 +398,7 @@ int gde_server_start(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t ri
     CK_S(cudaMemsetAsync(a.X, 0, inter ? 2 * slab : slab, s->stream));
     if (a.R2) CK_S(cudaMemsetAsync(a.R2, 0, slab, s->stream));
     CK_S(cudaMemsetAsync(a.mark, 0xff, (size_t)S * n * 4, s->stream));
+    if (a.RH) CK_S(cudaMemsetAsync(a.RH, 0, (size_t)S * a.rh_cut * 8, s->stream));
     CK_S(cudaMemsetAsync(Q.last_ns, 0, sizeof(unsigned long long), s->stream));
     std::vector<TileParams> tp(S);
     std::vector<ColState> cs(S);
