@@ -416,10 +416,10 @@ int build_static_records(gde_ctx* ctx, gde_graph* G, const int32_t* col) {
 // nodes in FP64 (the graph's hub prefix: rows longer than kHubLen).
 constexpr int64_t kRhMax = 1 << 16;
 
-int64_t served_slot_bytes(int64_t n, int64_t cap, int prec64, bool hk, const PushArgs& tun) {
+int64_t served_slot_bytes(int64_t n, int64_t cap, int prec64, bool hk, const PushArgs& tun, int64_t hub_cut) {
     const int64_t es = prec64 ? 8 : 4;
     const int64_t large_cap = cap / std::max(tun.chunk, 1) + cap / std::max(tun.med_max, 1) + 64;
-    return n * es * (3 + (hk ? 1 : 0)) + (prec64 ? 0 : n * 4 + kRhMax * 8) + n * 4 * 3 +
+    return n * es * (3 + (hk ? 1 : 0)) + (prec64 ? 0 : n * 4 + std::min(hub_cut, kRhMax) * 8) + n * 4 * 3 +
            n * (int64_t)sizeof(PushItem) + large_cap * (int64_t)sizeof(PushItem);
 }
 
@@ -440,7 +440,7 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     fill_tuning(p, base);
     if (budget_bytes > 0.0) {
         // admission by memory budget: only as many slots as fit
-        const int64_t per = served_slot_bytes(n, G->g.cap, prec64, any_hk, base);
+        const int64_t per = served_slot_bytes(n, G->g.cap, prec64, any_hk, base, G->g.hub_cut);
         const int64_t fit = (int64_t)(budget_bytes / (double)per);
         if (fit < 1) return fail(ctx, GDE_ENOMEM, "the HBM budget does not hold one query slot");
         S = (int)std::min<int64_t>(S, fit);
@@ -472,7 +472,7 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
         const size_t need = (size_t)nq * (size_t)a.xtile * 4;
         // under an HBM budget the query slabs count against it with the slots
         const bool in_budget = budget_bytes <= 0.0 ||
-                               (double)S * (double)served_slot_bytes(n, G->g.cap, prec64, any_hk, base) +
+                               (double)S * (double)served_slot_bytes(n, G->g.cap, prec64, any_hk, base, G->g.hub_cut) +
                                        (double)need <= budget_bytes;
         if (need <= freeb / 3 && in_budget) {
             void* xq = wsget(ctx, "Xq", need);

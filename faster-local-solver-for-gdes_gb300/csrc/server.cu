@@ -256,7 +256,8 @@ int gde_server_start(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t ri
     S = std::min(S, 512);
     const int64_t es = s->prec64 ? 8 : 4;
     const int64_t large_cap = G->g.cap / std::max(base.chunk, 1) + G->g.cap / std::max(base.med_max, 1) + 64;
-    const int64_t per_slot = n * es * (3 + (s->hk ? 1 : 0)) + (s->prec64 ? 0 : n * 4) + n * 4 * 3 +
+    const int64_t rh_bytes = s->prec64 ? 0 : std::min<int64_t>(G->g.hub_cut, (int64_t)1 << 16) * 8;
+    const int64_t per_slot = n * es * (3 + (s->hk ? 1 : 0)) + (s->prec64 ? 0 : n * 4) + rh_bytes + n * 4 * 3 +
                              n * (int64_t)sizeof(PushItem) + large_cap * (int64_t)sizeof(PushItem);
     if (hbm_budget_bytes > 0.0) {
         const int64_t fit = (int64_t)(hbm_budget_bytes / (double)per_slot);
