@@ -296,10 +296,7 @@ def run_ours(args):
     from gde import _lib as L
     from gde import api, graphs
 
-    tuning = {"slots": args.slots}
-    for kv in filter(None, args.tuning.split(",")):
-        k, v = kv.split("=")
-        tuning[k] = int(v)
+    tuning = dict(parse_tuning(args.tuning), slots=args.slots)
     g = graphs.chung_lu_wikitalk_shape()
     ctx = api.Context.get(local)
     G = api.Graph(g.indptr, g.indices, ctx=ctx)
@@ -603,6 +600,15 @@ def mixed_cpu_baseline(g, kinds, seeds, eps, alphas, tau, budget_s: float = 15.0
             "sample": f"{done} queries of the mix (eps as drawn, FP64 C ports, one per thread), {dt:.1f} s"}
 
 
+def parse_tuning(text):
+    """``k=v,...`` engine tuning overrides (integers, or floats such as sparse_eps=1e-6)."""
+    out = {}
+    for kv in filter(None, text.split(",")):
+        k, v = kv.split("=")
+        out[k] = float(v) if any(c in v for c in ".eE") else int(v)
+    return out
+
+
 def run_c4(args):
     """Served mixed queries on R-MAT scale 22: 60% PPR, 25% Katz, 15% heat kernel, Poisson arrivals."""
     import torch
@@ -636,6 +642,9 @@ def run_c4(args):
     config = {"workload": "served_mix_ppr_katz_hk_fp32_rmat22", "n": g.n, "nnz": g.nnz, "queries_per_step": Q,
               "ppr_alpha": ALPHA, "katz_alpha": "0.5 / d_max", "hk_tau": tau, "eps": "log-uniform [1e-8, 1e-5]",
               "hbm_budget_bytes": budget, "requested_slots": args.slots, "graph_generation_s": gen_s}
+    tuning = parse_tuning(args.tuning)
+    if tuning:
+        config["tuning"] = tuning
     if args.online:
         run_c4_online(args, g, G, x_dev, queries, config, tau, budget)
         return
@@ -644,7 +653,7 @@ def run_c4(args):
         kinds, seeds, eps, alphas, arr = queries(k, rate)
         return api.serve_mixed(G, kinds, seeds, eps, alphas=alphas, tau=tau, arrival_ms=arr, hbm_budget_bytes=budget,
                                prec="fp32", x_out=x_dev if x_out is None else x_out, device_out=device_out,
-                               slots=args.slots)
+                               slots=args.slots, tuning=tuning)
 
     for w in range(args.warmup):
         step(10 + w, 0)
@@ -656,7 +665,9 @@ def run_c4(args):
             lat = np.concatenate([o["latency_ms"] for o in outs])
             rows.append({"rate_qps": rate if rate > 0 else None, "queries_per_s": Q * len(times) / (sum(times) / 1e3),
                          "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
-                         "slots": int(outs[0]["stats"]["tiles"]), "ms_per_step": sum(times) / len(times)})
+                         "slots": int(outs[0]["stats"]["tiles"]), "ms_per_step": sum(times) / len(times),
+                         "table_queries": int(sum(o["stats"]["sparse_queries"] for o in outs)),
+                         "table_overflows": int(sum(o["stats"]["sparse_overflows"] for o in outs))})
             if rate <= 0:
                 sat = (times, outs, 100 + len(times) - 1)
     best = max(rows, key=lambda r: r["queries_per_s"])

@@ -230,7 +230,9 @@ int alloc_large(gde_ctx* ctx, gde_graph* G, int ntiles, TileWs& tw) {
 int run_engine(gde_ctx* ctx, PushArgs& a, int prec64, int W, gde_stats* st, double* kernel_ms) {
     int grid = engine_max_grid(prec64, W, ctx->sms);
     if (grid <= 0) return fail(ctx, GDE_ECUDA, "push kernel does not fit on the device");
-    if (a.groups > grid) a.groups = grid;  // every group holds at least one block
+    if (a.serve && a.queue.sp_blocks > grid / 2) a.queue.sp_blocks = grid / 2;  // at least half the grid stays dense
+    const int dense_grid = grid - (a.serve ? a.queue.sp_blocks : 0);
+    if (a.groups > dense_grid) a.groups = dense_grid;  // every group holds at least one block
     CK(cudaMemsetAsync(ctx->bar, 0, kMaxGroups * sizeof(GridBarrier), ctx->stream));
     CK(cudaMemsetAsync(ctx->derr, 0, sizeof(int), ctx->stream));
     CK(cudaMemsetAsync(ctx->dstats, 0, sizeof(LaunchStats), ctx->stream));
@@ -260,6 +262,8 @@ int run_engine(gde_ctx* ctx, PushArgs& a, int prec64, int W, gde_stats* st, doub
         st->check_ms += (double)ctx->hstats->check_ns * 1e-6;
         st->prep_ms += (double)ctx->hstats->prep_ns * 1e-6;
         st->scatter_ms += (double)ctx->hstats->scatter_ns * 1e-6;
+        st->sparse_queries += (int64_t)ctx->hstats->sp_done;
+        st->sparse_overflows += (int64_t)ctx->hstats->sp_ovf;
     }
     if (herr != 0) {
         // The launch stopped part-way: its marks may carry stamps the next
@@ -491,6 +495,24 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
         a.RH = (double*)wsget(ctx, "RH", (size_t)S * a.rh_cut * 8);
         if (!a.RH) return fail(ctx, GDE_ENOMEM, "device memory exhausted (FP64 hub residuals)");
     }
+    // Small queries (eps >= sparse_eps, PPR / Katz) go to hash-table blocks
+    // when the launch writes per-query {x, c} slabs: their entries land in
+    // the same slabs, so the read-out below serves both classes.
+    std::vector<int32_t> ord_d, ord_s;
+    int sp_cap = 0;
+    if (p->sparse_blocks > 0 && p->sparse_eps > 0.0 && a.xq && !r_out) {
+        for (int64_t q = 0; q < nq; q++) {
+            const int k = kinds ? kinds[q] : kind;
+            const bool small = (k == KIND_PPR || k == KIND_KATZ) && eps[q] >= p->sparse_eps;
+            (small ? ord_s : ord_d).push_back((int32_t)q);
+        }
+        if (ord_s.empty()) ord_d.clear();
+        sp_cap = 1024;
+        while (sp_cap < (p->sparse_cap > 0 ? std::min(p->sparse_cap, 1 << 24) : (1 << 16))) sp_cap <<= 1;
+    }
+    const int spB = ord_s.empty() ? 0 : (int)std::min<int64_t>(p->sparse_blocks, (int64_t)ord_s.size());
+    const int64_t nd = ord_s.empty() ? nq : (int64_t)ord_d.size();
+    auto dq = [&](int64_t i) -> int64_t { return ord_s.empty() ? i : (int64_t)ord_d[i]; };
     CK(cudaEventRecord(ctx->ev[2], ctx->stream));
     CK(cudaMemsetAsync(a.R, 0, slab, ctx->stream));
     if (a.RH) CK(cudaMemsetAsync(a.RH, 0, (size_t)S * a.rh_cut * 8, ctx->stream));
@@ -566,10 +588,10 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     }
     // the leading queries that have arrived at launch start go straight into
     // slots; the other slots start idle and admit queries as they arrive
-    int first = S;
+    int first = (int)std::min<int64_t>(S, nd);
     if (arrival_ms) {
         first = 0;
-        while (first < S && qarr[first] <= 0) first++;
+        while (first < S && first < nd && qarr[dq(first)] <= 0) first++;
     }
     CK(cudaMemcpyAsync(d_next, &first, 4, cudaMemcpyHostToDevice, ctx->stream));
     // ---- outputs: the caller's device rows, or staging rows copied back ----
@@ -599,16 +621,17 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     for (int t = 0; t < S; t++) {
         TileParams& P = tp[t];
         memset(&P, 0, sizeof(P));
-        const int k = (t < first) ? qk[t] : kind;
+        const int64_t qi = (t < first) ? dq(t) : 0;  // the query slot t starts with
+        const int k = (t < first) ? qk[qi] : kind;
         P.kind = k;
         P.method = (k == KIND_HK) ? M_HK_LOCAL : M_LOCAL_GD;
         P.ncols = 1;
-        P.alpha = (t < first) ? qal[t] : p->alpha;
+        P.alpha = (t < first) ? qal[qi] : p->alpha;
         P.tau = p->tau;
         P.x_gain = 1.0;
         if (k == KIND_HK) {
-            P.n_levels = qnl[t];
-            P.psi_tab = d_psi + qpo[t];
+            P.n_levels = qnl[qi];
+            P.psi_tab = d_psi + qpo[qi];
         }
         TileState& T = ts[t];
         memset(&T, 0, sizeof(T));
@@ -623,15 +646,15 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
             continue;
         }
         T.done = SLOT_LIVE;
-        T.qid = t;
+        T.qid = (int)qi;
         C.live = 1;
-        C.seed = qs[t];
-        C.theta = qt[t];
+        C.seed = qs[qi];
+        C.theta = qt[qi];
         InitCol I{};
         I.tile = t;
         I.col = 0;
-        I.seed = qs[t];
-        I.r0 = qr0[t];
+        I.seed = qs[qi];
+        I.r0 = qr0[qi];
         ic[t] = I;
     }
     CK(cudaMemcpyAsync(a.tp, tp.data(), S * sizeof(TileParams), cudaMemcpyHostToDevice, ctx->stream));
@@ -668,6 +691,48 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     Q.rounds = d_rounds;
     Q.start_ns = d_start;
     Q.finish_ns = d_finish;
+    Q.kind0 = kind;
+    Q.alpha0 = p->alpha;
+    if (spB > 0) {
+        const int64_t ns = (int64_t)ord_s.size();
+        int32_t* d_ord_d = (int32_t*)dev("q_order_d", ord_d.size() * 4);
+        int32_t* d_ord_s = (int32_t*)dev("q_order_s", ns * 4);
+        int* d_ovf = (int*)dev("sp_ovf", ns * 4);
+        int* d_ctr = (int*)dev("sp_ctr", 4 * 4);  // next_s, ovf_cnt, ovf_next, sp_left
+        const size_t ent = (size_t)spB * sp_cap;
+        int32_t* d_keys = (int32_t*)dev("sp_keys", ent * 4);
+        double* d_r = (double*)dev("sp_r", ent * 8);
+        double* d_x = (double*)dev("sp_x", ent * 8);
+        int32_t* d_list = (int32_t*)dev("sp_list", ent * 3 * 4);
+        double* d_push = (double*)dev("sp_push", ent * 8);
+        if (!d_ord_d || !d_ord_s || !d_ovf || !d_ctr || !d_keys || !d_r || !d_x || !d_list || !d_push)
+            return fail(ctx, GDE_ENOMEM, "small-query tables");
+        if (!ord_d.empty())
+            CK(cudaMemcpyAsync(d_ord_d, ord_d.data(), ord_d.size() * 4, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemcpyAsync(d_ord_s, ord_s.data(), ns * 4, cudaMemcpyHostToDevice, ctx->stream));
+        const int ctr[4] = {0, 0, 0, (int)ns};
+        CK(cudaMemcpyAsync(d_ctr, ctr, sizeof ctr, cudaMemcpyHostToDevice, ctx->stream));
+        CK(cudaMemsetAsync(d_ovf, 0xff, ns * 4, ctx->stream));
+        CK(cudaMemsetAsync(d_keys, 0xff, ent * 4, ctx->stream));  // -1: empty
+        CK(cudaMemsetAsync(d_r, 0, ent * 8, ctx->stream));
+        CK(cudaMemsetAsync(d_x, 0, ent * 8, ctx->stream));
+        Q.sp_blocks = spB;
+        Q.sp_cap = sp_cap;
+        Q.order_d = d_ord_d;
+        Q.nd = (int)ord_d.size();
+        Q.order_s = d_ord_s;
+        Q.ns = (int)ns;
+        Q.next_s = d_ctr;
+        Q.ovf_cnt = d_ctr + 1;
+        Q.ovf_next = d_ctr + 2;
+        Q.sp_left = d_ctr + 3;
+        Q.ovf = d_ovf;
+        Q.sp_keys = d_keys;
+        Q.sp_r = d_r;
+        Q.sp_x = d_x;
+        Q.sp_list = d_list;
+        Q.sp_push = d_push;
+    }
     double kernel_ms = 0.0;
     rc = run_engine(ctx, a, prec64, 1, stats, &kernel_ms);
     if (rc != GDE_OK) return rc;

@@ -208,6 +208,33 @@ struct ServeQueue {
     unsigned long long idle_ns;   // the launch ends after this long with nothing to do
     OnlineSlot* slot;             // [slots]
     const int32_t* perm;          // caller id -> internal id (nullptr: identity)
+    // Hash-compacted small queries (sp_blocks > 0): the launch's last
+    // sp_blocks blocks each solve one PPR / Katz local GD query at a time
+    // out of an open-addressing table of sp_cap entries in global memory
+    // (keys, FP64 residual and solution), instead of dense vectors.  Queries
+    // in order_s go there; one whose touched set outgrows the table is queued
+    // for the dense slots (ovf).  Dense slots take order_d (nullptr: query
+    // ids in order), then the overflow list.  A finished sparse query writes
+    // its entries into its {x, c} query slab (the launch needs xq != 0), so
+    // the read-out after the launch is the same for both classes.
+    int sp_blocks;
+    int sp_cap;                   // entries per table (power of two)
+    const int32_t* order_d;       // [nd] dense-class query ids, in arrival order
+    int nd;
+    const int32_t* order_s;       // [ns] sparse-class query ids, in arrival order
+    int ns;
+    int* next_s;                  // next order_s position
+    int* ovf;                     // [ns] overflowed query ids, -1 until written
+    int* ovf_cnt;                 // ovf positions handed out
+    int* ovf_next;                // next ovf entry to admit
+    int* sp_left;                 // sparse-class queries not yet finished or overflowed
+    int32_t* sp_keys;             // [sp_blocks][sp_cap] node id per entry (-1: empty)
+    double* sp_r;                 // [sp_blocks][sp_cap] residual
+    double* sp_x;                 // [sp_blocks][sp_cap] solution
+    int32_t* sp_list;             // [sp_blocks][3][sp_cap] frontier (two) and used-entry lists
+    double* sp_push;              // [sp_blocks][sp_cap] push value per frontier entry
+    int kind0;                    // single-kind queues: the queries' kind
+    double alpha0;                //                     and alpha
 };
 
 struct ColState {             // one per column slot
@@ -238,6 +265,8 @@ struct LaunchStats {          // roofline counters summed over a launch
     unsigned long long prep_ns;        // ... PREP phases
     unsigned long long scatter_ns;     // ... SCATTER phases
     unsigned long long iters;          // launch iterations run
+    unsigned long long sp_done;        // served small queries finished in hash tables
+    unsigned long long sp_ovf;         // ... handed to the dense slots
 };
 
 // Arrival counter and generation word on separate 128-byte lines: waiting

@@ -16,6 +16,12 @@ constexpr unsigned long long kSpinLimit = 1ull << 26;  // ~ seconds of polling
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ unsigned ld_volatile(const unsigned* p) { return *(volatile const unsigned*)p; }
 __device__ __forceinline__ int ld_volatile_i(const int* p) { return *(volatile const int*)p; }
+// A load that later loads of this thread cannot pass (device-scope acquire).
+__device__ __forceinline__ int ld_acquire_gpu_i(const int* p) {
+    int v;
+    asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
 
 // `limit` polls (0: kSpinLimit) before a waiting block gives up; `members`
 // blocks meet at `bar` (0: the whole grid).

@@ -461,7 +461,7 @@ struct GroupInfo {
 };
 __device__ __forceinline__ GroupInfo group_of(const PushArgs& a) {
     const int G = a.groups > 1 ? a.groups : 1;
-    const long long B = gridDim.x;
+    const long long B = (long long)gridDim.x - (a.serve ? a.queue.sp_blocks : 0);  // the dense blocks
     const int g = (int)((long long)blockIdx.x * G / B);
     const int start = (int)(((long long)g * B + G - 1) / G);
     const int end = (int)(((long long)(g + 1) * B + G - 1) / G);
@@ -1646,29 +1646,63 @@ __device__ void admit_query(const PushArgs& a, int t, int it) {
     if (threadIdx.x != 0) return;
     TileState& ts = a.ts[t];
     const ServeQueue& q = a.queue;
-    // the next query in order; group leaders take queries concurrently
+    // the next query in order (the dense-class order when small queries go to
+    // the hash-table blocks), then any query those blocks gave back; group
+    // leaders take queries concurrently
     const unsigned long long now = globaltimer_ns();
+    const int nd = q.order_d ? q.nd : q.nq;
     int qid = -1;
+    bool dense_left = true;
     if (q.arrival_ns) {
         // block 0 stamps the launch start; other groups may get here first
         const unsigned long long st0 = *(volatile const unsigned long long*)&a.stats->start_ns;
         if (st0 == 0) return;
         for (int tries = 0; tries < 4096; ++tries) {
             const int c = ld_volatile_i(q.next);
-            if (c >= q.nq) {
-                ts.done = SLOT_EMPTY;
-                return;
+            if (c >= nd) {
+                dense_left = false;
+                break;
             }
-            if (now < st0 + (unsigned long long)q.arrival_ns[c]) return;  // not arrived yet
+            const int cq = q.order_d ? q.order_d[c] : c;
+            if (now < st0 + (unsigned long long)q.arrival_ns[cq]) return;  // not arrived yet
             if (atomicCAS(q.next, c, c + 1) == c) {
-                qid = c;
+                qid = cq;
                 break;
             }
         }
-        if (qid < 0) return;  // another leader kept winning: try next round
+        if (qid < 0 && dense_left) return;  // another leader kept winning: try next round
     } else {
-        qid = atomicAdd(q.next, 1);
-        if (qid >= q.nq) {
+        const int c = atomicAdd(q.next, 1);
+        if (c < nd) qid = q.order_d ? q.order_d[c] : c;
+        else dense_left = false;
+    }
+    if (!dense_left) {
+        if (q.sp_blocks > 0) {
+            // queries whose touched set outgrew a hash table run here
+            // (sp_left is read first: at zero every ovf position has been handed out)
+            const int left = ld_acquire_gpu_i(q.sp_left);
+            for (int tries = 0; tries < 4096 && qid < 0; ++tries) {
+                const int c = ld_volatile_i(q.ovf_next);
+                if (c >= ld_volatile_i(q.ovf_cnt)) break;
+                if (atomicCAS(q.ovf_next, c, c + 1) == c) {
+                    // the position is handed out before its id is stored: wait for it (bounded)
+                    int v = ld_volatile_i(&q.ovf[c]);
+                    for (unsigned long long s = 0; v < 0; ++s) {
+                        if (s > (a.spin_limit ? a.spin_limit : (1ull << 26))) {
+                            atomicCAS(a.err, 0, GDE_EHANG);
+                            return;
+                        }
+                        v = ld_volatile_i(&q.ovf[c]);
+                    }
+                    qid = v;
+                }
+            }
+            if (qid < 0) {
+                // more may come while small queries are still running
+                if (left == 0 && ld_volatile_i(q.ovf_next) >= ld_volatile_i(q.ovf_cnt)) ts.done = SLOT_EMPTY;
+                return;
+            }
+        } else {
             ts.done = SLOT_EMPTY;
             return;
         }
@@ -1710,7 +1744,7 @@ __device__ void admit_query(const PushArgs& a, int t, int it) {
     cs.finish_ns = 0;
     if (sizeof(T) == 4 && a.RH && tile_crosses(a.tp[t]) && seed < a.rh_cut) rh_ptr(a, t)[seed] = q.r0[qid];
     else slab_ptr<T>(a.R, a, t)[(int64_t)seed * a.ld] = (T)q.r0[qid];
-    q.start_ns[qid] = now;
+    if (q.start_ns[qid] == 0) q.start_ns[qid] = now;  // an overflowed query keeps its first admission
     __threadfence();
     ts.done = SLOT_LIVE;
 }
@@ -1919,6 +1953,243 @@ __device__ void publish_online(const PushArgs& a, int t) {
     st_release_sys(&d->done_ticket, os.ticket);
 }
 
+// ---------------------------------------------------------------------------
+// Hash-compacted small queries.  One block solves one PPR / Katz local GD
+// query at a time with the synchronous rounds of the dense engine (the same
+// frontier sets: exact operation counts), but over an open-addressing table
+// of sp_cap entries {node id, FP64 residual, FP64 solution} in global memory
+// instead of dense n-vectors: a query that touches 10^4 nodes of a 2M-node
+// graph keeps 20 B per touched entry (the table stays in the L2) and clears
+// only the entries it used.  Rounds meet at __syncthreads, not at a grid
+// barrier.  A query that fills 3/4 of the table (or fails a bounded probe)
+// is handed to the dense slots and its partial work dropped.
+// ---------------------------------------------------------------------------
+constexpr int kSpEmpty = -1;
+constexpr int kSpProbes = 256;
+
+struct SpSh {
+    int qid;          // query in hand (-1: none left)
+    int cur_cnt, nxt_cnt, used;
+    int overflow;
+    int rounds;
+    double oper;
+    unsigned long long col_nodes;
+};
+
+__device__ __forceinline__ unsigned sp_hash(int v) { return (unsigned)v * 2654435761u; }
+
+// The entry of node v (inserted with zero residual and solution when new), or
+// -1 when the table is full.
+__device__ __forceinline__ int sp_find_insert(int32_t* keys, int32_t* used_list, int* used, int cap, int v) {
+    const unsigned mask = (unsigned)cap - 1u;
+    unsigned h = sp_hash(v) & mask;
+    for (int p = 0; p < kSpProbes; ++p) {
+        const int k = __ldcg(&keys[h]);
+        if (k == v) return (int)h;
+        if (k == kSpEmpty) {
+            const int prev = atomicCAS(&keys[h], kSpEmpty, v);
+            if (prev == kSpEmpty) {
+                const int pos = atomicAdd(used, 1);
+                if (pos >= (cap >> 2) * 3) return -1;  // load factor 3/4: the query leaves the table
+                used_list[pos] = (int)h;
+                return (int)h;
+            }
+            if (prev == v) return (int)h;
+        }
+        h = (h + 1u) & mask;
+    }
+    return -1;
+}
+
+__device__ __noinline__ void sparse_block_loop(const PushArgs& a, int c) {
+    __shared__ SpSh sp;
+    const ServeQueue& q = a.queue;
+    const DevGraph& g = a.g;
+    const int cap = q.sp_cap;
+    int32_t* keys = q.sp_keys + (int64_t)c * cap;
+    double* R = q.sp_r + (int64_t)c * cap;
+    double* X = q.sp_x + (int64_t)c * cap;
+    int32_t* lists = q.sp_list + (int64_t)c * 3 * cap;
+    int32_t* used_list = lists + 2 * cap;
+    double* push = q.sp_push + (int64_t)c * cap;
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    unsigned long long acc_nodes = 0;
+    double acc_vol = 0.0;
+    for (;;) {
+        // ---- the next small query, in arrival order ----
+        if (threadIdx.x == 0) {
+            sp.qid = -1;
+            for (;;) {
+                const int cpos = ld_volatile_i(q.next_s);
+                if (cpos >= q.ns) break;
+                const int cq = q.order_s[cpos];
+                if (q.arrival_ns) {
+                    const unsigned long long st0 = *(volatile const unsigned long long*)&a.stats->start_ns;
+                    if (st0 == 0 || globaltimer_ns() < st0 + (unsigned long long)q.arrival_ns[cq]) {
+                        if (ld_volatile_i(a.err) != 0) break;
+                        __nanosleep(2000);  // waits for an arrival time that is finite
+                        continue;
+                    }
+                }
+                if (atomicCAS(q.next_s, cpos, cpos + 1) == cpos) {
+                    sp.qid = cq;
+                    break;
+                }
+            }
+            sp.cur_cnt = 0;
+            sp.nxt_cnt = 0;
+            sp.used = 0;
+            sp.overflow = 0;
+            sp.rounds = 0;
+            sp.oper = 0.0;
+            sp.col_nodes = 0;
+        }
+        __syncthreads();
+        const int qid = sp.qid;
+        if (qid < 0) break;
+        const int kind = q.kind ? q.kind[qid] : q.kind0;
+        const double alpha = q.alpha ? q.alpha[qid] : q.alpha0;
+        const double theta = q.theta[qid];
+        const int seed = q.seed[qid];
+        if (threadIdx.x == 0) {
+            q.start_ns[qid] = globaltimer_ns();
+            const int h = sp_find_insert(keys, used_list, &sp.used, cap, seed);
+            const double r0 = q.r0[qid];
+            R[h] = r0;
+            lists[0] = h;
+            // the seed is the first frontier (ppr_solver.py:237) when at threshold (the assert at :213)
+            sp.cur_cnt = (r0 >= theta * g.degd[seed]) ? 1 : 0;
+        }
+        __syncthreads();
+        int par = 0;
+        for (int round = 0;; ++round) {
+            if (sp.cur_cnt == 0) break;
+            if (round >= a.max_rounds) {
+                // the round cap: the dense slots run it again and report the cap
+                if (threadIdx.x == 0) sp.overflow = 1;
+                __syncthreads();
+                break;
+            }
+            int32_t* cur = lists + par * cap;
+            int32_t* nxt = lists + (par ^ 1) * cap;
+            const int nf = sp.cur_cnt;
+            // ---- PREP: move each frontier entry's residual into its solution ----
+            double my_oper = 0.0;
+            for (int i = threadIdx.x; i < nf; i += kThreads) {
+                const int h = cur[i];
+                const int u = __ldcg(&keys[h]);
+                const double r = __ldcg(&R[h]);
+                R[h] = 0.0;
+                X[h] += r;
+                const double du = g.degd[u];
+                push[i] = (kind == KIND_KATZ) ? alpha * r : ((1. - alpha) * r) / du;  // ppr_solver.py:276-281
+                my_oper += du;
+            }
+            if (my_oper != 0.0) atomicAdd(&sp.oper, my_oper);
+            if (threadIdx.x == 0) {
+                sp.nxt_cnt = 0;
+                sp.rounds += 1;
+                sp.col_nodes += (unsigned long long)nf;
+            }
+            __syncthreads();
+            // ---- SCATTER: a warp per frontier row, an edge per lane ----
+            for (int i = warp; i < nf; i += kWarps) {
+                const int u = __ldcg(&keys[cur[i]]);
+                const int64_t rp = g.row_ptr[u];
+                const int len = g.row_len[u];
+                const double pv = push[i];
+                for (int j0 = 0; j0 < len; j0 += 32) {
+                    const int j = j0 + lane;
+                    bool cr = false;
+                    int h = -1;
+                    if (j < len && !ld_volatile_i(&sp.overflow)) {
+                        int v;
+                        uint32_t dc;
+                        load_edge(g, rp + j, v, dc);
+                        h = sp_find_insert(keys, used_list, &sp.used, cap, v);
+                        if (h < 0) {
+                            sp.overflow = 1;
+                        } else {
+                            const double old = atomicAdd(&R[h], pv);
+                            const double dv = (dc != g.deg_esc) ? (double)dc : g.degd[v];
+                            const double thr = theta * dv;
+                            cr = (old < thr) && (old + pv >= thr);  // ppr_solver.py:284-288
+                        }
+                    }
+                    const unsigned b = __ballot_sync(kFull, cr);
+                    if (b) {
+                        int base = 0;
+                        if (lane == 0) base = atomicAdd(&sp.nxt_cnt, __popc(b));
+                        base = __shfl_sync(kFull, base, 0);
+                        if (cr) nxt[base + __popc(b & ((1u << lane) - 1u))] = h;
+                    }
+                }
+            }
+            __syncthreads();
+            if (sp.overflow) break;
+            const int nn = sp.nxt_cnt;
+            __syncthreads();
+            if (threadIdx.x == 0) sp.cur_cnt = nn;
+            par ^= 1;
+            __syncthreads();
+        }
+        // ---- result into the query's {x, c} slab, or back to the dense slots ----
+        const bool ovf = sp.overflow != 0;
+        const int lim = (cap >> 2) * 3;
+        const int nu = min(sp.used, lim);
+        if (!ovf) {
+            float2* xs = reinterpret_cast<float2*>(reinterpret_cast<float*>(a.X) + (int64_t)qid * a.xtile);
+            for (int i = threadIdx.x; i < nu; i += kThreads) {
+                const int h = used_list[i];
+                const double x = X[h];
+                const float hi = (float)x;
+                xs[__ldcg(&keys[h])] = make_float2(hi, (float)((double)hi - x));  // read out as x - c
+            }
+        }
+        // clear the entries this query used: the table starts empty for the next
+        if (sp.used > lim) {
+            // a full table holds entries that never reached the used list
+            for (int h = threadIdx.x; h < cap; h += kThreads) {
+                keys[h] = kSpEmpty;
+                R[h] = 0.0;
+                X[h] = 0.0;
+            }
+        } else {
+            for (int i = threadIdx.x; i < nu; i += kThreads) {
+                const int h = used_list[i];
+                keys[h] = kSpEmpty;
+                R[h] = 0.0;
+                X[h] = 0.0;
+            }
+        }
+        __threadfence();
+        __syncthreads();
+        if (threadIdx.x == 0) {
+            if (ovf) {
+                const int pos = atomicAdd(q.ovf_cnt, 1);
+                *(volatile int*)&q.ovf[pos] = qid;
+                atomicAdd(&a.stats->sp_ovf, 1ull);
+            } else {
+                atomicAdd(&a.stats->sp_done, 1ull);
+                q.oper[qid] = sp.oper;
+                q.rounds[qid] = sp.rounds;
+                q.finish_ns[qid] = globaltimer_ns();
+                acc_nodes += sp.col_nodes;
+                acc_vol += sp.oper;
+            }
+            __threadfence();
+            atomicSub(q.sp_left, 1);
+        }
+        __syncthreads();
+    }
+    if (threadIdx.x == 0 && acc_nodes) {
+        atomicAdd(&a.stats->col_nodes, acc_nodes);
+        atomicAdd(&a.stats->union_nodes, acc_nodes);
+        atomicAdd(&a.stats->col_vol, acc_vol);
+        atomicAdd(&a.stats->union_vol, acc_vol);
+    }
+}
+
 // Opt-in per-block phase timeline (thread 0, first trace_iters iterations).
 __device__ __forceinline__ void trace_point(const PushArgs& a, int it, int k) {
     if (a.trace && it < a.trace_iters && threadIdx.x == 0)
@@ -1940,6 +2211,11 @@ __global__ void __launch_bounds__(kThreads, (W == 1 && sizeof(T) == 4)   ? GDE_M
     if (threadIdx.x == 0) {
         ps.acc_col_nodes = 0; ps.acc_union_nodes = 0;
         ps.acc_col_vol = 0.0; ps.acc_union_vol = 0.0;
+    }
+    // the launch's last sp_blocks blocks solve small queries out of hash tables
+    if (a.serve && a.queue.sp_blocks > 0 && (int)blockIdx.x >= (int)gridDim.x - a.queue.sp_blocks) {
+        sparse_block_loop(a, (int)blockIdx.x - ((int)gridDim.x - a.queue.sp_blocks));
+        return;
     }
     int it = 0;
     const bool online = a.serve && a.queue.online;

@@ -28,7 +28,8 @@ class Params(ctypes.Structure):
     _fields_ = [("kind", _int), ("method", _int), ("prec", _int), ("tile_w", _int),
                 ("alpha", _dbl), ("tau", _dbl), ("l_max", _dbl), ("mu_min", _dbl), ("beta", _dbl), ("omega", _dbl),
                 ("max_rounds", _int), ("small_max", _int), ("med_max", _int), ("chunk", _int), ("dense_div", _int),
-                ("slots", _int), ("groups", _int)]
+                ("slots", _int), ("groups", _int),
+                ("sparse_blocks", _int), ("sparse_cap", _int), ("sparse_eps", ctypes.c_double)]
 
 
 class Stats(ctypes.Structure):
@@ -36,7 +37,8 @@ class Stats(ctypes.Structure):
                 ("union_vol", _dbl), ("col_vol", _dbl), ("union_nodes", ctypes.c_uint64),
                 ("col_nodes", ctypes.c_uint64), ("tiles", _int), ("tile_w", _int),
                 ("check_ms", _dbl), ("prep_ms", _dbl), ("scatter_ms", _dbl), ("edit_path", _int),
-                ("edit_ms", _dbl), ("prec", _int)]
+                ("edit_ms", _dbl), ("prec", _int),
+                ("sparse_queries", _i64), ("sparse_overflows", _i64)]
 
     def as_dict(self) -> dict:
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -96,6 +96,10 @@ def make_params(kind: int, method: int, prec: str = "fp64", tile_w: int = 0, alp
     p.dense_div = int(t.get("dense_div", 0))
     p.slots = int(t.get("slots", 0))
     p.groups = int(t.get("groups", 0))
+    # served small queries out of hash tables: {"sparse_blocks": B, "sparse_eps": e, "sparse_cap": C}
+    p.sparse_blocks = int(t.get("sparse_blocks", 0))
+    p.sparse_cap = int(t.get("sparse_cap", 0))
+    p.sparse_eps = float(t.get("sparse_eps", 0.0))
     return p
 
 

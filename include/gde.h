@@ -77,6 +77,12 @@ typedef struct {
     int slots;         /* served PPR/Katz local GD: concurrent queries (one residual vector each); 0 = default */
     int groups;        /* served: the grid splits into this many block groups, each advancing its own slots
                           (t % groups) behind its own barrier; 0 = default (one group per slot) */
+    int sparse_blocks; /* served FP32 PPR / Katz local GD with solution rows: this many blocks of the launch
+                          each solve one small query at a time out of an open-addressing table of node
+                          entries instead of dense vectors; 0 = off */
+    int sparse_cap;    /* entries per table (rounded up to a power of two); 0 = default (65536).  A query
+                          that touches more than 3/4 of it moves to the dense slots */
+    double sparse_eps; /* queries with eps >= sparse_eps are small (the table class) */
 } gde_params;
 
 typedef struct {
@@ -97,6 +103,8 @@ typedef struct {
     double edit_ms;             /* gde_feature_update: host time from the call to the push (edit + repair) */
     int prec;                   /* gde_solve / gde_serve: the precision computed in (GDE_FP32 / GDE_FP64);
                                    Katz near its convergence radius is promoted to FP64 */
+    int64_t sparse_queries;     /* served: queries solved out of hash tables (gde_params.sparse_blocks) */
+    int64_t sparse_overflows;   /* served: small queries that outgrew their table and ran in a dense slot */
 } gde_stats;
 
 /* gde_stats.edit_path */

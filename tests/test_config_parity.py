@@ -6,10 +6,11 @@ C1: the 100k-node Chung-Lu graph (power-law exponent 2.1, mean degree 10,
     seed against an FP64 global solve (l1 error and the largest D^-1
     residual, which the stopping rule bounds by eps * alpha).
 C2: the 2.36M-node wiki-talk-shaped graph, served FP32 PPR local GD at
-    eps = 1e-7 (the benchmarked path) over 16 seeds against the FP64 oracle:
-    mean l1 <= 5e-7 and every seed <= 2e-6 (FP32 rounding, plus a node whose
-    FP64 residual lies within rounding of its threshold pushing a round
-    apart, about 2 eps alpha d of l1 each); the operation-count difference is
+    eps = 1e-7 (the benchmarked path) over 32 seeds against the FP64 oracle:
+    every seed l1 <= 1e-6 and the mean <= 3e-7.  A node whose FP64 residual
+    lies within FP32 rounding of its threshold may push a round apart, which
+    moves about 2 eps alpha d of l1; the highest-degree nodes, where that is
+    largest, keep their residual in FP64.  The operation-count difference is
     reported.
 C5: the 169k-node InstantGNN graph, two snapshots of 59,375 inserted edges
     on 8 feature columns: FP64 P, R and operation counts against the
@@ -76,16 +77,16 @@ def test_c2_served_fp32_l1_per_seed_against_fp64_oracle():
     Gd = api.Graph(g.indptr, g.indices)
     alpha, eps = 0.1, 1e-7
     deg = g.degree.astype(np.float64)
-    seeds = graphs.uniform_seeds(g, 16, seed=515151)
+    seeds = graphs.uniform_seeds(g, 32, seed=515151)
     res = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, eps, prec="fp32", alpha=alpha, tile_w=1, want_r=False,
-                    tuning={"slots": 16})
+                    tuning={"slots": 32})
     oo, xo = O.ppr_gd_many(g.n, g.indptr, g.indices, deg, seeds, alpha, eps, local=True, keep_x=True)
     l1 = np.abs(res["x"].astype(np.float64) - xo).sum(1)
     od = np.abs(res["oper"] - oo) / oo
     print(f"C2 served FP32 vs FP64 oracle: l1 max {l1.max():.3e} mean {l1.mean():.3e}; "
           f"oper rel diff max {od.max():.3e} (abs {np.abs(res['oper'] - oo).max():.0f})")
-    assert l1.mean() <= 5e-7, l1
-    assert l1.max() <= 2e-6, l1
+    assert l1.mean() <= 3e-7, l1
+    assert l1.max() <= 1e-6, l1
     assert od.max() < 1e-4, od
     Gd.free()
 
