@@ -1646,14 +1646,36 @@ __device__ void admit_query(const PushArgs& a, int t, int it) {
     if (threadIdx.x != 0) return;
     TileState& ts = a.ts[t];
     const ServeQueue& q = a.queue;
-    // the next query in order (the dense-class order when small queries go to
-    // the hash-table blocks), then any query those blocks gave back; group
-    // leaders take queries concurrently
+    // Queries a hash-table block gave back come first (they arrived before
+    // the dense-class queries still queued), then the next query in order
+    // (the dense-class order when small queries go to the hash-table blocks).
+    // Group leaders take queries concurrently.
     const unsigned long long now = globaltimer_ns();
-    const int nd = q.order_d ? q.nd : q.nq;
     int qid = -1;
+    int sp_left = 0;
+    if (q.sp_blocks > 0) {
+        // sp_left is read first: at zero every ovf position has been handed out
+        sp_left = ld_acquire_gpu_i(q.sp_left);
+        for (int tries = 0; tries < 4096 && qid < 0; ++tries) {
+            const int c = ld_volatile_i(q.ovf_next);
+            if (c >= ld_volatile_i(q.ovf_cnt)) break;
+            if (atomicCAS(q.ovf_next, c, c + 1) == c) {
+                // the position is handed out before its id is stored: wait for it (bounded)
+                int v = ld_volatile_i(&q.ovf[c]);
+                for (unsigned long long k = 0; v < 0; ++k) {
+                    if (k > (a.spin_limit ? a.spin_limit : (1ull << 26))) {
+                        atomicCAS(a.err, 0, GDE_EHANG);
+                        return;
+                    }
+                    v = ld_volatile_i(&q.ovf[c]);
+                }
+                qid = v;
+            }
+        }
+    }
     bool dense_left = true;
-    if (q.arrival_ns) {
+    const int nd = q.order_d ? q.nd : q.nq;
+    if (qid < 0 && q.arrival_ns) {
         // block 0 stamps the launch start; other groups may get here first
         const unsigned long long st0 = *(volatile const unsigned long long*)&a.stats->start_ns;
         if (st0 == 0) return;
@@ -1670,42 +1692,18 @@ __device__ void admit_query(const PushArgs& a, int t, int it) {
                 break;
             }
         }
-        if (qid < 0 && dense_left) return;  // another leader kept winning: try next round
-    } else {
+    } else if (qid < 0) {
         const int c = atomicAdd(q.next, 1);
         if (c < nd) qid = q.order_d ? q.order_d[c] : c;
         else dense_left = false;
     }
-    if (!dense_left) {
-        if (q.sp_blocks > 0) {
-            // queries whose touched set outgrew a hash table run here
-            // (sp_left is read first: at zero every ovf position has been handed out)
-            const int left = ld_acquire_gpu_i(q.sp_left);
-            for (int tries = 0; tries < 4096 && qid < 0; ++tries) {
-                const int c = ld_volatile_i(q.ovf_next);
-                if (c >= ld_volatile_i(q.ovf_cnt)) break;
-                if (atomicCAS(q.ovf_next, c, c + 1) == c) {
-                    // the position is handed out before its id is stored: wait for it (bounded)
-                    int v = ld_volatile_i(&q.ovf[c]);
-                    for (unsigned long long s = 0; v < 0; ++s) {
-                        if (s > (a.spin_limit ? a.spin_limit : (1ull << 26))) {
-                            atomicCAS(a.err, 0, GDE_EHANG);
-                            return;
-                        }
-                        v = ld_volatile_i(&q.ovf[c]);
-                    }
-                    qid = v;
-                }
-            }
-            if (qid < 0) {
-                // more may come while small queries are still running
-                if (left == 0 && ld_volatile_i(q.ovf_next) >= ld_volatile_i(q.ovf_cnt)) ts.done = SLOT_EMPTY;
-                return;
-            }
-        } else {
+    if (qid < 0) {
+        // nothing now; the slot is done when the dense order is used up and
+        // no hash-table query is left to give one back
+        if (!dense_left &&
+            (q.sp_blocks == 0 || (sp_left == 0 && ld_volatile_i(q.ovf_next) >= ld_volatile_i(q.ovf_cnt))))
             ts.done = SLOT_EMPTY;
-            return;
-        }
+        return;
     }
     const int64_t n = a.g.n;
     const int seed = q.seed[qid];
@@ -1967,6 +1965,9 @@ __device__ void publish_online(const PushArgs& a, int t) {
 constexpr int kSpEmpty = -1;
 constexpr int kSpProbes = 256;
 
+constexpr int kSpLong = 1024;  // rows at least this long are pushed by the whole block
+constexpr int kSpLongMax = 32;
+
 struct SpSh {
     int qid;          // query in hand (-1: none left)
     int cur_cnt, nxt_cnt, used;
@@ -1974,6 +1975,8 @@ struct SpSh {
     int rounds;
     double oper;
     unsigned long long col_nodes;
+    int nlong;                 // frontier rows of at least kSpLong edges this round
+    int long_idx[kSpLongMax];  // their frontier positions
 };
 
 __device__ __forceinline__ unsigned sp_hash(int v) { return (unsigned)v * 2654435761u; }
@@ -1999,6 +2002,38 @@ __device__ __forceinline__ int sp_find_insert(int32_t* keys, int32_t* used_list,
         h = (h + 1u) & mask;
     }
     return -1;
+}
+
+// One edge push of a hash-table query: find or insert the target, add the
+// push value to its FP64 residual, and append it to the next frontier when
+// it crosses its threshold (warp-uniform call: every lane of the warp).
+__device__ __forceinline__ void sp_push_edge(const DevGraph& g, SpSh& sp, int32_t* keys, int32_t* used_list,
+                                             double* R, int32_t* nxt, int cap, double theta, bool act, int64_t e,
+                                             double pv) {
+    const int lane = threadIdx.x & 31;
+    bool cr = false;
+    int h = -1;
+    if (act && !ld_volatile_i(&sp.overflow)) {
+        int v;
+        uint32_t dc;
+        load_edge(g, e, v, dc);
+        h = sp_find_insert(keys, used_list, &sp.used, cap, v);
+        if (h < 0) {
+            sp.overflow = 1;
+        } else {
+            const double old = atomicAdd(&R[h], pv);
+            const double dv = (dc != g.deg_esc) ? (double)dc : g.degd[v];
+            const double thr = theta * dv;
+            cr = (old < thr) && (old + pv >= thr);  // ppr_solver.py:284-288
+        }
+    }
+    const unsigned b = __ballot_sync(kFull, cr);
+    if (b) {
+        int base = 0;
+        if (lane == 0) base = atomicAdd(&sp.nxt_cnt, __popc(b));
+        base = __shfl_sync(kFull, base, 0);
+        if (cr) nxt[base + __popc(b & ((1u << lane) - 1u))] = h;
+    }
 }
 
 __device__ __noinline__ void sparse_block_loop(const PushArgs& a, int c) {
@@ -2084,46 +2119,46 @@ __device__ __noinline__ void sparse_block_loop(const PushArgs& a, int c) {
                 const double du = g.degd[u];
                 push[i] = (kind == KIND_KATZ) ? alpha * r : ((1. - alpha) * r) / du;  // ppr_solver.py:276-281
                 my_oper += du;
+                if (du > (double)((cap >> 2) * 3)) sp.overflow = 1;  // its row alone outgrows the table
             }
             if (my_oper != 0.0) atomicAdd(&sp.oper, my_oper);
             if (threadIdx.x == 0) {
                 sp.nxt_cnt = 0;
+                sp.nlong = 0;
                 sp.rounds += 1;
                 sp.col_nodes += (unsigned long long)nf;
             }
             __syncthreads();
-            // ---- SCATTER: a warp per frontier row, an edge per lane ----
+            // ---- SCATTER: a warp per frontier row, an edge per lane; rows of
+            // kSpLong edges or more (up to kSpLongMax a round) by the whole block ----
             for (int i = warp; i < nf; i += kWarps) {
+                const int u = __ldcg(&keys[cur[i]]);
+                const int len = g.row_len[u];
+                if (len >= kSpLong) {
+                    int slot = kSpLongMax;
+                    if (lane == 0) slot = atomicAdd(&sp.nlong, 1);
+                    slot = __shfl_sync(kFull, slot, 0);
+                    if (slot < kSpLongMax) {
+                        if (lane == 0) sp.long_idx[slot] = i;
+                        continue;
+                    }
+                }
+                const int64_t rp = g.row_ptr[u];
+                const double pv = push[i];
+                for (int j0 = 0; j0 < len; j0 += 32)
+                    sp_push_edge(g, sp, keys, used_list, R, nxt, cap, theta, j0 + lane < len, rp + j0 + lane, pv);
+            }
+            __syncthreads();
+            const int nlong = min(sp.nlong, kSpLongMax);
+            for (int k = 0; k < nlong; ++k) {
+                const int i = sp.long_idx[k];
                 const int u = __ldcg(&keys[cur[i]]);
                 const int64_t rp = g.row_ptr[u];
                 const int len = g.row_len[u];
                 const double pv = push[i];
-                for (int j0 = 0; j0 < len; j0 += 32) {
-                    const int j = j0 + lane;
-                    bool cr = false;
-                    int h = -1;
-                    if (j < len && !ld_volatile_i(&sp.overflow)) {
-                        int v;
-                        uint32_t dc;
-                        load_edge(g, rp + j, v, dc);
-                        h = sp_find_insert(keys, used_list, &sp.used, cap, v);
-                        if (h < 0) {
-                            sp.overflow = 1;
-                        } else {
-                            const double old = atomicAdd(&R[h], pv);
-                            const double dv = (dc != g.deg_esc) ? (double)dc : g.degd[v];
-                            const double thr = theta * dv;
-                            cr = (old < thr) && (old + pv >= thr);  // ppr_solver.py:284-288
-                        }
-                    }
-                    const unsigned b = __ballot_sync(kFull, cr);
-                    if (b) {
-                        int base = 0;
-                        if (lane == 0) base = atomicAdd(&sp.nxt_cnt, __popc(b));
-                        base = __shfl_sync(kFull, base, 0);
-                        if (cr) nxt[base + __popc(b & ((1u << lane) - 1u))] = h;
-                    }
-                }
+                for (int j0 = 0; j0 < len; j0 += kThreads)
+                    sp_push_edge(g, sp, keys, used_list, R, nxt, cap, theta, j0 + (int)threadIdx.x < len,
+                                 rp + j0 + threadIdx.x, pv);
             }
             __syncthreads();
             if (sp.overflow) break;

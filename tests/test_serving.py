@@ -190,3 +190,32 @@ def test_slot_groups_give_the_same_results(cl, groups, arrivals):
     np.testing.assert_allclose(mixed["oper"], ref["oper"], rtol=1e-12)
     for i in range(24):
         assert rel_l1(mixed["x"][i], ref["x"][i]) < FP64_L1, i
+
+
+def test_rows_into_pinned_device_and_pageable_memory_agree(cl):
+    """Pinned host rows are written by the device directly; device rows in place;
+    pageable rows through staging.  All three hold the same values (Katz seed
+    correction and heat-kernel scale included)."""
+    import torch
+    g, Gd = cl
+    nq = 30
+    kinds = np.array([L.PPR, L.KATZ, L.HK] * (nq // 3), dtype=np.int32)
+    seeds = graphs.uniform_seeds(g, nq, seed=27)
+    eps = np.exp(np.random.default_rng(27).uniform(np.log(1e-6), np.log(1e-5), nq))
+    alphas = np.where(kinds == L.KATZ, 1.0 / (float(g.degree.max()) + 1.0), 0.1)
+    kw = dict(alphas=alphas, tau=5.0, prec="fp32", slots=3)
+    pinned = torch.full((nq, g.n), float("nan"), dtype=torch.float32).pin_memory()
+    a = api.serve_mixed(Gd, kinds, seeds, eps, x_out=pinned, device_out=False, **kw)
+    dev = torch.full((nq, g.n), float("nan"), dtype=torch.float32, device="cuda")
+    b = api.serve_mixed(Gd, kinds, seeds, eps, x_out=dev, device_out=True, **kw)
+    c = api.serve_mixed(Gd, kinds, seeds, eps, **kw)  # pageable numpy rows
+    xb = dev.cpu().numpy()
+    assert np.isfinite(pinned.numpy()).all() and np.isfinite(xb).all()
+    for i in range(nq):
+        alone = (api.solve(Gd, L.HK, L.HK_LOCAL, seeds[i:i + 1], eps[i:i + 1], prec="fp64", tau=5.0, want_r=False)
+                 if kinds[i] == L.HK else
+                 api.solve(Gd, int(kinds[i]), L.LOCAL_GD, seeds[i:i + 1], eps[i:i + 1], prec="fp64",
+                           alpha=float(alphas[i]), tile_w=1, want_r=False))
+        for x in (pinned[i].numpy(), xb[i], c["x"][i]):
+            assert rel_l1(x, alone["x"][0]) < 1e-4, (i, int(kinds[i]))
+    np.testing.assert_allclose(a["oper"], b["oper"], rtol=1e-3)
