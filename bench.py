@@ -481,6 +481,7 @@ def run_c3(args):
 
     s0, e0 = batch(0)
     best = tune.autotune(G, L.PPR, s0[:256], e0[:256], prec="fp32", alpha=ALPHA, max_p99_ms=args.max_p99_ms)
+    best = dict(best, tuning=dict(best["tuning"], **parse_tuning(args.tuning)))  # --tuning overrides
     stream = torch.cuda.ExternalStream(api.ctx_stream(ctx), device=f"cuda:{local}")
     flush = torch.empty(512 << 20, dtype=torch.uint8, device=f"cuda:{local}")
     x_dev = torch.empty((Q, g.n), dtype=torch.float32, device=f"cuda:{local}")

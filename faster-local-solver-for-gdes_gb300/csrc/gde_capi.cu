@@ -456,11 +456,19 @@ int solve_served(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t nq, co
     PushArgs& a = tw.a;
     a.small_max = base.small_max; a.med_max = base.med_max; a.chunk = base.chunk;
     a.dense_div = base.dense_div; a.max_rounds = base.max_rounds; a.allow_dense = base.allow_dense;
-    // independent slot groups, each behind its own barrier; the default is
-    // one group per slot (measured best on the 2.36M-node workload at 24 to
-    // 64 slots: a slot's rounds then wait only for the ~10-20 blocks working
-    // on it, and the groups keep the memory system busy while one waits)
-    a.groups = std::max(1, std::min(std::min(p->groups > 0 ? p->groups : S, S), kMaxGroups));
+    // Independent slot groups, each behind its own barrier.  The default is
+    // one group per slot for PPR-only queues (measured best on the 2.36M- and
+    // 100k-node PPR workloads: a slot's rounds wait only for the ~12 blocks
+    // working on it, and the groups keep the memory system busy while one
+    // waits), and one group per 8 slots when the queue holds Katz or
+    // heat-kernel queries, whose frontiers span much of the graph and want
+    // more blocks each (measured on the R-MAT mix: +25% saturation and a
+    // 7x lower p99 at light load than one group per slot).
+    bool wide = (kind == KIND_KATZ || kind == KIND_HK);
+    if (kinds)
+        for (int64_t q = 0; q < nq && !wide; q++) wide = (kinds[q] == KIND_KATZ || kinds[q] == KIND_HK);
+    const int g_default = wide ? std::max(1, S / 8) : S;
+    a.groups = std::max(1, std::min(std::min(p->groups > 0 ? p->groups : g_default, S), kMaxGroups));
     rc = alloc_large(ctx, G, S, tw);
     if (rc != GDE_OK) return rc;
     const size_t es = prec64 ? 8 : 4;

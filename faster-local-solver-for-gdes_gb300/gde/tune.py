@@ -4,10 +4,11 @@ Times ``api.solve`` on a sample of the caller's queries for each candidate
 configuration (device time of the call, best of ``reps``) and keeps the
 fastest, or, with ``max_p99_ms``, the fastest whose 99th-percentile query
 latency (device time from a query's start to its finish) stays within the
-bound.  The search is two-stage: first the execution shape (served slots
+bound.  The search is staged: first the execution shape (served slots
 for single-column tiles, or node x column tiles of width 4..32), then the
 degree-bucket thresholds (rows per lane / per warp, long-row chunk) for the
-winning shape.  Results are cached per graph, kind, precision, sample size
+winning shape, and for served shapes the number of block groups the slots
+share.  Results are cached per graph, kind, precision, sample size
 and latency bound in a JSON file next to the graph cache, so a workload is
 tuned once.
 """
@@ -39,6 +40,9 @@ BUCKETS = [
     {"med_max": 1024, "chunk": 1024},
     {"med_max": 128, "chunk": 128},
 ]
+# served shapes: slots per block group (the engine's default is one group per
+# slot for PPR queues, one per 8 slots with Katz or heat-kernel queries)
+SLOTS_PER_GROUP = [2, 8]
 
 
 def _cache_path(graph: api.Graph, key: str) -> str:
@@ -72,7 +76,8 @@ def _pick(table, max_p99_ms):
 
 
 def autotune(graph: api.Graph, kind: int, seeds, eps, *, prec: str = "fp32", alpha: float = 0.1, reps: int = 2,
-             shapes=None, buckets=None, use_cache: bool = True, max_p99_ms: float | None = None) -> dict:
+             shapes=None, buckets=None, slots_per_group=None, use_cache: bool = True,
+             max_p99_ms: float | None = None) -> dict:
     """Best configuration for solving queries like (seeds, eps) on ``graph``.
 
     ``max_p99_ms``: keep only configurations whose p99 query latency is
@@ -95,6 +100,12 @@ def autotune(graph: api.Graph, kind: int, seeds, eps, *, prec: str = "fp32", alp
         cfg = dict(shape)
         cfg.update(b)
         table.append((cfg, *_time(graph, kind, seeds, eps, prec, alpha, cfg, reps)))
+    best = _pick(table, max_p99_ms)[0]
+    if best.get("tile_w") == 1 and "slots" in best:
+        for spg in (SLOTS_PER_GROUP if slots_per_group is None else slots_per_group):
+            cfg = dict(best)
+            cfg["groups"] = max(1, cfg["slots"] // spg)
+            table.append((cfg, *_time(graph, kind, seeds, eps, prec, alpha, cfg, reps)))
     best, ms, p99 = _pick(table, max_p99_ms)
     out = {"tile_w": best["tile_w"], "tuning": {k: v for k, v in best.items() if k != "tile_w"}, "ms": ms,
            "p99_ms": p99, "max_p99_ms": max_p99_ms, "queries": int(seeds.shape[0]), "table": table}
