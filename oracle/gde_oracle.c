@@ -824,9 +824,12 @@ i64 orc_hk_taylor(i64 n, const i64 *indptr, const i32 *indices, const double *de
 /* (instantGNNParallel allocates p as float32, :55), else float64.          */
 /* qn is the circular queue modulus (n+2 from the callers).                  */
 /* ------------------------------------------------------------------------ */
-static void ign_push(i64 qn, const i64 *indptr, const i32 *indices, const i64 *degree, double alpha,
-                     const double *eps_vec, double omega, int sor, float *p32, double *p64, double *r,
-                     i64 *queue, i64 front, i64 rear, unsigned char *q_mark, double beta) {
+static i64 ign_push(i64 qn, const i64 *indptr, const i32 *indices, const i64 *degree, double alpha,
+                    const double *eps_vec, double omega, int sor, float *p32, double *p64, double *r,
+                    i64 *queue, i64 front, i64 rear, unsigned char *q_mark, double beta) {
+    /* returns the work done, sum of degree[u] over the pushes (the reference
+     * does not count it; this is the count the synchronous form reports) */
+    i64 oper = 0;
     while (rear != front) {
         front = (front + 1) % qn;
         i64 u = queue[front];
@@ -840,6 +843,7 @@ static void ign_push(i64 qn, const i64 *indptr, const i32 *indices, const i64 *d
         double res_u = sor ? omega * r[u] : r[u];
         if (p32) p32[u] = (float)((double)p32[u] + alpha * res_u); else p64[u] += alpha * res_u;
         double push_u = (1. - alpha) * res_u / pow((double)degree[u], 1 - beta);
+        oper += degree[u];
         r[u] = sor ? (1 - omega) * r[u] : 0;
         for (i64 e = indptr[u]; e < indptr[u] + degree[u]; e++) {
             i64 v = indices[e];
@@ -856,11 +860,13 @@ static void ign_push(i64 qn, const i64 *indptr, const i32 *indices, const i64 *d
             q_mark[u] = 1;
         }
     }
+    return oper;
 }
 
 /* instantGNNParallel / instantGNNSorParallel for one column (:46-71, :108-134).
- * r (stride rs) is updated in place; p receives the propagated column. */
-void orc_ign_static_column(i64 n, const i64 *indptr, const i32 *indices, const i64 *degree, double alpha,
+ * r (stride rs) is updated in place; p receives the propagated column.
+ * Returns the push's work (sum of degree[u] over the pushes). */
+i64 orc_ign_static_column(i64 n, const i64 *indptr, const i32 *indices, const i64 *degree, double alpha,
                            double eps, double omega, int sor, double beta, double *p_out, i64 ps, double *r,
                            i64 rs) {
     double *eps_vec = (double *)malloc((size_t)n * sizeof(double));
@@ -877,16 +883,17 @@ void orc_ign_static_column(i64 n, const i64 *indptr, const i32 *indices, const i
             q_mark[i] = 1;
         }
     }
+    i64 oper;
     if (!sor) {
         float *p = (float *)calloc((size_t)n, sizeof(float));
-        ign_push(n + 2, indptr, indices, degree, alpha, eps_vec, 1.0, 0, p, NULL, rc, queue, front, rear, q_mark,
-                 beta);
+        oper = ign_push(n + 2, indptr, indices, degree, alpha, eps_vec, 1.0, 0, p, NULL, rc, queue, front, rear,
+                        q_mark, beta);
         for (i64 i = 0; i < n; i++) p_out[i * ps] = (double)p[i];
         free(p);
     } else {
         double *p = (double *)calloc((size_t)n, sizeof(double));
-        ign_push(n + 2, indptr, indices, degree, alpha, eps_vec, omega, 1, NULL, p, rc, queue, front, rear, q_mark,
-                 beta);
+        oper = ign_push(n + 2, indptr, indices, degree, alpha, eps_vec, omega, 1, NULL, p, rc, queue, front, rear,
+                        q_mark, beta);
         for (i64 i = 0; i < n; i++) p_out[i * ps] = p[i];
         free(p);
     }
@@ -895,6 +902,7 @@ void orc_ign_static_column(i64 n, const i64 *indptr, const i32 *indices, const i
     free(rc);
     free(queue);
     free(q_mark);
+    return oper;
 }
 
 /* updetaGraph (InstantGNN.py:137-180) == updeta_graph (ppr_solver.py:723-766).

@@ -65,7 +65,7 @@ def lib():
         L.orc_hk_sor_sync.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _dbl, _int, _p, _p, _p]
         L.orc_hk_taylor.restype = _i64
         L.orc_hk_taylor.argtypes = [_i64, _p, _p, _p, _i64, _dbl, _dbl, _p]
-        L.orc_ign_static_column.restype = None
+        L.orc_ign_static_column.restype = _i64
         L.orc_ign_static_column.argtypes = [_i64, _p, _p, _p, _dbl, _dbl, _dbl, _int, _dbl, _p, _i64, _p, _i64]
         L.orc_update_graph.restype = None
         L.orc_update_graph.argtypes = [_i64, _p, _p, _p, _p, _p, _i64, _int, _p, _p, _p, _p, _p, _p, _p, _p]
@@ -201,13 +201,19 @@ def _ign_graph(indptr, indices, degree):
 
 
 def ign_static(n, indptr, indices, degree, alpha, eps, P, R, beta, omega=1.0, sor=False):
-    """``instantGNNParallel`` / ``instantGNNSorParallel`` (InstantGNN.py:46-134); P, R (n x F) in place."""
+    """``instantGNNParallel`` / ``instantGNNSorParallel`` (InstantGNN.py:46-134); P, R (n x F) in place.
+
+    Returns the per-column work of the FIFO push (sum of the pushing nodes' degrees; the reference
+    itself returns only run times).
+    """
     indptr, indices, degree = _ign_graph(indptr, indices, degree)
     assert P.dtype == np.float64 and R.dtype == np.float64 and P.flags.c_contiguous and R.flags.c_contiguous
     F = R.shape[1]
+    opers = np.zeros(F, np.int64)
     for f in range(F):
-        lib().orc_ign_static_column(n, _ptr(indptr), _ptr(indices), _ptr(degree), alpha, eps, omega, int(sor), beta,
-                                    P.ctypes.data + 8 * f, F, R.ctypes.data + 8 * f, F)
+        opers[f] = lib().orc_ign_static_column(n, _ptr(indptr), _ptr(indices), _ptr(degree), alpha, eps, omega,
+                                               int(sor), beta, P.ctypes.data + 8 * f, F, R.ctypes.data + 8 * f, F)
+    return opers
 
 
 def update_graph(n, indptr, indices, degree, us, vs, onlyinsert):
