@@ -1044,6 +1044,24 @@ def run_c2_arms(args):
                 arms.append({"method": mname, "prec": prec, "queries_per_s": Q * len(times) / (sum(times) / 1e3),
                              "ms_per_step": sum(times) / len(times), "mean_oper": float(outs[-1]["oper"].mean()),
                              "x": outs[-1]["x"], "oper": outs[-1]["oper"]})
+        # global GD in FP32 (ppr_gd_standard_gpu): every node in every round, so the dense phases (CHECK, the
+        # dense PREP) stream over all n nodes; their share of the launch bounds what staging them could gain
+        kg = 8
+        def gfn(k):
+            return api.solve(G, L.PPR, L.GLOBAL_GD, seeds[:kg], EPS, prec="fp32", alpha=ALPHA, want_r=False,
+                             device_out=True)
+        gfn(0)
+        gt, gouts = _timed_steps(stream, flush, max(1, args.steps // 2), gfn)
+        gst = gouts[-1]["stats"]
+        rounds = int(np.max(gouts[-1]["rounds"]))
+        tw = int(gst["tile_w"])
+        # CHECK reads each node's residual row (tile_w FP32 values) and its FP64 degree once per round
+        check_bytes = float(gst["tiles"]) * rounds * g.n * (4 * tw + 8)
+        global_arm = {"method": "global_gd", "prec": "fp32", "queries": kg, "queries_per_s": kg * len(gt) / (sum(gt) / 1e3),
+                      "ms_per_step": sum(gt) / len(gt), "rounds": rounds, "tile_w": tw, "tiles": int(gst["tiles"]),
+                      "phase_ms": {k: float(gst[k + "_ms"]) for k in ("check", "prep", "scatter")},
+                      "kernel_ms": float(gst["kernel_ms"]),
+                      "check_gbs": check_bytes / max(float(gst["check_ms"]), 1e-9) / 1e6}
     xs = torch.zeros(g.n, dtype=torch.float32, device=f"cuda:{local}")
     api.plain_ppr_local(G, int(seeds[0]), ALPHA, EPS, x_out=xs)
     torch.cuda.synchronize()
@@ -1084,7 +1102,8 @@ def run_c2_arms(args):
         "vs_baseline": None, "dtype": "f32", "data": "synthetic",
         "config": {"workload": "ppr_local_gd_cheby_fp64_fp32_50_seeds_chung_lu_2.36M", "n": g.n, "nnz": g.nnz,
                    "queries_per_step": Q, "alpha": ALPHA, "eps": EPS, "value_arm": "local_gd fp32"},
-        "arms": arms, "plain_gpu": {"value": plain, "unit": "queries/s", "sample": "16 queries"},
+        "arms": arms, "global_gd": global_arm,
+        "plain_gpu": {"value": plain, "unit": "queries/s", "sample": "16 queries"},
         "cpu_baseline": {"value": gd_cpu, "unit": "queries/s", "cores": threads, "kind": "port",
                          "sample": f"{k} of the seeds, ppr_gd local FP64, one per thread; local Chebyshev "
                                    f"(synchronous order) {ch_cpu:.1f} q/s"},

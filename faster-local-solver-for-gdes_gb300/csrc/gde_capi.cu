@@ -1025,6 +1025,14 @@ int gde_graph_upload(gde_ctx* ctx, int64_t n, int64_t cap, const int64_t* indptr
             delete G;
             return fail(ctx, GDE_EINVAL, "column index out of range at position " + std::to_string(j));
         }
+    if (row_len)  // ... but a row's live entries are node ids
+        for (int64_t u = 0; u < n; u++)
+            for (int64_t j = indptr[u]; j < indptr[u] + len0[u]; j++)
+                if (indices[j] == n) {
+                    delete G;
+                    return fail(ctx, GDE_EINVAL, "row " + std::to_string(u) + " holds the padding sentinel at "
+                                "position " + std::to_string(j) + ", inside its row length");
+                }
     std::vector<int32_t> col_new;
     const int32_t* col_src = indices;
     int64_t cap_new = cap;

@@ -7,19 +7,16 @@
 // GPU (InstantGNN.py:303-318 for InstantGNN, ppr_solver.py:776-792 for the
 // beta = 0 PPR update); (3) push from the repaired nodes with the engine.
 //
-// Batches run on the device: insert-only batches (device_insert) decide in
-// parallel which edges are inserted and where every new entry lands, with
-// exactly the sequential semantics; batches with deletions
-// (device_mixed_edit) run as a dataflow over the edges in which each edge
-// waits (bounded) on the previous edge of each endpoint.  The caller's host
-// arrays receive the same values afterwards.  Three cases keep a sequential
-// pass on the host, on purpose: a batch with a self-loop (the reference
-// writes both endpoints' appends into one slot and counts two degrees, a
-// quirk not worth a device path), a graph whose degree array is not its row
-// length, and a batch that fills a row (the host pass then reproduces the
-// reference's partial edit before GDE_ECAPACITY is returned).  The host
-// pass's effect on the device graph is uploaded as (position, value) entries
-// plus the new degree tables.
+// Every batch runs on the device; there is no host pass.  Insert-only
+// batches (device_insert) decide in parallel which edges are inserted and
+// where every new entry lands, with exactly the sequential semantics.
+// Batches with deletions or self-loops, and insert-only batches that find a
+// row full, run as a dataflow over the edges (device_mixed_edit) in which
+// each edge waits (bounded) on the previous edge of each endpoint.  An edge
+// that fails (no slack for an insertion, or a self-loop insertion that would
+// make a padding slot part of its row) stops the batch: the edges before it
+// are applied, as the sequential pass would leave them, and its error is
+// returned.  The caller's host arrays receive the same values afterwards.
 #include <cuda_runtime.h>
 
 #include <cmath>
@@ -27,7 +24,6 @@
 #include <chrono>
 #include <cstring>
 #include <string>
-#include <unordered_map>
 #include <vector>
 
 #include "gde_common.cuh"
@@ -58,27 +54,9 @@ void gde_internal_graph_relayout(gde_graph* G, int64_t* row_ptr, int32_t* col, i
 
 namespace {
 
-struct KeyMap {
-    std::vector<int64_t> keys;             // first-insertion order
-    std::vector<std::vector<int64_t>> nbr; // appended neighbours
-    std::unordered_map<int64_t, int64_t> slot;
-    void add(int64_t a, int64_t b) {
-        auto it = slot.find(a);
-        int64_t s;
-        if (it == slot.end()) {
-            s = (int64_t)keys.size();
-            slot.emplace(a, s);
-            keys.push_back(a);
-            nbr.emplace_back();
-        } else {
-            s = it->second;
-        }
-        nbr[s].push_back(b);
-    }
-};
-
-// Per-key repair factors (computed on the host with the C library's pow,
-// in the reference's operation order).
+// Per-key repair factors, in the reference's operation order (from the
+// device power tables of the edit, or computed by gde_feature_repair from the
+// caller's keys).
 struct RepairKey {
     int32_t u;
     int32_t ins_beg, ins_end;   // into nbr[]
@@ -489,21 +467,38 @@ __device__ __forceinline__ void warp_replace_all(int32_t* col, int64_t r, int d,
     if (t0 + lane < d && __ldcg(&col[r + t0 + lane]) == x) col[r + t0 + lane] = y;
 }
 
-// state[0]: set when an insertion found no slack in its rows (the batch is
-// then abandoned and the host pass runs it).  A wait that outlasts
-// `poll_limit` polls sets GDE_EHANG in err; either flag stops every waiter.
-// Since a node's edges run in batch order, the node's insert and delete
-// counters give each applied edge its rank among the node's insertions or
-// deletions (rank[2e], rank[2e + 1] for u, v): the repair's neighbour lists
-// come out in batch order without a sort.
+// A failing edge stops the batch: an insertion that finds no slack in its
+// rows, or a self-loop insertion over a slot that holds no node id (see
+// below).  The edge records (index << 8 | reason) in *fail (atomicMin, so
+// the lowest failing index wins) and raises *state, which stops every
+// waiter; the host then restores the touched rows and runs the prefix of
+// the batch before that edge.  A wait that outlasts `poll_limit` polls sets
+// GDE_EHANG in err.  Since a node's edges run in batch order, the node's
+// insert and delete counters give each applied edge its rank among the
+// node's insertions or deletions (rank[2e], rank[2e + 1] for u, v): the
+// repair's neighbour lists come out in batch order without a sort.
+//
+// Self-loops (u == v) follow the sequential pass literally: a deletion moves
+// u's last entry into the hole, every other u in the row takes the last
+// entry too, and the degree drops by two (InstantGNN.py:159-164); an
+// insertion writes u into one slot and counts two degrees (:171-174), so the
+// slot after it becomes live with whatever it held.  That slot may hold a
+// stale id (the sequential result is then reproduced) or the padding
+// sentinel n, which the next push would read out of bounds: that edge fails
+// with kFailLoopSlot instead.
+constexpr unsigned long long kFailNone = ~0ull;
+enum : int { kFailNoSlack = 1, kFailLoopSlot = 2 };
+
 __global__ void mix_edit_kernel(const int64_t* row_ptr, int32_t* col, int32_t* row_len, const MixOp* ops, int k,
-                                uint8_t* done, uint8_t* outcome, int* ins_cnt, int* del_cnt, int* rank, int* state,
-                                int64_t poll_limit, int* err) {
+                                int only_insert, int64_t n, uint8_t* done, uint8_t* outcome, int* ins_cnt,
+                                int* del_cnt, int* rank, int* state, unsigned long long* fail, int64_t poll_limit,
+                                int* err) {
     const int lane = threadIdx.x & 31;
     const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int nwarps = (gridDim.x * blockDim.x) >> 5;
     for (int e = warp; e < k; e += nwarps) {
         const MixOp op = ops[e];
+        const bool loop = op.u == op.v;
         // row starts and ends never change during the batch: load them before the wait
         const int64_t ru = row_ptr[op.u], ru_end = row_ptr[op.u + 1];
         const int64_t rv = row_ptr[op.v], rv_end = row_ptr[op.v + 1];
@@ -525,43 +520,66 @@ __global__ void mix_edit_kernel(const int64_t* row_ptr, int32_t* col, int32_t* r
         }
         if (!__shfl_sync(0xffffffffu, go, 0)) return;
         __threadfence();  // the predecessors' writes before this edge's reads
-        const int du = __ldcg(&row_len[op.u]), dv = __ldcg(&row_len[op.v]);
+        const int du = __ldcg(&row_len[op.u]), dv = loop ? du : __ldcg(&row_len[op.v]);
         // first position of v in u's row (InstantGNN.py:153-155)
         const int found = warp_find_first(col, ru, du, op.v, lane);
         uint8_t oc = MIX_NOOP;
+        int reason = 0;
         if (found >= 0) {
-            if (du > 1 && dv > 1) {  // the degree-1 guard keeps the edge (:157-158)
+            if (!only_insert && du > 1 && dv > 1) {  // insert-only batches and the degree-1 guard keep it (:157-158)
                 // swap-with-last in u's row; every u in v's row takes v's last entry (:159-162)
                 const int32_t lastv = __ldcg(&col[rv + dv - 1]);
                 if (lane == 0) col[ru + found] = __ldcg(&col[ru + du - 1]);
                 warp_replace_all(col, rv, dv, op.u, lastv, lane);
                 if (lane == 0) {
-                    row_len[op.u] = du - 1;
-                    row_len[op.v] = dv - 1;
+                    if (loop) {
+                        row_len[op.u] = du - 2;  // both decrements land on u (:163-164)
+                    } else {
+                        row_len[op.u] = du - 1;
+                        row_len[op.v] = dv - 1;
+                    }
                 }
                 oc = MIX_DELETE;
             }
-        } else if (ru + du >= ru_end || rv + dv >= rv_end) {
-            // no slack left for the append: nothing is written, the batch stops
-            if (lane == 0) atomicExch(state, 1);
-            return;
+        } else if (ru + du + (loop ? 1 : 0) >= ru_end || rv + dv >= rv_end) {
+            reason = kFailNoSlack;  // no slack left for the append: nothing is written
+        } else if (loop && (uint64_t)(uint32_t)__ldcg(&col[ru + du + 1]) >= (uint64_t)n) {
+            reason = kFailLoopSlot;
         } else {
-            // append to both rows (:171-174)
+            // append to both rows (:171-174); one slot and two degrees for a self-loop
             if (lane == 0) {
                 col[ru + du] = op.v;
                 col[rv + dv] = op.u;
-                row_len[op.u] = du + 1;
-                row_len[op.v] = dv + 1;
+                if (loop) {
+                    row_len[op.u] = du + 2;
+                } else {
+                    row_len[op.u] = du + 1;
+                    row_len[op.v] = dv + 1;
+                }
             }
             oc = MIX_INSERT;
         }
+        if (reason != 0) {
+            if (lane == 0) {
+                atomicMin(fail, ((unsigned long long)e << 8) | (unsigned long long)reason);
+                atomicExch(state, 1);
+            }
+            return;
+        }
         if (lane == 0 && oc != MIX_NOOP) {
             int* c = oc == MIX_INSERT ? ins_cnt : del_cnt;
-            const int a = __ldcg(&c[op.u]), b = __ldcg(&c[op.v]);
-            rank[2 * e] = a;
-            rank[2 * e + 1] = b;
-            c[op.u] = a + 1;
-            c[op.v] = b + 1;
+            const int a = __ldcg(&c[op.u]);
+            if (loop) {
+                rank[2 * e] = a;
+                rank[2 * e + 1] = a + 1;
+                c[op.u] = a + 2;
+            } else {
+                const int b = __ldcg(&c[op.v]);
+                rank[2 * e] = a;
+                rank[2 * e + 1] = b;
+                c[op.u] = a + 1;
+                c[op.v] = b + 1;
+            }
         }
         __threadfence();  // every lane's edit visible before the successors start
         __syncwarp();
@@ -634,7 +652,12 @@ __global__ void mix_gather_kernel(const int64_t* row_ptr, const int32_t* col, co
 // insertions (keys), their repair factors and neighbour lists, on the device.
 struct DeviceEdit {
     int status = GDE_OK;
-    bool fallback = false;       // the host pass runs the batch instead
+    bool fallback = false;       // device_insert only: the dataflow pass runs the batch instead
+    // A failing edge (no slack for an insertion, or a self-loop insertion
+    // over a slot without a node id): the edges before it are applied, its
+    // error is returned after that partial edit, and nothing is pushed.
+    int late_status = GDE_OK;
+    const char* late_msg = nullptr;
     const int32_t* keys = nullptr;
     int nkeys = 0;
     RepairKey* rkeys = nullptr;
@@ -643,34 +666,14 @@ struct DeviceEdit {
 };
 
 DeviceEdit device_mixed_edit(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t* h_degree, const int32_t* us,
-                             const int32_t* vs, int64_t k, int kind, double beta, uint8_t* outcome) {
+                             const int32_t* vs, int64_t k, int only_insert, int kind, double beta,
+                             uint8_t* outcome) {
     DeviceEdit M;
     const int64_t n = G->g.n;
     const int64_t* indptr;
     const int64_t* hlen;
     int64_t nn;
     gde_internal_graph_host(G, &indptr, &hlen, &nn);
-    if (k >= ((int64_t)1 << 30)) { M.fallback = true; return M; }
-    for (int64_t e = 0; e < k; e++)
-        if (us[e] == vs[e]) { M.fallback = true; return M; }  // self-loops keep the host pass
-    // each edge's predecessor on either endpoint: the last earlier edge touching it
-    std::vector<int32_t>& last = G->edit_last;  // -1 outside this function
-    if ((int64_t)last.size() != n) last.assign((size_t)n, -1);
-    std::vector<MixOp> ops((size_t)k);
-    std::vector<int32_t> touched;
-    for (int64_t e = 0; e < k; e++) {
-        const int32_t u = us[e], v = vs[e];
-        MixOp& op = ops[(size_t)e];
-        op.u = u;
-        op.v = v;
-        op.pu = last[u];
-        op.pv = last[v];
-        if (op.pu < 0) touched.push_back(u);
-        if (op.pv < 0) touched.push_back(v);
-        last[u] = last[v] = (int32_t)e;
-    }
-    for (const int32_t u : touched) last[u] = -1;
-    const int64_t nt = (int64_t)touched.size();
     cudaStream_t st = ctx->stream;
     auto ws = [&](const char* name, size_t bytes) { return gde_internal_wsget(ctx, name, std::max<size_t>(bytes, 8)); };
     MixOp* d_ops = (MixOp*)ws("mix_ops", (size_t)k * sizeof(MixOp));
@@ -679,51 +682,80 @@ DeviceEdit device_mixed_edit(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int
     int* d_rank = (int*)ws("mix_rank", (size_t)k * 8);
     int* d_icnt = (int*)ws("mix_icnt", (size_t)n * 4);
     int* d_dcnt = (int*)ws("mix_dcnt", (size_t)n * 4);
-    int* d_state = (int*)ws("mix_state", 8);
-    int32_t* d_nodes = (int32_t*)ws("mix_nodes", (size_t)nt * 4);
-    if (!d_ops || !d_done || !d_out || !d_rank || !d_icnt || !d_dcnt || !d_state || !d_nodes) {
+    int* d_state = (int*)ws("mix_state", 16);
+    unsigned long long* d_fail = (unsigned long long*)ws("mix_fail", 8);
+    int32_t* d_nodes = (int32_t*)ws("mix_nodes", (size_t)std::min<int64_t>(2 * k, n) * 4);
+    if (!d_ops || !d_done || !d_out || !d_rank || !d_icnt || !d_dcnt || !d_state || !d_fail || !d_nodes) {
         M.status = gde_internal_fail(ctx, GDE_ENOMEM, "edit batch buffers");
         return M;
     }
     auto ck = [&](cudaError_t e2, const char* what) {
         if (e2 != cudaSuccess && M.status == GDE_OK) M.status = gde_internal_fail(ctx, GDE_ECUDA, what);
     };
-    ck(cudaMemcpyAsync(d_ops, ops.data(), (size_t)k * sizeof(MixOp), cudaMemcpyHostToDevice, st), "edit upload");
-    ck(cudaMemcpyAsync(d_nodes, touched.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, st), "edit upload");
-    ck(cudaMemsetAsync(d_done, 0, (size_t)k, st), "edit init");
-    ck(cudaMemsetAsync(d_icnt, 0, (size_t)n * 4, st), "edit init");
-    ck(cudaMemsetAsync(d_dcnt, 0, (size_t)n * 4, st), "edit init");
-    ck(cudaMemsetAsync(d_state, 0, 8, st), "edit init");
-    ck(cudaMemsetAsync(ctx->derr, 0, sizeof(int), st), "edit init");
     int per_sm = 0;
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mix_edit_kernel, kEdT, 0);
-    const int64_t want = (k * 32 + kEdT - 1) / kEdT;  // a warp per edge at most
-    const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(per_sm, 1) * ctx->sms, want));
     const int64_t* row_ptr = G->g.row_ptr;
     int32_t* col = G->col;
     int32_t* rl = G->row_len;
-    int ki = (int)k;
-    // a wait is bounded by the whole batch running in sequence (>= 1 us a poll)
-    int64_t poll_limit = std::max<int64_t>((int64_t)1 << 22, 64 * k);
-    if (ctx->wait_limit > 0) poll_limit = ctx->wait_limit;
     int* err = ctx->derr;
-    void* args[] = {(void*)&row_ptr, (void*)&col,    (void*)&rl,     (void*)&d_ops,   (void*)&ki,
-                    (void*)&d_done,  (void*)&d_out,  (void*)&d_icnt, (void*)&d_dcnt,  (void*)&d_rank,
-                    (void*)&d_state, (void*)&poll_limit, (void*)&err};
-    if (M.status == GDE_OK)
-        ck(cudaLaunchCooperativeKernel((void*)mix_edit_kernel, dim3(grid), dim3(kEdT), args, 0, st), "edit launch");
-    int herr = 0, hfull = 0;
-    ck(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st), "edit status");
-    ck(cudaMemcpyAsync(&hfull, d_state, 4, cudaMemcpyDeviceToHost, st), "edit status");
-    if (outcome) ck(cudaMemcpyAsync(outcome, d_out, (size_t)k, cudaMemcpyDeviceToHost, st), "edit outcomes");
-    ck(cudaStreamSynchronize(st), "edit kernel");
-    if (M.status != GDE_OK) return M;
-    if (herr != 0 || hfull != 0) {
-        // An insertion found a row full (or a wait ran out).  Edges after it
-        // in batch order may already be applied, so the touched rows go back
-        // to the caller's arrays (still unedited); for a full row the host
-        // pass then reproduces the reference's partial edit and its capacity
-        // error.
+    // The batch runs as one dataflow pass.  If an edge fails, the rows the
+    // pass touched go back to the caller's arrays (still unedited) and the
+    // prefix before the lowest failing edge runs again; every edge of that
+    // prefix saw exactly its sequential state, so the prefix shrinks to the
+    // first edge that fails in batch order, whose error is then returned
+    // after the edit of the edges before it.
+    int64_t kk = k;
+    std::vector<int32_t>& last = G->edit_last;  // -1 outside this function
+    if ((int64_t)last.size() != n) last.assign((size_t)n, -1);
+    std::vector<MixOp> ops;
+    std::vector<int32_t> touched;
+    for (;;) {
+        // each edge's predecessor on either endpoint: the last earlier edge touching it
+        ops.assign((size_t)kk, MixOp{});
+        touched.clear();
+        for (int64_t e = 0; e < kk; e++) {
+            const int32_t u = us[e], v = vs[e];
+            MixOp& op = ops[(size_t)e];
+            op.u = u;
+            op.v = v;
+            op.pu = last[u];
+            op.pv = last[v];
+            if (op.pu < 0) touched.push_back(u);
+            if (op.pv < 0 && v != u) touched.push_back(v);
+            last[u] = last[v] = (int32_t)e;
+        }
+        for (const int32_t u : touched) last[u] = -1;
+        const int64_t nt = (int64_t)touched.size();
+        ck(cudaMemcpyAsync(d_ops, ops.data(), (size_t)kk * sizeof(MixOp), cudaMemcpyHostToDevice, st), "edit upload");
+        ck(cudaMemcpyAsync(d_nodes, touched.data(), (size_t)nt * 4, cudaMemcpyHostToDevice, st), "edit upload");
+        ck(cudaMemsetAsync(d_done, 0, (size_t)kk, st), "edit init");
+        ck(cudaMemsetAsync(d_icnt, 0, (size_t)n * 4, st), "edit init");
+        ck(cudaMemsetAsync(d_dcnt, 0, (size_t)n * 4, st), "edit init");
+        ck(cudaMemsetAsync(d_state, 0, 16, st), "edit init");
+        ck(cudaMemsetAsync(d_fail, 0xff, 8, st), "edit init");
+        ck(cudaMemsetAsync(ctx->derr, 0, sizeof(int), st), "edit init");
+        const int64_t want = (kk * 32 + kEdT - 1) / kEdT;  // a warp per edge at most
+        const int grid = (int)std::max<int64_t>(1, std::min<int64_t>((int64_t)std::max(per_sm, 1) * ctx->sms, want));
+        int ki = (int)kk;
+        int64_t nl = n;
+        // a wait is bounded by the whole batch running in sequence (>= 1 us a poll)
+        int64_t poll_limit = std::max<int64_t>((int64_t)1 << 22, 64 * kk);
+        if (ctx->wait_limit > 0) poll_limit = ctx->wait_limit;
+        void* args[] = {(void*)&row_ptr, (void*)&col,    (void*)&rl,     (void*)&d_ops,   (void*)&ki,
+                        (void*)&only_insert, (void*)&nl, (void*)&d_done, (void*)&d_out,  (void*)&d_icnt,
+                        (void*)&d_dcnt,  (void*)&d_rank, (void*)&d_state, (void*)&d_fail, (void*)&poll_limit,
+                        (void*)&err};
+        if (M.status == GDE_OK)
+            ck(cudaLaunchCooperativeKernel((void*)mix_edit_kernel, dim3(grid), dim3(kEdT), args, 0, st),
+               "edit launch");
+        int herr = 0;
+        unsigned long long hfail = kFailNone;
+        ck(cudaMemcpyAsync(&herr, err, sizeof(int), cudaMemcpyDeviceToHost, st), "edit status");
+        ck(cudaMemcpyAsync(&hfail, d_fail, 8, cudaMemcpyDeviceToHost, st), "edit status");
+        ck(cudaStreamSynchronize(st), "edit kernel");
+        if (M.status != GDE_OK) return M;
+        if (herr == 0 && hfail == kFailNone) break;
+        // The touched rows go back to the caller's (unedited) arrays.
         std::vector<int64_t> nodes, pos;
         std::vector<int32_t> val;
         nodes.reserve(touched.size());
@@ -736,14 +768,27 @@ DeviceEdit device_mixed_edit(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int
         }
         M.status = gde_internal_graph_refresh_nodes(ctx, G, h_degree, nodes.data(), (int64_t)nodes.size(),
                                                     pos.data(), val.data(), (int64_t)pos.size(), NAN, 0);
-        if (M.status == GDE_OK && herr != 0)
+        if (M.status != GDE_OK) return M;
+        if (herr != 0) {
             M.status = gde_internal_fail(ctx, GDE_EHANG, "edit batch: a device-side wait ran out");
-        M.fallback = true;
-        return M;
+            return M;
+        }
+        kk = (int64_t)(hfail >> 8);
+        if ((int)(hfail & 0xff) == kFailNoSlack) {
+            M.late_status = GDE_ECAPACITY;
+            M.late_msg = "padded row has no slack for an insertion";
+        } else {
+            M.late_status = GDE_EINVAL;
+            M.late_msg = "a self-loop insertion would make a padding slot (no node id) part of the row";
+        }
+        if (kk == 0) return M;  // nothing before the failing edge
     }
+    if (outcome) ck(cudaMemcpyAsync(outcome, d_out, (size_t)kk, cudaMemcpyDeviceToHost, st), "edit outcomes");
+    const int64_t nt = (int64_t)touched.size();
+    const int ki = (int)kk;
     // ---- repair lists, keys and degree tables, all on the device ----
     const int nbk = (int)std::min<int64_t>(4096, (n + kEdT - 1) / kEdT + 1);
-    const int tb = (int)std::min<int64_t>(4096, (k + kEdT - 1) / kEdT + 1);
+    const int tb = (int)std::min<int64_t>(4096, (kk + kEdT - 1) / kEdT + 1);
     int* d_size = (int*)ws("mix_size", (size_t)n * 4);
     int* d_off = (int*)ws("mix_off", (size_t)(n + 1) * 4);
     int* d_flag = (int*)ws("mix_flag", (size_t)n * 4);
@@ -1043,228 +1088,96 @@ static int feature_update_impl(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, i
         G->dmax = -1.0;  // the degree bound recomputed and the spectral estimate dropped
         G->lam_max_est = NAN;
     }
-    // ---- the edit, the repair keys and the push all on the device: insert-only
-    // batches in one pass, batches with deletions as a dataflow over the edges ----
-    bool dev_ok = k > 0 && G->deg_is_len;
-    for (int64_t e = 0; dev_ok && e < k; e++)
-        dev_ok = us[e] >= 0 && us[e] < n && vs[e] >= 0 && vs[e] < n && us[e] != vs[e];
-    if (dev_ok) {
-        if (kind == KIND_IGN) {
-            int rc0 = gde_internal_ign_tables(ctx, G, p->beta);
-            if (rc0 == GDE_OK) rc0 = ensure_power_tables(ctx, G, p->beta);
-            if (rc0 != GDE_OK) return rc0;
-        }
-        DeviceEdit D = only_insert ? device_insert(ctx, G, h_indices, h_degree, us, vs, k, kind, p->beta, outcome)
-                                   : device_mixed_edit(ctx, G, h_indices, h_degree, us, vs, k, kind, p->beta, outcome);
-        if (D.status != GDE_OK) return D.status;
-        // InstantGNN tables built for an earlier call are not updated by this
-        // kind's edit: the next InstantGNN call rebuilds them
-        if (kind != KIND_IGN) G->ign_beta = NAN;
-        if (!D.fallback && edit_only) {
-            if (stats) {
-                memset(stats, 0, sizeof(*stats));
-                stats->edit_path = only_insert ? GDE_EDIT_DEVICE_INSERT : GDE_EDIT_DEVICE_DATAFLOW;
-                stats->edit_ms = since_entry();
-            }
-            return GDE_OK;
-        }
-        if (!D.fallback) {
-            cudaStream_t st = gde_internal_stream(ctx);
-            const int prec64 = (p->prec == GDE_FP64);
-            if (D.nkeys > 0) {
-                const int64_t total = (int64_t)D.nkeys * F;
-                const int blocks = (int)((total + 255) / 256);
-                if (prec64) {
-                    repair_pass1<double><<<blocks, 256, 0, st>>>(D.rkeys, D.nkeys, (double*)Pm, (double*)Rm, ld, F,
-                                                                  kind, p->alpha);
-                    repair_pass2<double><<<blocks, 256, 0, st>>>(D.rkeys, D.nkeys, D.nbr, (const double*)Pm,
-                                                                  (double*)Rm, (const double*)Xm, ld, F, kind,
-                                                                  p->alpha, gde_internal_npush(G),
-                                                                  gde_internal_degd(G));
-                } else {
-                    repair_pass1<float><<<blocks, 256, 0, st>>>(D.rkeys, D.nkeys, (float*)Pm, (float*)Rm, ld, F,
-                                                                 kind, p->alpha);
-                    repair_pass2<float><<<blocks, 256, 0, st>>>(D.rkeys, D.nkeys, D.nbr, (const float*)Pm,
-                                                                 (float*)Rm, (const float*)Xm, ld, F, kind, p->alpha,
-                                                                 gde_internal_npush(G), gde_internal_degd(G));
-                }
-                cudaError_t e = cudaGetLastError();
-                if (e != cudaSuccess) return gde_internal_fail(ctx, GDE_ECUDA, cudaGetErrorString(e));
-            }
-            std::vector<double> opers(F, 0.0);
-            const double edit_ms = since_entry();
-            if (D.nkeys > 0) {
-                int rc = gde_internal_feature_push(ctx, G, p, F, Pm, Rm, ld, eps, D.keys, D.nkeys, opers.data(),
-                                                   stats);
-                if (rc != GDE_OK) return rc;
-            } else if (stats) {
-                memset(stats, 0, sizeof(*stats));
-            }
-            // the beta = 0 PPR update counts the repair work (ppr_solver.py:776-792)
-            const double oper_repair = 2.0 * (double)D.nkeys + (double)D.repair_nbr;
-            if (oper_out)
-                for (int64_t c = 0; c < F; c++) oper_out[c] = opers[c] + (kind == KIND_UPPR ? oper_repair : 0.0);
-            if (stats) {
-                stats->edit_path = only_insert ? GDE_EDIT_DEVICE_INSERT : GDE_EDIT_DEVICE_DATAFLOW;
-                stats->edit_ms = edit_ms;
-            }
-            return GDE_OK;
-        }
-    }
-    std::vector<int64_t> old_degree(h_degree, h_degree + n);
-    // ---- (1) sequential edit, InstantGNN.py:147-179 ----
-    KeyMap ins, del;
-    std::vector<int64_t> pos;
-    std::vector<int32_t> val;
-    int status = GDE_OK;
+    // ---- the edit, the repair keys and the push, all on the device ----
+    if (k >= ((int64_t)1 << 30)) return gde_internal_fail(ctx, GDE_EINVAL, "edge batch too large (2^30 edges at most)");
+    bool loops = false;
     for (int64_t e = 0; e < k; e++) {
-        int64_t u = us[e], v = vs[e];
-        if (u < 0 || u >= n || v < 0 || v >= n) { status = GDE_EINVAL; break; }
-        bool insertion = true;
-        for (int64_t i = indptr[u]; i < indptr[u] + h_degree[u]; i++) {
-            if (v == h_indices[i]) {
-                insertion = false;
-                if (only_insert || h_degree[u] == 1 || h_degree[v] == 1) break;
-                int64_t lu = indptr[u] + h_degree[u] - 1;
-                h_indices[i] = h_indices[lu];
-                pos.push_back(i); val.push_back(h_indices[i]);
-                for (int64_t kk = indptr[v]; kk < indptr[v] + h_degree[v]; kk++)
-                    if (u == h_indices[kk]) {
-                        h_indices[kk] = h_indices[indptr[v] + h_degree[v] - 1];
-                        pos.push_back(kk); val.push_back(h_indices[kk]);
-                    }
-                h_degree[u] -= 1;
-                h_degree[v] -= 1;
-                del.add(u, v);
-                del.add(v, u);
-                if (outcome) outcome[e] = MIX_DELETE;
-                break;
-            }
-        }
-        if (insertion) {
-            if (indptr[u] + h_degree[u] >= indptr[u + 1] || indptr[v] + h_degree[v] >= indptr[v + 1] ||
-                (u == v && indptr[u] + h_degree[u] + 1 >= indptr[u + 1])) {
-                status = GDE_ECAPACITY;
-                break;
-            }
-            int64_t pu = indptr[u] + h_degree[u], pv = indptr[v] + h_degree[v];
-            h_indices[pu] = (int32_t)v;
-            pos.push_back(pu); val.push_back((int32_t)v);
-            h_indices[pv] = (int32_t)u;
-            pos.push_back(pv); val.push_back((int32_t)u);
-            h_degree[u] += 1;
-            h_degree[v] += 1;
-            ins.add(u, v);
-            ins.add(v, u);
-            if (outcome) outcome[e] = MIX_INSERT;
-        }
+        if (us[e] < 0 || us[e] >= n || vs[e] < 0 || vs[e] >= n)
+            return gde_internal_fail(ctx, GDE_EINVAL, "edge endpoint out of range");
+        loops = loops || us[e] == vs[e];
     }
-    // A slot can be written more than once (swap-with-last deletions); the
-    // device receives each touched slot once, with its final value.
-    std::sort(pos.begin(), pos.end());
-    pos.erase(std::unique(pos.begin(), pos.end()), pos.end());
-    val.resize(pos.size());
-    for (size_t i = 0; i < pos.size(); i++) val[i] = h_indices[pos[i]];
-    // only the nodes whose degree changed get new degree tables
-    std::vector<int64_t> touched;
-    touched.reserve(ins.keys.size() + del.keys.size());
-    for (int64_t u : ins.keys) touched.push_back(u);
-    for (int64_t u : del.keys) touched.push_back(u);
-    std::sort(touched.begin(), touched.end());
-    touched.erase(std::unique(touched.begin(), touched.end()), touched.end());
-    int rc = gde_internal_graph_refresh_nodes(ctx, G, h_degree, touched.data(), (int64_t)touched.size(), pos.data(),
-                                              val.data(), (int64_t)pos.size(), p->beta, kind == KIND_IGN);
-    if (rc != GDE_OK) return rc;
-    if (status != GDE_OK)
-        return gde_internal_fail(ctx, status, status == GDE_ECAPACITY ? "padded row has no slack for an insertion"
-                                                                      : "edge endpoint out of range");
-    if (edit_only) {
+    // The reference keeps one degree array that is both the row length and
+    // the degree of the thresholds; an edit sets both from the new row.
+    if (k > 0 && !G->deg_is_len)
+        return gde_internal_fail(ctx, GDE_EINVAL, "edge batches need a padded graph whose degree is its row length");
+    if (k == 0) {
+        if (oper_out)
+            for (int64_t c = 0; c < F; c++) oper_out[c] = 0.0;
         if (stats) {
             memset(stats, 0, sizeof(*stats));
-            stats->edit_path = GDE_EDIT_HOST;
+            stats->edit_path = only_insert ? GDE_EDIT_DEVICE_INSERT : GDE_EDIT_DEVICE_DATAFLOW;
             stats->edit_ms = since_entry();
         }
         return GDE_OK;
     }
-    // ---- (2) repair at the touched nodes ----
-    std::vector<RepairKey> keys;
-    std::vector<int32_t> nbr;
-    double oper_repair = 2.0 * (double)ins.keys.size();
-    for (size_t s = 0; s < ins.keys.size(); s++) {
-        RepairKey K{};
-        int64_t u = ins.keys[s];
-        K.u = (int32_t)u;
-        double d = (double)h_degree[u], od = (double)old_degree[u];
-        if (kind == KIND_IGN) {
-            const double b = p->beta;
-            K.a1 = std::pow(d / od, 1 - b);
-            K.a2 = std::pow(od, 1 - b);
-            K.a3 = std::pow(d, 1 - b);
-            K.b1 = std::pow(od, b);
-            K.b2 = std::pow(d, b);
-        } else {
-            K.a1 = d;
-            K.a2 = od;
+    if (kind == KIND_IGN) {
+        int rc0 = gde_internal_ign_tables(ctx, G, p->beta);
+        if (rc0 == GDE_OK) rc0 = ensure_power_tables(ctx, G, p->beta);
+        if (rc0 != GDE_OK) return rc0;
+    }
+    // Insert-only batches decide every edge in parallel (device_insert); a
+    // batch with deletions or self-loops, or an insert-only batch that finds
+    // a row full, runs as the dataflow over the edges.
+    DeviceEdit D;
+    int path = GDE_EDIT_DEVICE_DATAFLOW;
+    if (only_insert && !loops) {
+        D = device_insert(ctx, G, h_indices, h_degree, us, vs, k, kind, p->beta, outcome);
+        path = GDE_EDIT_DEVICE_INSERT;
+    }
+    if (path == GDE_EDIT_DEVICE_DATAFLOW || (D.status == GDE_OK && D.fallback)) {
+        D = device_mixed_edit(ctx, G, h_indices, h_degree, us, vs, k, only_insert, kind, p->beta, outcome);
+        path = GDE_EDIT_DEVICE_DATAFLOW;
+    }
+    if (D.status != GDE_OK) return D.status;
+    // InstantGNN tables built for an earlier call are not updated by this
+    // kind's edit: the next InstantGNN call rebuilds them
+    if (kind != KIND_IGN) G->ign_beta = NAN;
+    if (D.late_status != GDE_OK || edit_only) {
+        // (a failing edge: the edges before it are applied, on the device and
+        // in the caller's arrays, and nothing is repaired or pushed)
+        if (stats) {
+            memset(stats, 0, sizeof(*stats));
+            stats->edit_path = path;
+            stats->edit_ms = since_entry();
         }
-        K.ins_beg = (int32_t)nbr.size();
-        for (int64_t v : ins.nbr[s]) nbr.push_back((int32_t)v);
-        K.ins_end = (int32_t)nbr.size();
-        oper_repair += (double)ins.nbr[s].size();
-        K.del_beg = K.del_end = K.ins_end;
-        bool use_del = (kind == KIND_UPPR) || !only_insert;
-        auto it = del.slot.find(u);
-        if (use_del && it != del.slot.end()) {
-            for (int64_t v : del.nbr[it->second]) nbr.push_back((int32_t)v);
-            K.del_end = (int32_t)nbr.size();
-            oper_repair += (double)del.nbr[it->second].size();
-        }
-        keys.push_back(K);
+        return D.late_status != GDE_OK ? gde_internal_fail(ctx, D.late_status, D.late_msg) : GDE_OK;
     }
     cudaStream_t st = gde_internal_stream(ctx);
     const int prec64 = (p->prec == GDE_FP64);
-    std::vector<int32_t> cand;
-    if (!keys.empty()) {
-        RepairKey* d_keys = (RepairKey*)gde_internal_wsget(ctx, "repair_keys", keys.size() * sizeof(RepairKey));
-        int32_t* d_nbr = (int32_t*)gde_internal_wsget(ctx, "repair_nbr", std::max<size_t>(nbr.size(), 1) * 4);
-        if (!d_keys || !d_nbr) return gde_internal_fail(ctx, GDE_ENOMEM, "repair tables");
-        cudaMemcpyAsync(d_keys, keys.data(), keys.size() * sizeof(RepairKey), cudaMemcpyHostToDevice, st);
-        if (!nbr.empty()) cudaMemcpyAsync(d_nbr, nbr.data(), nbr.size() * 4, cudaMemcpyHostToDevice, st);
-        int64_t total = (int64_t)keys.size() * F;
-        int blocks = (int)((total + 255) / 256);
+    if (D.nkeys > 0) {
+        const int64_t total = (int64_t)D.nkeys * F;
+        const int blocks = (int)((total + 255) / 256);
         if (prec64) {
-            repair_pass1<double><<<blocks, 256, 0, st>>>(d_keys, (int)keys.size(), (double*)Pm, (double*)Rm, ld, F,
-                                                          kind, p->alpha);
-            repair_pass2<double><<<blocks, 256, 0, st>>>(d_keys, (int)keys.size(), d_nbr, (const double*)Pm,
-                                                          (double*)Rm, (const double*)Xm, ld, F, kind, p->alpha,
+            repair_pass1<double><<<blocks, 256, 0, st>>>(D.rkeys, D.nkeys, (double*)Pm, (double*)Rm, ld, F, kind,
+                                                          p->alpha);
+            repair_pass2<double><<<blocks, 256, 0, st>>>(D.rkeys, D.nkeys, D.nbr, (const double*)Pm, (double*)Rm,
+                                                          (const double*)Xm, ld, F, kind, p->alpha,
                                                           gde_internal_npush(G), gde_internal_degd(G));
         } else {
-            repair_pass1<float><<<blocks, 256, 0, st>>>(d_keys, (int)keys.size(), (float*)Pm, (float*)Rm, ld, F, kind,
+            repair_pass1<float><<<blocks, 256, 0, st>>>(D.rkeys, D.nkeys, (float*)Pm, (float*)Rm, ld, F, kind,
                                                          p->alpha);
-            repair_pass2<float><<<blocks, 256, 0, st>>>(d_keys, (int)keys.size(), d_nbr, (const float*)Pm, (float*)Rm,
+            repair_pass2<float><<<blocks, 256, 0, st>>>(D.rkeys, D.nkeys, D.nbr, (const float*)Pm, (float*)Rm,
                                                          (const float*)Xm, ld, F, kind, p->alpha,
                                                          gde_internal_npush(G), gde_internal_degd(G));
         }
         cudaError_t e = cudaGetLastError();
         if (e != cudaSuccess) return gde_internal_fail(ctx, GDE_ECUDA, cudaGetErrorString(e));
-        for (auto& K : keys) cand.push_back(K.u);
     }
-    // ---- (3) push from the repaired nodes (InstantGNN.py:315-325) ----
+    // ---- push from the repaired nodes (InstantGNN.py:315-325) ----
     std::vector<double> opers(F, 0.0);
     const double edit_ms = since_entry();
-    if (!cand.empty()) {
-        int32_t* d_cand = (int32_t*)gde_internal_wsget(ctx, "update_cand", cand.size() * 4);
-        if (!d_cand) return gde_internal_fail(ctx, GDE_ENOMEM, "candidate list");
-        cudaMemcpyAsync(d_cand, cand.data(), cand.size() * 4, cudaMemcpyHostToDevice, st);
-        rc = gde_internal_feature_push(ctx, G, p, F, Pm, Rm, ld, eps, d_cand, (int64_t)cand.size(), opers.data(),
-                                       stats);
+    if (D.nkeys > 0) {
+        int rc = gde_internal_feature_push(ctx, G, p, F, Pm, Rm, ld, eps, D.keys, D.nkeys, opers.data(), stats);
         if (rc != GDE_OK) return rc;
     } else if (stats) {
         memset(stats, 0, sizeof(*stats));
     }
+    // the beta = 0 PPR update counts the repair work (ppr_solver.py:776-792)
+    const double oper_repair = 2.0 * (double)D.nkeys + (double)D.repair_nbr;
     if (oper_out)
         for (int64_t c = 0; c < F; c++) oper_out[c] = opers[c] + (kind == KIND_UPPR ? oper_repair : 0.0);
     if (stats) {
-        stats->edit_path = GDE_EDIT_HOST;
+        stats->edit_path = path;
         stats->edit_ms = edit_ms;
     }
     return GDE_OK;

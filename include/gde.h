@@ -108,10 +108,11 @@ typedef struct {
 } gde_stats;
 
 /* gde_stats.edit_path */
-#define GDE_EDIT_HOST 0             /* sequential host pass (a self-loop, a degree array that is not the row
-                                       length, or a row without slack for an insertion) */
-#define GDE_EDIT_DEVICE_INSERT 1    /* insert-only batch on the device */
-#define GDE_EDIT_DEVICE_DATAFLOW 2  /* batch with deletions on the device, as a dataflow over the edges */
+#define GDE_EDIT_HOST 0             /* not reported by this library (every batch runs on the device); kept so
+                                       the values of the other two stay fixed */
+#define GDE_EDIT_DEVICE_INSERT 1    /* insert-only batch on the device, every edge decided in parallel */
+#define GDE_EDIT_DEVICE_DATAFLOW 2  /* batch with deletions or self-loops, or an insert-only batch that found a
+                                       row full: on the device, as a dataflow over the edges */
 
 /* ---- context / errors ---- */
 const char *gde_status_str(int status);
@@ -316,7 +317,15 @@ int gde_feature_push(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t F,
  * pushes from the repaired nodes (with p->omega as gde_feature_push; the
  * colouring is rebuilt for the edited graph).  Replaces instantGNNUpdateBatchParallel
  * (InstantGNN.py:332-359) and update_ppr_parallel (ppr_solver.py:824-849).
- * X may be NULL for GDE_UPPR. */
+ * X may be NULL for GDE_UPPR.  The whole edit runs on the device.  Before
+ * anything is edited, an endpoint outside [0, n) or a graph uploaded with a
+ * degree array that is not its row length gives GDE_EINVAL.  An edge that
+ * fails stops the batch after the edges before it, which stay applied (in
+ * the caller's arrays and on the device), and nothing is repaired or pushed:
+ * an insertion into a row without slack gives GDE_ECAPACITY; a self-loop
+ * insertion, which the reference writes into one slot while counting two
+ * degrees, gives GDE_EINVAL when the second slot holds the padding sentinel
+ * n (the next push would read it as a node id). */
 int gde_feature_update(gde_ctx *ctx, gde_graph *g, int32_t *h_indices, int64_t *h_degree, const int32_t *us,
                        const int32_t *vs, int64_t k, int only_insert, const gde_params *p, int64_t F, void *P,
                        void *R, const void *X, int64_t ld, double eps, double *oper_out, gde_stats *stats);
@@ -328,9 +337,10 @@ int gde_feature_update(gde_ctx *ctx, gde_graph *g, int32_t *h_indices, int64_t *
  * caller's host arrays h_indices / h_degree and the resident graph.
  * outcome (host, may be NULL): k bytes, per edge 0 = no change, 1 = inserted,
  * 2 = deleted, from which the caller rebuilds the reference's
- * insert_neighbor / delete_neighbor maps in batch order.  A row without
- * slack stops the batch (GDE_ECAPACITY) after the edges before it, as the
- * sequential pass would.  stats (may be NULL) gets edit_path and edit_ms. */
+ * insert_neighbor / delete_neighbor maps in batch order.  Errors as for
+ * gde_feature_update: a row without slack stops the batch (GDE_ECAPACITY)
+ * after the edges before it, as the sequential pass would.  stats (may be
+ * NULL) gets edit_path and edit_ms. */
 int gde_graph_update(gde_ctx *ctx, gde_graph *g, int32_t *h_indices, int64_t *h_degree, const int32_t *us,
                      const int32_t *vs, int64_t k, int only_insert, uint8_t *outcome, gde_stats *stats);
 

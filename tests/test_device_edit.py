@@ -7,9 +7,12 @@ rows.  The device pass keeps that sequential meaning exactly: each edge waits
 until every earlier edge that shares an endpoint has been applied.  These
 tests check, on padded graphs with slack, that the device pass ran
 (``gde_stats.edit_path``) and that the edited arrays, the repaired residuals
-and the push are the same as the oracle's sequential pass.  A batch whose
-insertion finds a row full is handed to the host pass, which applies the
-edges before it and reports ``GDE_ECAPACITY``.
+and the push are the same as the oracle's sequential pass.  Every batch
+runs on the device: a batch whose insertion finds a row full applies the
+edges before it and reports ``GDE_ECAPACITY``; self-loops follow the
+sequential pass literally, and a self-loop insertion that would make a
+padding slot part of its row reports ``GDE_EINVAL`` after the edges before
+it.
 """
 import numpy as np
 import pytest
@@ -20,7 +23,7 @@ from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 
-EDIT_HOST, EDIT_DEVICE_DATAFLOW = 0, 2
+EDIT_DEVICE_DATAFLOW = 2
 
 
 def _padded(g, slack):
@@ -122,9 +125,9 @@ def test_row_touched_more_often_than_its_slack_stays_on_the_device():
     assert res["stats"]["edit_path"] == EDIT_DEVICE_DATAFLOW
 
 
-def test_batch_that_fills_a_row_gives_the_host_pass_partial_edit_and_error():
-    """A row without slack for an insertion: the device run is abandoned, the touched rows go back to
-    the caller's arrays, and the host pass applies the edges before that one and reports the error."""
+def test_batch_that_fills_a_row_applies_the_edges_before_it_and_errors():
+    """A row without slack for an insertion: the device run stops, the touched rows go back to the
+    caller's arrays, the edges before that one run again on the device, and the error is reported."""
     import torch
     g = graphs.chung_lu(3000, 2.2, 6.0, 120.0, seed=24)
     n = g.n
@@ -312,3 +315,149 @@ def test_device_edit_rules_on_tiny_graphs(case):
     assert res["stats"]["edit_path"] == EDIT_DEVICE_DATAFLOW
     np.testing.assert_array_equal(ix, ix_o)
     np.testing.assert_array_equal(dg, dg_o)
+
+
+def _loop_graph(slack=4):
+    """A 12-node ring with three chords, padded; node 3 carries a self-loop entry the way the
+    reference's data format stores one (one slot, one degree, data_process_GNN.py:103-105)."""
+    n = 12
+    edges = [(i, (i + 1) % n) for i in range(n)] + [(0, 6), (2, 8), (4, 10)]
+    ip, ix, dg = _tiny_padded(n, edges, slack)
+    ix[ip[3] + dg[3]] = 3
+    dg[3] += 1
+    return n, ip, ix, dg
+
+
+def _edit_and_push(n, ip, ix, dg, us, vs, only_insert, Gd=None):
+    """gde_feature_update (PPR update, FP64) against the oracle's sequential edit + synchronous push."""
+    import torch
+    us = np.asarray(us, np.int32)
+    vs = np.asarray(vs, np.int32)
+    ix_o, dg_o = ix.copy(), dg.copy()
+    F = 2
+    Po = np.zeros((F, n))
+    Ro = np.zeros((F, n))
+    Ro[0, 1] = 0.2
+    Ro[1, 7] = 0.2
+    if Gd is None:
+        Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    P = torch.from_numpy(np.ascontiguousarray(Po.T)).cuda()
+    R = torch.from_numpy(np.ascontiguousarray(Ro.T)).cuda()
+    oo = O.update_ppr(n, ip, ix_o, dg_o, 0.2, 1e-4, 1.0, Po, Ro, us, vs, sync=True)
+    res = api.feature_update(Gd, L.UPPR, ix, dg, us, vs, only_insert, P, R, None, 1e-4, alpha=0.2, prec="fp64",
+                             tile_w=1)
+    assert res["stats"]["edit_path"] == EDIT_DEVICE_DATAFLOW
+    np.testing.assert_array_equal(ix, ix_o)
+    np.testing.assert_array_equal(dg, dg_o)
+    np.testing.assert_allclose(res["oper"], oo, rtol=1e-12)
+    np.testing.assert_allclose(P.cpu().numpy().T, Po, rtol=1e-9, atol=1e-13)
+    np.testing.assert_allclose(R.cpu().numpy().T, Ro, rtol=1e-9, atol=1e-13)
+    return Gd
+
+
+def test_self_loop_deletion_on_the_device():
+    """(3, 3) on a row that holds its loop: the loop leaves, every other 3 in the row takes the
+    row's last entry, and the degree drops by two (InstantGNN.py:159-164)."""
+    n, ip, ix, dg = _loop_graph()
+    _edit_and_push(n, ip, ix, dg, [1, 3, 5], [7, 3, 9], False)
+
+
+def test_self_loop_insertion_over_a_stale_slot_matches_the_sequential_pass():
+    """Two deletions leave node 0's old entries behind its row; (0, 0) then writes one slot and
+    counts two degrees, so the second slot's stale id joins the row, as in the reference."""
+    n, ip, ix, dg = _loop_graph()
+    Gd = _edit_and_push(n, ip, ix, dg, [0, 0], [1, 11], False)
+    assert dg[0] == 1
+    _edit_and_push(n, ip, ix, dg, [0, 2], [0, 9], False, Gd)
+    assert dg[0] == 3 and ix[ip[0] + 1] == 0 and ix[ip[0] + 2] < n
+
+
+def test_insert_only_batch_with_self_loops_on_the_device():
+    """An insert-only batch with self-loops runs as the dataflow: (3, 3) on the loop's row is
+    kept; the stale-slot insertion of a self-loop matches the sequential pass."""
+    n, ip, ix, dg = _loop_graph()
+    Gd = _edit_and_push(n, ip, ix, dg, [0, 0], [1, 11], False)
+    us = np.array([3, 5, 0], np.int32)
+    vs = np.array([3, 1, 0], np.int32)
+    ix_o, dg_o = ix.copy(), dg.copy()
+    O.update_graph(n, ip, ix_o, dg_o, us, vs, True)
+    res = api.graph_update(Gd, ix, dg, us, vs, True)
+    assert res["stats"]["edit_path"] == EDIT_DEVICE_DATAFLOW
+    np.testing.assert_array_equal(res["outcome"], [0, 1, 1])
+    np.testing.assert_array_equal(ix, ix_o)
+    np.testing.assert_array_equal(dg, dg_o)
+    fresh = api.Graph(ip, ix.copy(), row_len=dg.copy(), degree=dg.astype(np.float64))
+    a = api.solve(Gd, L.PPR, L.LOCAL_GD, [0, 5], 1e-6, prec="fp64", alpha=0.15, tile_w=1)
+    b = api.solve(fresh, L.PPR, L.LOCAL_GD, [0, 5], 1e-6, prec="fp64", alpha=0.15, tile_w=1)
+    np.testing.assert_array_equal(a["oper"], b["oper"])
+    np.testing.assert_allclose(a["x"], b["x"], rtol=1e-12, atol=1e-16)
+
+
+@pytest.mark.parametrize("only_insert", [False, True])
+def test_self_loop_insertion_over_the_padding_sentinel_is_an_error(only_insert):
+    """(7, 7) on a row whose next free slots hold the sentinel n: the reference would make the
+    sentinel part of the row and its next push would read it as a node id.  The edges before it
+    stay applied, the error is GDE_EINVAL, and the device graph equals a fresh upload."""
+    import torch
+    n, ip, ix, dg = _loop_graph()
+    us = np.array([1, 7, 2], np.int32)
+    vs = np.array([5, 7, 9], np.int32)
+    ix_o, dg_o = ix.copy(), dg.copy()
+    O.update_graph(n, ip, ix_o, dg_o, us[:1], vs[:1], only_insert)
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    P = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    R = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    with pytest.raises(L.GDEError) as ei:
+        api.feature_update(Gd, L.UPPR, ix, dg, us, vs, only_insert, P, R, None, 1e-4, alpha=0.2, prec="fp64",
+                           tile_w=1)
+    assert ei.value.status == L.GDE_EINVAL
+    np.testing.assert_array_equal(ix, ix_o)
+    np.testing.assert_array_equal(dg, dg_o)
+    fresh = api.Graph(ip, ix.copy(), row_len=dg.copy(), degree=dg.astype(np.float64))
+    a = api.solve(Gd, L.PPR, L.LOCAL_GD, [1, 7], 1e-6, prec="fp64", alpha=0.15, tile_w=1)
+    b = api.solve(fresh, L.PPR, L.LOCAL_GD, [1, 7], 1e-6, prec="fp64", alpha=0.15, tile_w=1)
+    np.testing.assert_array_equal(a["oper"], b["oper"])
+    np.testing.assert_allclose(a["x"], b["x"], rtol=1e-12, atol=1e-16)
+
+
+def test_endpoint_out_of_range_edits_nothing():
+    import torch
+    n, ip, ix, dg = _loop_graph()
+    ix0, dg0 = ix.copy(), dg.copy()
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    P = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    R = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    for bad in (n, -1):
+        with pytest.raises(L.GDEError) as ei:
+            api.feature_update(Gd, L.UPPR, ix, dg, np.array([1, bad], np.int32), np.array([5, 2], np.int32), False,
+                               P, R, None, 1e-4, alpha=0.2, prec="fp64", tile_w=1)
+        assert ei.value.status == L.GDE_EINVAL
+        np.testing.assert_array_equal(ix, ix0)
+        np.testing.assert_array_equal(dg, dg0)
+
+
+def test_insert_only_batch_that_fills_a_row_applies_the_edges_before_it():
+    """An insert-only batch whose parallel pass finds a row full runs as the dataflow, which
+    applies the edges before the failing insertion and reports GDE_ECAPACITY."""
+    import torch
+    n, ip, ix, dg = _loop_graph(slack=2)
+    us = np.array([1, 2, 1, 1, 4], np.int32)
+    vs = np.array([5, 6, 7, 9, 8], np.int32)  # node 1 takes a third insertion with two free slots
+    ix_o, dg_o = ix.copy(), dg.copy()
+    O.update_graph(n, ip, ix_o, dg_o, us[:3], vs[:3], True)
+    Gd = api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    P = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    R = torch.zeros((n, 1), dtype=torch.float64, device="cuda")
+    with pytest.raises(L.GDEError) as ei:
+        api.feature_update(Gd, L.UPPR, ix, dg, us, vs, True, P, R, None, 1e-4, alpha=0.2, prec="fp64", tile_w=1)
+    assert ei.value.status == L.GDE_ECAPACITY
+    np.testing.assert_array_equal(ix, ix_o)
+    np.testing.assert_array_equal(dg, dg_o)
+
+
+def test_upload_rejects_the_padding_sentinel_inside_a_row():
+    n, ip, ix, dg = _loop_graph()
+    ix[ip[4] + 1] = n
+    with pytest.raises(L.GDEError) as ei:
+        api.Graph(ip, ix, row_len=dg, degree=dg.astype(np.float64))
+    assert ei.value.status == L.GDE_EINVAL
