@@ -76,6 +76,18 @@ __device__ __forceinline__ bool ge_threshold(float r, float t32, double theta, d
     return (double)r >= theta * d;
 }
 
+// The same decision for a threshold that is not theta times an integer
+// degree (InstantGNN's theta d^(1-beta), the heat kernel's theta d / (N psi)):
+// t32 is its FP32 approximation, within 2^-21 (relative) of the FP64 value
+// thr64() -- a few roundings of 2^-24 each -- so the 2^-20 band still
+// brackets it, and thr64() is evaluated only inside the band.
+template <typename F>
+__device__ __forceinline__ bool ge_band(float r, float t32, F thr64) {
+    if (r >= t32 * (1.f + 0x1p-20f)) return true;
+    if (r < t32 * (1.f - 0x1p-20f)) return false;
+    return (double)r >= thr64();
+}
+
 // ---------------------------------------------------------------------------
 // Vector helpers: VEC contiguous columns per lane.
 // ---------------------------------------------------------------------------
@@ -328,6 +340,7 @@ __device__ void check_phase(const PushArgs& a, int t, int it, int* s_cnt) {
     constexpr int L = W / VEC;
     __shared__ int s_live[kMaxW];
     __shared__ double s_theta[kMaxW];
+    __shared__ float s_theta_f[kMaxW];
     __shared__ int s_par;
     const int64_t n = a.g.n;
     const T* R = slab_ptr<T>(a.R, a, t);
@@ -336,9 +349,14 @@ __device__ void check_phase(const PushArgs& a, int t, int it, int* s_cnt) {
         const ColState& c = a.cs[(int64_t)t * W + threadIdx.x];
         s_live[threadIdx.x] = (threadIdx.x < a.tp[t].ncols) && c.live;
         s_theta[threadIdx.x] = c.theta;
+        s_theta_f[threadIdx.x] = (float)c.theta;
         s_cnt[threadIdx.x] = 0;
     }
     __syncthreads();
+    // FP32 tiles on integer degrees test in FP32 (exact through the band of
+    // ge_threshold) and read the 4-byte degree: FP64 is a small fraction of
+    // the FP32 rate on GB300, and this phase touches every node.
+    const bool f32 = (sizeof(T) == 4) && a.g.degf_exact;
     int lane_g = threadIdx.x % L;
     int c0 = lane_g * VEC;
     int cnt[VEC];
@@ -349,11 +367,19 @@ __device__ void check_phase(const PushArgs& a, int t, int it, int* s_cnt) {
     for (int64_t u = gid; u < n; u += ng) {
         Vec<T, VEC> rv;
         vload<T, VEC>(R + u * a.ld + c0, rv);
-        double d = a.g.degd[u];
+        if (f32) {
+            const float df = a.g.degf[u];
 #pragma unroll
-        for (int i = 0; i < VEC; ++i) {
-            double thr = s_theta[c0 + i] * d;
-            cnt[i] += (s_live[c0 + i] && fabs((double)rv.v[i]) >= thr) ? 1 : 0;
+            for (int i = 0; i < VEC; ++i)
+                cnt[i] += (s_live[c0 + i] && ge_threshold(fabsf((float)rv.v[i]), s_theta_f[c0 + i] * df,
+                                                          s_theta[c0 + i], (double)df)) ? 1 : 0;
+        } else {
+            double d = a.g.degd[u];
+#pragma unroll
+            for (int i = 0; i < VEC; ++i) {
+                double thr = s_theta[c0 + i] * d;
+                cnt[i] += (s_live[c0 + i] && fabs((double)rv.v[i]) >= thr) ? 1 : 0;
+            }
         }
     }
 #pragma unroll
@@ -706,13 +732,24 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
     int my_nodes[VEC];
     double thr_scale[VEC];
     bool live[VEC];
+    // FP32 tiles on integer degrees decide and push in FP32, as the W = 1
+    // path does: each threshold test is exact through the FP64 band
+    // (ge_band), and the push value is formed in FP32, the tile's precision.
+    // FP64 is a small fraction of the FP32 rate on GB300, and a dense round
+    // visits every node and column.  Chebyshev keeps its recurrence in FP64.
+    const bool f32 = (sizeof(T) == 4) && g.degf_exact && !cheby;
+    float thr_f[VEC];
+    const double hk_div = hk ? (double)sh.tp.n_levels * sh.psi : 1.0;
 #pragma unroll
     for (int k = 0; k < VEC; ++k) {
         my_oper[k] = 0.0;
         my_nodes[k] = 0;
         live[k] = sh.col_live[c0 + k] != 0;
         thr_scale[k] = sh.col_theta[c0 + k];
+        thr_f[k] = (float)(hk ? thr_scale[k] / hk_div : thr_scale[k]);
     }
+    const float alpha_f = (float)alpha, omalpha_f = (float)(1. - alpha), xgain_f = (float)sh.tp.x_gain;
+    const float hkc_f = hk ? (float)(sh.tp.tau / ((double)sh.level + 1.)) : 0.f;
     double my_vol = 0.0;
     int my_cnt = 0;
 
@@ -736,22 +773,30 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
             bool absorb = false;
             bool any = false;
             Vec<T, VEC> r;
+            float df = 1.f;
             if (valid) {
                 u = sh.dense ? (int)i : cand[i];
                 const int64_t off = (int64_t)u * a.ld + c0;
                 const int64_t xoff = (int64_t)u * xld + c0;
                 vload<T, VEC>(R + off, r);
                 // fast test first: most scanned nodes are below every threshold
-                du = g.degf_exact ? (double)g.degf[u] : g.degd[u];
+                df = g.degf[u];
+                du = g.degf_exact ? (double)df : g.degd[u];
                 const double thr_base = (kind == KIND_IGN) ? g.nfac[u] : du;
+                const float base_f = (kind == KIND_IGN) ? (float)thr_base : df;
     #pragma unroll
                 for (int k = 0; k < VEC; ++k) {
                     if (!live[k]) continue;
-                    const double rv = (double)r.v[k];
                     bool a_k;
                     if (global) {
-                        a_k = (rv != 0.0);
+                        a_k = (r.v[k] != T(0));
+                    } else if (f32) {
+                        a_k = ge_band(fabsf((float)r.v[k]), thr_f[k] * base_f, [&] {
+                            return hk ? ((thr_scale[k] * thr_base) / (double)sh.tp.n_levels) / sh.psi
+                                      : thr_scale[k] * thr_base;
+                        });
                     } else {
+                        const double rv = (double)r.v[k];
                         double thr;
                         if (hk) thr = ((thr_scale[k] * thr_base) / (double)sh.tp.n_levels) / sh.psi;
                         else thr = thr_scale[k] * thr_base;
@@ -772,8 +817,8 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
                     }
                 }
                 if (any) {
-                    du = g.degd[u];
                     absorb = ign && is_absorbing(g, u);
+                    const float npush_f = (f32 && kind == KIND_IGN) ? (float)g.npush[u] : 1.f;
                     Vec<T, VEC> dxv;
                     if (cheby) vload<T, VEC>(DX + off, dxv);
                     Vec<T, VEC> xadd;
@@ -799,7 +844,22 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
                             // An absorbing node (threshold 0) is visited once by the
                             // reference's initial scan and never re-enqueued; with a
                             // zero residual it has nothing to absorb.
-                            if (absorb && rv == 0.0) { act[k] = false; continue; }
+                            if (absorb && r.v[k] == T(0)) { act[k] = false; continue; }
+                            if (f32) {
+                                const float rf = (float)r.v[k];
+                                float pvf;
+                                if (kind == KIND_PPR || kind == KIND_UPPR) pvf = (omalpha_f * rf) / df;
+                                else if (kind == KIND_KATZ) pvf = alpha_f * rf;
+                                else if (kind == KIND_HK) pvf = sh.final_level ? rf / df : (hkc_f * rf) / df;
+                                else pvf = (omalpha_f * rf) / npush_f;
+                                push.v[k] = absorb ? T(0) : (T)pvf;
+                                xadd.v[k] = (kind == KIND_IGN && !absorb) ? (T)(xgain_f * rf) : r.v[k];
+                                r.v[k] = T(0);
+                                wrote = true;
+                                my_nodes[k] += 1;
+                                if (!absorb) my_oper[k] += du;
+                                continue;
+                            }
                             double pv;
                             if (kind == KIND_PPR || kind == KIND_UPPR) pv = ((1. - alpha) * rv) / du;
                             else if (kind == KIND_KATZ) pv = alpha * rv;
