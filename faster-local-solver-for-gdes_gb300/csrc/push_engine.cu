@@ -907,15 +907,17 @@ __device__ void prep_range(const PushArgs& a, int t, const TileSh& sh, PrepSh& p
                                 }
                         } else if (XC) {
                             // Kahan-compensated FP32 accumulation of the solution
+                            Vec<float, VEC> cc;
+                            vload<float, VEC>(XC + xoff, cc);
     #pragma unroll
                             for (int k = 0; k < VEC; ++k)
                                 if (act[k]) {
-                                    float cc = XC[xoff + k];
-                                    float y = (float)xadd.v[k] - cc;
+                                    float y = (float)xadd.v[k] - cc.v[k];
                                     float s = (float)xv.v[k] + y;
-                                    XC[xoff + k] = (s - (float)xv.v[k]) - y;
+                                    cc.v[k] = (s - (float)xv.v[k]) - y;
                                     xv.v[k] = (T)s;
                                 }
+                            vstore<float, VEC>(XC + xoff, cc);
                         } else {
     #pragma unroll
                             for (int k = 0; k < VEC; ++k)
@@ -1106,10 +1108,30 @@ template <typename T, int VEC>
 __device__ __forceinline__ void push_edge(const DevGraph& g, T* tgt, int64_t ld, int c0, int v, const Vec<T, VEC>& p,
                                           bool tgt_scale);
 
+// Did an addition take node v's residual from `old` to `s` across its
+// threshold theta * d_v?  Exact; FP32 residuals on integer degrees decide in
+// FP32 outside the band of ge_threshold.
+template <typename T>
+__device__ __forceinline__ bool crossed(const DevGraph& g, int v, T old, T s, double theta, float theta_f) {
+    if constexpr (sizeof(T) == 4) {
+        if (g.degf_exact) {
+            const float df = g.degf[v];
+            const float t32 = theta_f * df;
+            return !ge_threshold((float)old, t32, theta, (double)df) && ge_threshold((float)s, t32, theta, (double)df);
+        }
+    }
+    const double thr = theta * (g.degf_exact ? (double)g.degf[v] : g.degd[v]);
+    return ((double)old < thr) && ((double)s >= thr);
+}
+
 template <typename T, int VEC>
-__device__ __forceinline__ void load_thetas(const ColState* cs, int c0, bool cross, double (&theta)[VEC]) {
+__device__ __forceinline__ void load_thetas(const ColState* cs, int c0, bool cross, double (&theta)[VEC],
+                                            float (&theta_f)[VEC]) {
 #pragma unroll
-    for (int k = 0; k < VEC; ++k) theta[k] = cross ? cs[c0 + k].theta : 0.0;
+    for (int k = 0; k < VEC; ++k) {
+        theta[k] = cross ? cs[c0 + k].theta : 0.0;
+        theta_f[k] = (float)theta[k];
+    }
 }
 
 // One edge of a push for the L lanes of a group: add p into row v of the
@@ -1117,7 +1139,8 @@ __device__ __forceinline__ void load_thetas(const ColState* cs, int c0, bool cro
 // every touched v (sparse tracking).  Every lane of the warp must call it.
 template <typename T, int W, int VEC, int L>
 __device__ __forceinline__ void edge_step(const PushArgs& a, const ScatterCtx<T, W>& c, bool ok, int v, int c0,
-                                          int lane_g, int grp_w, const Vec<T, VEC>& p, const double (&theta)[VEC]) {
+                                          int lane_g, int grp_w, const Vec<T, VEC>& p, const double (&theta)[VEC],
+                                          const float (&theta_f)[VEC]) {
     bool cr = false;
     bool combined = false;
     if constexpr (VEC == 1 && L == 1) {
@@ -1143,9 +1166,7 @@ __device__ __forceinline__ void edge_step(const PushArgs& a, const ScatterCtx<T,
                     if (c.cross) {
                         const T old = atomicAdd(addr, tot);
                         const T s = old + tot;
-                        const double dv = a.g.degf_exact ? (double)a.g.degf[v] : a.g.degd[v];
-                        const double thr = theta[0] * dv;
-                        cr = ((double)old < thr) && ((double)s >= thr);
+                        cr = crossed<T>(a.g, v, old, s, theta[0], theta_f[0]);
                     } else {
                         atomicAdd(addr, tot);
                     }
@@ -1159,13 +1180,11 @@ __device__ __forceinline__ void edge_step(const PushArgs& a, const ScatterCtx<T,
         if (c.cross) {
             Vec<T, VEC> old;
             vatomic_ret<T, VEC>(c.tgt + (int64_t)v * c.tld + c0, p, old);
-            const double dv = a.g.degf_exact ? (double)a.g.degf[v] : a.g.degd[v];
 #pragma unroll
             for (int k = 0; k < VEC; ++k) {
                 if (p.v[k] == T(0)) continue;
                 const T s = old.v[k] + p.v[k];  // the value the atomic stored
-                const double thr = theta[k] * dv;
-                cr |= ((double)old.v[k] < thr) && ((double)s >= thr);
+                cr |= crossed<T>(a.g, v, old.v[k], s, theta[k], theta_f[k]);
             }
         } else {
             push_edge<T, VEC>(a.g, c.tgt, c.tld, c0, v, p, c.tgt_scale);
@@ -1210,7 +1229,8 @@ __device__ void scatter_warp_items(const PushArgs& a, const PushItem* items, int
     const int lane_g = lane % L, grp_w = lane / L;
     const int c0 = lane_g * VEC;
     double theta[VEC];
-    load_thetas<T, VEC>(c.cs, c0, c.cross, theta);
+    float theta_f[VEC];
+    load_thetas<T, VEC>(c.cs, c0, c.cross, theta, theta_f);
     for (long long k = beg + warp; k < end; k += kWarps) {
         const PushItem it = items[k * step];
         Vec<T, VEC> p;
@@ -1219,7 +1239,7 @@ __device__ void scatter_warp_items(const PushArgs& a, const PushItem* items, int
             const int j = j0 + grp_w;
             const bool ok = j < it.len;
             const int v = ok ? g.col[it.rp + j] : 0;
-            edge_step<T, W, VEC, L>(a, c, ok, v, c0, lane_g, grp_w, p, theta);
+            edge_step<T, W, VEC, L>(a, c, ok, v, c0, lane_g, grp_w, p, theta, theta_f);
         }
     }
 }
@@ -1560,7 +1580,8 @@ __device__ void scatter_small_flat(const PushArgs& a, int t, const ScatterCtx<T,
     const int c0 = lane_g * VEC;
     const PushItem* bsmall = a.bsmall + (int64_t)t * a.g.n;
     double theta[VEC];
-    load_thetas<T, VEC>(c.cs, c0, c.cross, theta);
+    float theta_f[VEC];
+    load_thetas<T, VEC>(c.cs, c0, c.cross, theta, theta_f);
     for (long long kb = beg + (long long)warp * GPW; kb < end; kb += (long long)kWarps * GPW) {
         const long long k = kb + grp_w;
         int len = 0;
@@ -1599,7 +1620,7 @@ __device__ void scatter_small_flat(const PushArgs& a, int t, const ScatterCtx<T,
 #pragma unroll
             for (int i = 0; i < VEC; ++i) pr.v[i] = __shfl_sync(kFull, p.v[i], r * L + lane_g);
             const int v = ok ? g.col[rpr + (e - exr)] : 0;
-            edge_step<T, W, VEC, L>(a, c, ok, v, c0, lane_g, grp_w, pr, theta);
+            edge_step<T, W, VEC, L>(a, c, ok, v, c0, lane_g, grp_w, pr, theta, theta_f);
         }
     }
 }
