@@ -12,6 +12,7 @@ from __future__ import annotations
 import ctypes
 import os
 import subprocess
+import threading
 
 import numpy as np
 
@@ -21,6 +22,7 @@ OUT_DIR = os.path.join(HERE, "_build")
 LIB = os.path.join(OUT_DIR, "libgde_oracle.so")
 
 _lib = None
+_lib_lock = threading.Lock()  # the first call may come from several worker threads at once
 _i64 = ctypes.c_int64
 _dbl = ctypes.c_double
 _int = ctypes.c_int
@@ -32,7 +34,7 @@ def build(force: bool = False) -> str:
     os.makedirs(OUT_DIR, exist_ok=True)
     if not force and os.path.exists(LIB) and os.path.getmtime(LIB) >= os.path.getmtime(SRC):
         return LIB
-    tmp = LIB + f".{os.getpid()}.tmp"
+    tmp = LIB + f".{os.getpid()}.{threading.get_ident()}.tmp"
     cmd = ["gcc", "-O2", "-fPIC", "-shared", "-fopenmp", "-ffp-contract=off", "-std=c99", SRC, "-o", tmp, "-lm"]
     subprocess.run(cmd, check=True)
     os.replace(tmp, LIB)
@@ -40,6 +42,11 @@ def build(force: bool = False) -> str:
 
 
 def lib():
+    with _lib_lock:
+        return _lib if _lib is not None else _load()
+
+
+def _load():
     global _lib
     if _lib is None:
         build()
