@@ -15,10 +15,10 @@ exactly; that is tested in ``test_gpu_parity.py`` and ``test_sor.py``):
 * ``hk_sor_queue`` local with omega != 1 (hk_solver.py:206-295): the GPU
   relaxes each node to its threshold at every level.
 
-This file reports, on the 100k-node Chung-Lu graph of the CPU-baseline
-configuration, how the operation count and the error against the FP64 truth
-of the GPU's order compare with the reference's order, both computed by the
-oracle.  Run with ``-s`` to print the table.  The asserted bounds are wide;
+This file reports, on the 100k-node Chung-Lu graph (exponent 2.1, mean
+degree 10, maximum 2,000), how the operation count and the error against the
+FP64 truth of the GPU's order compare with the reference's order, both
+computed by the oracle.  Run with ``-s`` to print the table.  The asserted bounds are wide;
 the measured ratios are the point.
 """
 import numpy as np
