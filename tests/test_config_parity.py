@@ -15,6 +15,8 @@ C2: the 2.36M-node wiki-talk-shaped graph, served FP32 PPR local GD at
 C5: the 169k-node InstantGNN graph, two snapshots of 59,375 inserted edges
     on 8 feature columns: FP64 P, R and operation counts against the
     oracle's synchronous update per snapshot; FP32 within a stated bound.
+C3: 64 seeds in the tuned 8-column node x seed tiles, eps log-uniform in
+    [1e-8, 1e-5], FP32 against the FP64 oracle at each seed's eps.
 FP32 global GD (ppr_gd_standard_gpu, katz_gd_standard_gpu) on the C1 graph.
 """
 import numpy as np
@@ -70,6 +72,29 @@ def test_c1_fp32_global_gd_ppr_and_katz(c1):
             assert abs(iters - iters_o) <= 1, (kind, i, iters, iters_o)
             err = np.abs(res["x"][i].astype(np.float64) - xo).sum() / np.abs(xo).sum()
             assert err < 1e-5, (kind, i, err)
+
+
+def test_c3_node_seed_tiles_fp32_against_fp64_oracle(c1):
+    """C3's tuned shape: 64 seeds in 8-column node x seed tiles (short rows up to 16 edges), eps
+    log-uniform in [1e-8, 1e-5], FP32 residuals.  Every seed within the FP32 flip bound of its own
+    eps (a threshold tie at a node of degree d moves about 2 eps alpha d of l1), the mean relative
+    l1 below 2e-5, operation counts within 0.1%."""
+    g, Gd = c1
+    alpha = 0.1
+    deg = g.degree.astype(np.float64)
+    rng = np.random.default_rng(2)
+    seeds = graphs.uniform_seeds(g, 64, seed=3)
+    eps = np.exp(rng.uniform(np.log(1e-8), np.log(1e-5), 64))
+    res = api.solve(Gd, L.PPR, L.LOCAL_GD, seeds, eps, prec="fp32", alpha=alpha, tile_w=8,
+                    tuning={"small_max": 16})
+    rels = []
+    for i, s in enumerate(seeds):
+        xo, _, oo = O.ppr_gd(g.n, g.indptr, g.indices, deg, int(s), alpha, float(eps[i]), True)
+        rel = np.abs(res["x"][i].astype(np.float64) - xo).sum() / np.abs(xo).sum()
+        rels.append(rel)
+        assert rel < 2e-6 + 3 * 2 * eps[i] * alpha * deg.max(), (i, eps[i], rel)
+        assert abs(res["oper"][i] - oo) <= 1e-3 * oo, (i, res["oper"][i], oo)
+    assert np.mean(rels) < 2e-5, np.mean(rels)
 
 
 def test_c2_served_fp32_l1_per_seed_against_fp64_oracle():
