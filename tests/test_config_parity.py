@@ -76,9 +76,13 @@ def test_c1_fp32_global_gd_ppr_and_katz(c1):
 
 def test_c3_node_seed_tiles_fp32_against_fp64_oracle(c1):
     """C3's tuned shape: 64 seeds in 8-column node x seed tiles (short rows up to 16 edges), eps
-    log-uniform in [1e-8, 1e-5], FP32 residuals.  Every seed within the FP32 flip bound of its own
-    eps (a threshold tie at a node of degree d moves about 2 eps alpha d of l1), the mean relative
-    l1 below 2e-5, operation counts within 0.1%."""
+    log-uniform in [1e-8, 1e-5], FP32 residuals, against the FP64 oracle at each seed's eps.
+
+    A node whose FP64 residual lies within FP32 rounding of its threshold eps alpha d pushes a
+    round apart, which moves about 2 eps alpha d of l1.  Over a query's hundreds of rounds such
+    ties recur: on this graph the worst seeds of both the tiles and the served slots show 3 to 5
+    of them at the largest degree (relative l1 up to 2.6e-4 at eps 2.6e-7), most seeds none.  Each
+    seed is held to 10 at the largest degree, the mean to 2e-5, operation counts to 0.1%."""
     g, Gd = c1
     alpha = 0.1
     deg = g.degree.astype(np.float64)
@@ -92,7 +96,7 @@ def test_c3_node_seed_tiles_fp32_against_fp64_oracle(c1):
         xo, _, oo = O.ppr_gd(g.n, g.indptr, g.indices, deg, int(s), alpha, float(eps[i]), True)
         rel = np.abs(res["x"][i].astype(np.float64) - xo).sum() / np.abs(xo).sum()
         rels.append(rel)
-        assert rel < 2e-6 + 3 * 2 * eps[i] * alpha * deg.max(), (i, eps[i], rel)
+        assert rel < 2e-6 + 10 * 2 * eps[i] * alpha * deg.max(), (i, eps[i], rel)
         assert abs(res["oper"][i] - oo) <= 1e-3 * oo, (i, res["oper"][i], oo)
     assert np.mean(rels) < 2e-5, np.mean(rels)
 
