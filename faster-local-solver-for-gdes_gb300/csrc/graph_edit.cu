@@ -922,7 +922,7 @@ DeviceEdit device_insert(gde_ctx* ctx, gde_graph* G, int32_t* h_indices, int64_t
     DI_CK(cudaStreamSynchronize(st));
     if (herr != 0) {
         // no slack for some insertion (or an overfull hash table): nothing was
-        // written yet; the host pass applies the sequential partial edit
+        // written yet; the dataflow pass applies the sequential partial edit
         R.fallback = true;
         return R;
     }
