@@ -152,9 +152,10 @@ struct OnlineSlot {           // the query a slot holds (copied out of the ring 
     int32_t kind;
     int32_t rounds;
     int32_t status;           // GDE_OK, or GDE_EITERCAP when max_rounds stopped it
-    int32_t pad;
+    int32_t pending;          // 1: `mail` holds a request for this idle slot, not admitted yet
     double oper;
     unsigned long long admit_ns, finish_ns;
+    OnlineReq mail;           // written by the ring reader, read by the slot's own group at admission
 };
 
 struct TileState {            // device-updated
@@ -203,7 +204,9 @@ struct ServeQueue {
     const long long* tail;        // host-written: tickets submitted so far
     long long* head;              // device-written (host-visible): tickets admitted so far
     const int* stop;              // host-written stop flag
-    int* quit;                    // device: every block leaves at the next round start when set
+    int* quit;                    // device: set by the ring reader (stop flag, or idle) for every group
+    int* gquit;                   // device [groups]: each group's copy of quit, taken before its round's
+                                  // last barrier, so that all its blocks leave at the same round start
     unsigned long long* last_ns;  // device: %globaltimer of the last round with work
     unsigned long long idle_ns;   // the launch ends after this long with nothing to do
     OnlineSlot* slot;             // [slots]

@@ -1912,16 +1912,61 @@ __device__ __forceinline__ int ld_relaxed_sys_i(const int* p) {
     return v;
 }
 
-// Block 0, thread 0: the next submitted query into idle slot t, if any.
+// The ring reader (thread 0 of group 0's first block, once per round of that
+// group): submitted requests go, in ring order, into the mailboxes of idle
+// slots of any group; `head` then tells the host that the ring entries are
+// free again.  A slot's own group admits the request at its next round end
+// (admit_online), so each group keeps its own round count and barrier.
+__device__ bool route_online(const PushArgs& a) {
+    const ServeQueue& q = a.queue;
+    long long head = *q.head;  // only this thread writes it
+    const long long tail = ld_acquire_sys(q.tail);
+    if (head >= tail) return false;
+    const long long head0 = head;
+    for (int t = 0; t < a.ntiles && head < tail; ++t) {
+        OnlineSlot& os = q.slot[t];
+        // the mailbox flag first: an owner that just admitted from it wrote
+        // the slot's state before clearing the flag
+        if (ld_volatile_i(&os.pending) != 0) continue;
+        __threadfence();
+        if (ld_volatile_i(&a.ts[t].done) != SLOT_IDLE) continue;
+        const volatile OnlineReq* rq = q.req + (head % q.cap);
+        OnlineReq m;
+        m.kind = rq->kind;
+        m.seed = rq->seed;
+        m.seed_caller = rq->seed_caller;
+        m.n_levels = rq->n_levels;
+        m.psi_off = rq->psi_off;
+        m.out64 = rq->out64;
+        m.theta = rq->theta;
+        m.r0 = rq->r0;
+        m.alpha = rq->alpha;
+        m.x_out = rq->x_out;
+        m.ticket = rq->ticket;
+        os.mail = m;
+        __threadfence();
+        *(volatile int*)&os.pending = 1;
+        ++head;
+    }
+    if (head == head0) return false;
+    __threadfence_system();
+    *q.head = head;
+    __threadfence_system();
+    return true;
+}
+
+// Thread 0 of a group's first block: the request in idle slot t's mailbox
+// (placed by route_online) becomes the slot's query from the next round of
+// this group on.
 template <typename T, int W>
 __device__ bool admit_online(const PushArgs& a, int t, int it) {
     const ServeQueue& q = a.queue;
-    const long long head = *q.head;  // only this thread writes it
-    if (head >= ld_acquire_sys(q.tail)) return false;
-    const volatile OnlineReq* rq = q.req + (head % q.cap);
+    OnlineSlot& os = q.slot[t];
+    if (ld_volatile_i(&os.pending) == 0) return false;
+    __threadfence();
+    const volatile OnlineReq* rq = &os.mail;
     const int k = rq->kind;
     const int seed = rq->seed;
-    OnlineSlot& os = q.slot[t];
     os.ticket = rq->ticket;
     os.x_out = rq->x_out;
     os.out64 = rq->out64;
@@ -1940,8 +1985,6 @@ __device__ bool admit_online(const PushArgs& a, int t, int it) {
     tp.n_levels = (k == KIND_HK) ? rq->n_levels : 0;
     tp.psi_tab = (k == KIND_HK) ? q.psi + rq->psi_off : nullptr;
     const double theta = rq->theta, r0 = rq->r0;
-    *q.head = head + 1;
-    __threadfence_system();
     // stamps keep growing within the slot: skip past the last query's
     ts.stamp = ts.stamp + max(it - ts.t0, 0) + 2;
     for (int i = 0; i < 3; ++i) ts.cand_cnt[i] = 0;
@@ -1970,6 +2013,8 @@ __device__ bool admit_online(const PushArgs& a, int t, int it) {
     os.admit_ns = globaltimer_ns();
     __threadfence();
     ts.done = SLOT_LIVE;
+    __threadfence();
+    *(volatile int*)&os.pending = 0;  // after the state: the reader checks the flag first
     return true;
 }
 
@@ -2340,7 +2385,7 @@ __global__ void __launch_bounds__(kThreads, (W == 1 && sizeof(T) == 4)   ? GDE_M
     if (online && blockIdx.x == 0 && threadIdx.x == 0) *a.queue.last_ns = globaltimer_ns();
     for (; it < a.round_budget; ++it) {
         // online server: block 0 decided to stop (stop flag, or idle) last round
-        if (online && ld_volatile_i(a.queue.quit) != 0) break;
+        if (online && ld_volatile_i(a.queue.gquit + gi.id) != 0) break;
         trace_point(a, it, TP_ITER);
         // ---- live tiles of this round (identical in every block) ----
         if (threadIdx.x == 0) { rs.any_check = 0; rs.any_idle = 0; rs.ndrain = 0; }
@@ -2542,6 +2587,7 @@ __global__ void __launch_bounds__(kThreads, (W == 1 && sizeof(T) == 4)   ? GDE_M
                     publish_online(a, rs.drain[k]);
                     a.ts[rs.drain[k]].done = SLOT_IDLE;  // admitted from the next round on
                 }
+                if (gi.id == 0 && route_online(a)) admitted = true;
                 if (rs.any_idle)
                     for (int t = 0; t < a.ntiles; ++t)
                         if (rs.idle[t] == 1 && admit_online<T, W>(a, t, it)) admitted = true;
@@ -2573,14 +2619,21 @@ __global__ void __launch_bounds__(kThreads, (W == 1 && sizeof(T) == 4)   ? GDE_M
                         ts.done = SLOT_DRAIN;
                     }
                 }
-                // leave on the stop flag, or after idle_ns with nothing live,
-                // draining or admitted (every slot is then idle: a later
-                // launch picks the ring up where this one left it)
-                const unsigned long long now = globaltimer_ns();
-                const bool busy = ntl > 0 || rs.ndrain > 0 || admitted;
-                if (busy) *a.queue.last_ns = now;
-                if (ld_relaxed_sys_i(a.queue.stop) != 0 || (!busy && now - *a.queue.last_ns > a.queue.idle_ns))
-                    *a.queue.quit = 1;
+                // Group 0 decides for the server: leave on the stop flag, or
+                // after idle_ns with nothing live, draining, in a mailbox or in
+                // the ring in any group (every slot is then idle: a later
+                // launch picks the ring up where this one left it).  Every
+                // group takes its copy of the decision before its barrier.
+                if (gi.id == 0) {
+                    const unsigned long long now = globaltimer_ns();
+                    bool busy = ntl > 0 || rs.ndrain > 0 || admitted || *a.queue.head < ld_acquire_sys(a.queue.tail);
+                    for (int t = 0; t < a.ntiles && !busy; ++t)
+                        busy = ld_volatile_i(&a.queue.slot[t].pending) != 0 || ld_volatile_i(&a.ts[t].done) != SLOT_IDLE;
+                    if (busy) *a.queue.last_ns = now;
+                    if (ld_relaxed_sys_i(a.queue.stop) != 0 || (!busy && now - *a.queue.last_ns > a.queue.idle_ns))
+                        *(volatile int*)a.queue.quit = 1;
+                }
+                a.queue.gquit[gi.id] = ld_volatile_i(a.queue.quit);
             }
         }
         trace_point(a, it, TP_SCAT_ENTER);

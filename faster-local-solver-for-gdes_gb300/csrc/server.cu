@@ -167,10 +167,11 @@ struct gde_server {
     // One launch: runs until the kernel leaves (idle or stop).  Slot stamps
     // continue from the last launch (the kernel's iteration count restarts).
     int launch_once() {
-        CK_RET(cudaMemsetAsync(a.bar, 0, sizeof(GridBarrier), stream));
+        CK_RET(cudaMemsetAsync(a.bar, 0, (size_t)std::max(a.groups, 1) * sizeof(GridBarrier), stream));
         CK_RET(cudaMemsetAsync(a.err, 0, sizeof(int), stream));
         CK_RET(cudaMemsetAsync(a.stats, 0, sizeof(LaunchStats), stream));
         CK_RET(cudaMemsetAsync(a.queue.quit, 0, sizeof(int), stream));
+        CK_RET(cudaMemsetAsync(a.queue.gquit, 0, (size_t)std::max(a.groups, 1) * sizeof(int), stream));
         cudaEvent_t e0, e1;
         cudaEventCreate(&e0);
         cudaEventCreate(&e1);
@@ -301,14 +302,25 @@ int gde_server_start(gde_ctx* ctx, gde_graph* G, const gde_params* p, int64_t ri
     a.ts = (TileState*)s->dalloc(S * sizeof(TileState));
     a.cs = (ColState*)s->dalloc(S * sizeof(ColState));
     a.stats = (LaunchStats*)s->dalloc(sizeof(LaunchStats));
-    a.bar = (GridBarrier*)s->dalloc(sizeof(GridBarrier));
+    // Slot groups, each behind its own barrier, as in gde_serve: the default
+    // is one group per slot for a PPR/Katz server and one per 8 slots for a
+    // server that takes heat-kernel queries (gde_params.groups overrides).
+    // Group 0 also reads the ring and places requests into idle slots of
+    // every group.
+    {
+        const int g_default = s->hk ? std::max(1, S / 8) : S;
+        a.groups = std::max(1, std::min(std::min(p->groups > 0 ? p->groups : g_default, S),
+                                        std::min(kMaxGroups, s->grid)));
+    }
+    a.bar = (GridBarrier*)s->dalloc((size_t)a.groups * sizeof(GridBarrier));
     a.err = (int*)s->dalloc(sizeof(int));
     ServeQueue& Q = a.queue;
     Q.quit = (int*)s->dalloc(sizeof(int));
+    Q.gquit = (int*)s->dalloc((size_t)a.groups * sizeof(int));
     Q.last_ns = (unsigned long long*)s->dalloc(sizeof(unsigned long long));
     Q.slot = (OnlineSlot*)s->dalloc(S * sizeof(OnlineSlot));
     bool ok = a.R && a.X && (!s->hk || a.R2) && a.P && a.cand && a.bsmall && a.blarge && a.mark && a.tp && a.ts &&
-              a.cs && a.stats && a.bar && a.err && Q.quit && Q.last_ns && Q.slot;
+              a.cs && a.stats && a.bar && a.err && Q.quit && Q.gquit && Q.last_ns && Q.slot;
     if (!ok) {
         int rc = s->fail(GDE_ENOMEM, "device memory exhausted (server slots)");
         s->free_all();

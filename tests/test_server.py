@@ -59,10 +59,15 @@ def _wait(srv, tickets, timeout_s=60.0):
     return out
 
 
-def test_submissions_while_running_equal_the_query_alone(cl):
+@pytest.mark.parametrize("slots,groups", [(4, 0), (8, 4), (6, 6)])
+def test_submissions_while_running_equal_the_query_alone(cl, slots, groups):
+    """Queries submitted while earlier ones run, in one launch: each equals the query alone.  With
+    several slot groups, group 0 places requests into the idle slots of every group, and each group
+    admits them at its own round boundary behind its own barrier."""
     import torch
     g, Gd = cl
-    srv = api.Server(Gd, prec="fp64", slots=4, tau=TAU, idle_ms=500.0)
+    srv = api.Server(Gd, prec="fp64", slots=slots, tau=TAU, idle_ms=500.0,
+                     tuning={"groups": groups} if groups else None)
     kinds, seeds, eps, alphas = _queries(g, 16, seed=41)
     rows = torch.full((16, g.n), float("nan"), dtype=torch.float64, device="cuda")
     torch.cuda.synchronize()
