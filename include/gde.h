@@ -224,7 +224,9 @@ int gde_serve_mixed(gde_ctx *ctx, gde_graph *g, const gde_params *p, int64_t nq,
  * precision p->prec, a ring of ring_capacity requests in pinned host memory,
  * and starts a host thread that keeps the push kernel running while there is
  * work: the kernel admits each submitted query into a free slot at a round
- * boundary, advances every live slot together, writes each finished query's
+ * boundary, advances the live slots in groups that each keep their own round
+ * and barrier (p->groups; default one per slot, or one per 8 slots when
+ * p->tau >= 1), writes each finished query's
  * solution row (as the reference returns it: Katz x[s] - 1, heat kernel
  * x / e^tau) into the caller's row, and publishes a completion record.
  * After idle_ms with nothing to do the kernel returns; the next submit
