@@ -1693,8 +1693,8 @@ __device__ void finish_round(const PushArgs& a, int t, int level, bool dense_nex
         // the next round's retire
         if (ts.front_cnt[par] == 0 || (hk_end && !a.serve)) {
             if (a.serve && a.queue.online) {
-                // online slot: its row is gathered by every block in this
-                // SCATTER; next round clears the slot and publishes the result
+                // online slot: its row is gathered by every block of its group
+                // in this SCATTER; next round clears the slot and publishes the result
                 const ColState& cs = a.cs[(int64_t)t * W];
                 OnlineSlot& os = a.queue.slot[t];
                 os.oper = cs.oper;
@@ -1703,7 +1703,7 @@ __device__ void finish_round(const PushArgs& a, int t, int level, bool dense_nex
                 ts.done = SLOT_DRAIN;
             } else if (a.serve) {
                 // served slot: the query's result is extracted and the slot
-                // cleared by every block in this SCATTER; admit next round
+                // cleared by every block of its group in this SCATTER; admit next round
                 const ColState& cs = a.cs[(int64_t)t * W];
                 const int q = ts.qid;
                 a.queue.oper[q] = cs.oper;
@@ -2021,7 +2021,8 @@ __device__ bool admit_online(const PushArgs& a, int t, int it) {
 // A finished online query's row, caller ids [beg, end): gathered through
 // the node permutation into the caller's row, x - c for a Kahan slab, with
 // the Katz x[s] -= 1 and the heat kernel's x / e^tau.  Read-only on the
-// slot: its vectors are cleared next round, after every block's gather.
+// slot: its vectors are cleared next round, after the gather of every block
+// of its group.
 template <typename T, int W>
 __device__ void gather_online_range(const PushArgs& a, int t, long long beg, long long end) {
     const ServeQueue& q = a.queue;
@@ -2062,8 +2063,8 @@ __device__ void clear_slot_range(const PushArgs& a, int t, long long beg, long l
     }
 }
 
-// Block 0, thread 0: a drained slot's completion record (its row was
-// gathered, by every block, in the previous round).
+// Thread 0 of the slot's group's first block: a drained slot's completion
+// record (its row was gathered, by the group's blocks, in the previous round).
 __device__ void publish_online(const PushArgs& a, int t) {
     const ServeQueue& q = a.queue;
     const OnlineSlot& os = q.slot[t];
@@ -2384,7 +2385,8 @@ __global__ void __launch_bounds__(kThreads, (W == 1 && sizeof(T) == 4)   ? GDE_M
     const int G = a.groups > 1 ? a.groups : 1;
     if (online && blockIdx.x == 0 && threadIdx.x == 0) *a.queue.last_ns = globaltimer_ns();
     for (; it < a.round_budget; ++it) {
-        // online server: block 0 decided to stop (stop flag, or idle) last round
+        // online server: group 0 decided to stop (stop flag, or idle), and this
+        // group took its copy of the decision before last round's barrier
         if (online && ld_volatile_i(a.queue.gquit + gi.id) != 0) break;
         trace_point(a, it, TP_ITER);
         // ---- live tiles of this round (identical in every block) ----
@@ -2535,7 +2537,7 @@ __global__ void __launch_bounds__(kThreads, (W == 1 && sizeof(T) == 4)   ? GDE_M
                     else retire_range<T, W>(a, rs.tiles[k], b, e);
                 }
             }
-            // online slots drained last round: every block an equal share of their nodes
+            // online slots drained last round: every block of the group an equal share of their nodes
             if (online && rs.ndrain > 0) {
                 block_share((long long)rs.ndrain * n, lo, hi, gi);
                 for (long long x = lo; x < hi;) {

@@ -9,10 +9,14 @@
 //
 //   submit  the host writes the request into a ring in pinned, mapped host
 //           memory and publishes it with a release store of `tail`;
-//   admit   block 0 of the kernel reads `tail` (acquire, system scope) each
-//           round and moves the next request into an idle slot;
+//   route   the slots run in groups with their own barriers; group 0's first
+//           block reads `tail` (acquire, system scope) each of its rounds and
+//           copies requests into the mailboxes of idle slots of any group;
+//   admit   each group moves a mailbox request into its idle slot at its own
+//           round boundary;
 //   finish  the slot's solution row is gathered into the caller's row (device
-//           memory or pinned host memory) by every block; next round the
+//           memory or pinned host memory) by the blocks of the slot's
+//           group; next round the
 //           slot's vectors are cleared and the completion record is published
 //           (release store of done_ticket), which gde_server_poll reads;
 //   idle    after idle_ms with nothing live, draining or admitted the kernel
